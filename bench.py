@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 path tracer on the random-spheres workload (the
+second benchmark configuration: 1920x1080, 128 spp, 488 spheres, max depth
+50, Russian roulette after depth 10, seeded synthetic scene).
+
+One step = one full render of the workload (all 128 frames) through the C
+ABI.  Prints one JSON line (rank 0).  `--impl reference` times the CPU
+restatement of the reference's device programs (the reference itself needs
+the OptiX 6 SDK and an OpenGL window, neither of which exists here) on a
+bounded sample of the same workload with all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "optix-path-tracer_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, PKG)
+
+WORKLOADS = {
+    # name: (generator, width, height, spp, render kwargs, description)
+    "spheres": ("random_spheres", 1920, 1080, 128, dict(max_depth=50, rr_depth=10),
+                "random spheres: 1920x1080, 128 spp, 488 spheres (ground r=1000, 22x22 grid, "
+                "3 large), gradient sky, max depth 50, RR after depth 10"),
+    "cornell": ("cornell_c1", 512, 512, 64, dict(max_depth=50, rr_depth=3),
+                "Cornell box: 512x512, 64 spp, 8 primitives (6 quads + 2 rotated boxes), "
+                "one area light, max depth 50, RR after depth 3"),
+    "heightfield": ("heightfield_scene", 1920, 1080, 256, dict(max_depth=50, rr_depth=10),
+                    "triangle heightfield: 1920x1080, 256 spp, 2,097,152 triangles, "
+                    "TS/AS/ON tiles, 2048x1024 HDR sky"),
+}
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_sample(scene, w, h, spp, kw, target_s, threads, max_stride=None):
+    """Times the CPU oracle on a strided pixel subset of the workload,
+    growing the sample until it takes about target_s seconds."""
+    sys.path.insert(0, ORACLE)
+    import oracle
+    o = oracle.Oracle(scene)
+    stride, frames = 4096, 4
+    while True:
+        acc, st = o.render(w, h, frames, pixel_stride=stride, threads=threads, **kw)
+        if st["seconds"] >= target_s or (stride == 1 and frames >= spp):
+            break
+        grow = max(1.5, min(8.0, target_s / max(st["seconds"], 1e-3)))
+        if frames < spp:
+            frames = min(spp, int(frames * grow) + 1)
+        else:
+            stride = max(1, int(stride / grow))
+    return st, stride, frames
+
+
+def run_reference(args, wl):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import ptgb
+    gen, w, h, spp, kw, desc = wl
+    scene = getattr(ptgb, gen)(w, h)
+    threads = os.cpu_count()
+    sys.path.insert(0, ORACLE)
+    import oracle
+    o = oracle.Oracle(scene)
+    # size one step to about 3 s of CPU work
+    st, stride, frames = cpu_sample(scene, w, h, spp, kw, 3.0, threads)
+    for _ in range(args.warmup):
+        o.render(w, h, frames, pixel_stride=stride, threads=threads, **kw)
+    secs, paths, rays = 0.0, 0, 0
+    for _ in range(args.steps):
+        _, s = o.render(w, h, frames, pixel_stride=stride, threads=threads, **kw)
+        secs += s["seconds"]
+        paths += s["paths"]
+        rays += s["ext_rays"] + s["shadow_rays"]
+    value = paths / secs
+    sample = f"every {stride}th pixel x {frames} of {spp} spp per step ({paths // args.steps} paths)"
+    line = {
+        "impl": "reference", "metric": "paths/s", "value": value, "unit": "paths/s",
+        "mrays_per_s": rays / secs / 1e6, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": desc, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "OptiX 6 + OpenGL reference cannot run here; CPU restatement of its device "
+                "programs (oracle/oracle.cpp) on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl):
+    import numpy as np
+    import torch
+    import ptgb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    gen, w, h, spp, kw, desc = wl
+    scene = getattr(ptgb, gen)(w, h)
+    # per-rank frames: rank r renders frames [r*spp, (r+1)*spp): weak scaling
+    frame0 = rank * spp
+    rend = ptgb.GpuRenderer(scene, device=local, timing=True)
+    prm = ptgb.GpuRenderer.params(w, h, spp, frame0=frame0, **kw)
+    acc = torch.zeros((h, w, 4), dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        rend.render(prm, acc.data_ptr())
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    dev_ms, paths, ext, shadow, stage = 0.0, 0, 0, 0, [0.0] * 5
+    launches, iters = 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()                      # evict L2 between steps
+        torch.cuda.synchronize()
+        rend.render(prm, acc.data_ptr())   # synchronous; device-timed inside
+        st = rend.stats()
+        dev_ms += st["render_ms"]
+        paths += st["paths"]
+        ext += st["ext_rays"]
+        shadow += st["shadow_rays"]
+        launches += st["kernel_launches"]
+        iters += st["iterations"]
+        stage = [a + b for a, b in zip(stage, st["stage_ms"])]
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_s = dev_ms / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s, wall, float(paths), float(ext + shadow)], device=f"cuda:{local}")
+        mx = t.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = t.clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        dev_s, wall = float(mx[0]), float(mx[1])
+        tot_paths, tot_rays = float(sm[2]), float(sm[3])
+    else:
+        tot_paths, tot_rays = float(paths), float(ext + shadow)
+    value = tot_paths / dev_s
+
+    # ---- end to end through the C ABI with host buffers: upload + BVH build
+    # (pt_commit) and render into pinned host memory with the D2H read
+    host_acc = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory()
+    host_np = host_acc.numpy()
+    lib = rend.lib
+    e2e_paths, e2e_t = 0, 0.0
+    for i in range(args.steps):
+        barrier()
+        t1 = time.perf_counter()
+        rend._c(lib.pt_commit(rend.ctx))
+        rend.render(prm, host_np)
+        e2e_t += time.perf_counter() - t1
+        e2e_paths += rend.stats()["paths"]
+    st = rend.stats()
+    h2d = int(st["bvh_bytes"]) + 64 * len(scene.materials)
+    d2h = w * h * 16
+
+    # ---- algorithmic bytes per ray from a counters pass (outside the timing)
+    cnt = ptgb.GpuRenderer(scene, device=local, counters=True)
+    cprm = ptgb.GpuRenderer.params(w, h, max(1, spp // 16), frame0=frame0, **kw)
+    cnt.render(cprm, acc.data_ptr())
+    cs = cnt.stats()
+    rays_c = cs["ext_rays"] + cs["shadow_rays"]
+    n_node = cs["node_fetches"] / rays_c
+    n_prim = cs["prim_tests"] / rays_c
+    b_ray = 32 + 16 + 80 * n_node + 48 * n_prim
+    cnt.close()
+    trace_ms = stage[1] + stage[3]
+    trace_launches = 2 * iters
+    achieved = (ext + shadow) * b_ray / (trace_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            tr = json.load(f).get(args.workload)
+        if tr:
+            traffic = tr["dram_bytes_per_ray"] * (ext + shadow) / trace_launches
+    except (OSError, ValueError, KeyError):
+        pass
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count()
+        cst, stride, frames = cpu_sample(scene, w, h, spp, kw, args.cpu_seconds, threads)
+        cpu = {"value": cst["paths"] / cst["seconds"], "unit": "paths/s", "cores": threads,
+               "kind": "port",
+               "sample": f"every {stride}th pixel x {frames} spp of the same workload "
+                         f"({cst['paths']} paths, {cst['seconds']:.1f} s)",
+               "mrays_per_s": (cst["ext_rays"] + cst["shadow_rays"]) / cst["seconds"] / 1e6}
+
+    if rank == 0:
+        line = {
+            "metric": "paths/s", "value": value, "unit": "paths/s",
+            "mrays_per_s": tot_rays / dev_s / 1e6,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "frames_per_rank": spp,
+                       "l2": "flushed between steps (256 MiB write); per-step working set "
+                             "(path state + per-path results) exceeds L2",
+                       "parallelism": f"replicas{world}" if world > 1 else "single"},
+            "e2e": {"value": e2e_paths / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "includes": "pt_commit (scene upload + BVH8 build) + pt_render into pinned "
+                                "host memory"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_trace + k_trace_shadow (BVH8 closest hit)",
+                         "peak_source": peak_kind,
+                         "bytes_per_ray": b_ray, "nodes_per_ray": n_node,
+                         "prims_per_ray": n_prim,
+                         "avg_launch_ms": trace_ms / trace_launches,
+                         "rays_per_launch": (ext + shadow) / trace_launches},
+            "stage_ms_per_step": {k: v / args.steps for k, v in
+                                  zip(["generate", "trace", "shade", "shadow_trace", "finish"],
+                                      stage)},
+            "wall_s": wall,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    rend.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

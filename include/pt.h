@@ -1,0 +1,201 @@
+/*
+ * pt.h - C ABI of the GB300 path tracer (libpt.so).
+ *
+ * This is the drop-in boundary for the hot path of joaovbs96/OptiX-Path-Tracer:
+ * everything the reference's host code hands to OptiX (context variables,
+ * geometry instances, materials, light callables, miss programs, the launch)
+ * crosses this interface instead.  The C++ classes of host_includes/ are
+ * re-created on top of it in pt_scene.hpp.
+ *
+ * Conventions
+ *  - Every function returns PT_OK (0) or a negative PT_E* status; no C++
+ *    exception crosses the ABI.  pt_last_error() describes the last failure.
+ *  - The library copies every scene input at the call; the caller keeps
+ *    ownership of its arrays and of output buffers.
+ *  - One context per host thread; calls on a context are serialised by the
+ *    caller.  GPU work is issued on the stream passed to pt_render (a
+ *    cudaStream_t given as void*, NULL = the legacy default stream).
+ *  - Output pointers may be host or device memory (detected per call).
+ *  - Transforms are affine 3x4 object-to-world matrices, row major
+ *    (m[0..3] is the first row); NULL means identity.
+ */
+#ifndef PT_H
+#define PT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define PT_API __declspec(dllexport)
+#else
+#define PT_API __attribute__((visibility("default")))
+#endif
+
+enum pt_status {
+  PT_OK = 0,
+  PT_EINVAL = -1,   /* invalid argument or scene state */
+  PT_ENOMEM = -2,   /* host or device allocation failed */
+  PT_ECUDA = -3,    /* CUDA runtime error */
+  PT_ETIMEOUT = -4, /* a bounded device wait ran out */
+  PT_EQUEUE = -5,   /* a work queue overflowed */
+  PT_ESTATE = -6    /* call not valid in the current state (e.g. not committed) */
+};
+
+enum pt_axis { PT_X_AXIS = 0, PT_Y_AXIS = 1, PT_Z_AXIS = 2 }; /* programs/common.hpp:28 */
+
+enum pt_miss_kind { /* host_includes/programs.hpp:32 Miss_Programs */
+  PT_MISS_GRADIENT = 0,
+  PT_MISS_CONSTANT = 1,
+  PT_MISS_HDR = 2,  /* environmental_mapping, programs/miss.cu:64-95 */
+  PT_MISS_IMG = 3   /* image_background, programs/miss.cu:51-59 */
+};
+
+enum pt_mode {
+  PT_MODE_REF = 0,        /* statement-for-statement semantics of programs/ */
+  PT_MODE_CONSISTENT = 1  /* local shading frames, matching pdfs, env NEE */
+};
+
+typedef struct pt_context pt_context;
+
+typedef struct pt_options {
+  int device;          /* CUDA device ordinal */
+  int path_slots;      /* wavefront path-state slots; 0 = automatic */
+  int enable_counters; /* count BVH node fetches and primitive tests */
+  int enable_timing;   /* per-stage device times (CUDA events in the graph) */
+} pt_options;
+
+typedef struct pt_render_params {
+  int width, height;   /* launch size (programs/raygen.cu:22-23) */
+  int spp;             /* frames to accumulate in this call */
+  int frame0;          /* first frame index ("frame", main.cpp:264) */
+  int max_depth;       /* "maxDepth", main.cpp:63 (default 50) */
+  int rr_enable;       /* "russian", main.cpp:62 */
+  int rr_depth;        /* RR starts when depth > rr_depth (raygen.cu:112: 10) */
+  int mode;            /* pt_mode */
+  int guide;           /* learned sampling guide: 0 = off */
+} pt_render_params;
+
+typedef struct pt_stats {
+  uint64_t paths;          /* paths completed by the last pt_render */
+  uint64_t ext_rays;       /* extension rays traced */
+  uint64_t shadow_rays;    /* shadow rays traced */
+  uint64_t node_fetches;   /* BVH8 nodes fetched (counters enabled only) */
+  uint64_t prim_tests;     /* primitive tests (counters enabled only) */
+  uint64_t bvh_nodes;      /* BVH8 node count of the committed scene */
+  uint64_t bvh_bytes;      /* bytes of nodes + primitive records */
+  int bvh_depth;           /* depth of the BVH8 */
+  double build_ms;         /* last pt_commit, host wall time */
+  double render_ms;        /* last pt_render, device time */
+  uint64_t iterations;     /* wavefront iterations of the last render */
+  uint64_t kernel_launches;/* kernels launched by the last render */
+  /* device time per stage (enable_timing): generate, trace, shade,
+     shadow trace, finish + queue advance */
+  double stage_ms[5];
+} pt_stats;
+
+/* ---- context (replaces optix::Context, host_includes/host_common.hpp:21-45) */
+PT_API int pt_context_create(const pt_options* opt, pt_context** out);
+PT_API int pt_context_destroy(pt_context* ctx);
+PT_API const char* pt_last_error(pt_context* ctx);
+PT_API const char* pt_version(void);
+
+/* ---- materials (host_includes/materials.hpp) ----------------------------
+ * Colours are the constant textures the reference passes
+ * (Constant_Texture, host_includes/textures.hpp:20-37).  Each returns the
+ * material id in *id. */
+/* Lambertian(Texture*)                         materials.hpp:43-58 */
+PT_API int pt_material_lambertian(pt_context* ctx, const float albedo[3], uint32_t* id);
+/* Metal(Texture*, fuzz)                        materials.hpp:61-78 */
+PT_API int pt_material_metal(pt_context* ctx, const float albedo[3], float fuzz, uint32_t* id);
+/* Dielectric(base, extinction, ref_idx, density) materials.hpp:81-103 */
+PT_API int pt_material_dielectric(pt_context* ctx, const float base[3], const float extinction[3],
+                                  float ref_idx, float density, uint32_t* id);
+/* Diffuse_Light(Texture*)                      materials.hpp:106-122 */
+PT_API int pt_material_diffuse_light(pt_context* ctx, const float emission[3], uint32_t* id);
+/* Oren_Nayar(Texture*, R) with the sigma->A,B mapping of materials.hpp:191-198 */
+PT_API int pt_material_oren_nayar(pt_context* ctx, const float albedo[3], float roughness,
+                                  uint32_t* id);
+/* Torrance_Sparrow(Texture*, nu, nv), alpha = max(r,1e-3)^2, materials.hpp:218-238 */
+PT_API int pt_material_torrance_sparrow(pt_context* ctx, const float color[3], float nu, float nv,
+                                        uint32_t* id);
+/* Ashikhmin_Shirley(diffuse, specular, nu, nv), nu,nv >= 1, materials.hpp:162-179 */
+PT_API int pt_material_ashikhmin_shirley(pt_context* ctx, const float diffuse[3],
+                                         const float specular[3], float nu, float nv,
+                                         uint32_t* id);
+
+/* ---- geometry (host_includes/hitables.hpp, mesh.hpp) ---------------------
+ * Primitive ids are assigned in call order (a mesh takes nt consecutive ids);
+ * equal hit distances resolve to the lower id. */
+/* Sphere(center, radius, BRDF*)                hitables.hpp:89-128 */
+PT_API int pt_add_sphere(pt_context* ctx, const float center[3], float radius, uint32_t material,
+                         const float xform[12], uint32_t* prim_id);
+/* AARect(a0,a1,b0,b1,k,flip,axis,BRDF*)        hitables.hpp:210-270 */
+PT_API int pt_add_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k, int flip,
+                       int axis, uint32_t material, const float xform[12], uint32_t* prim_id);
+/* Box(p0, p1, BRDF*)                           hitables.hpp:273-316 */
+PT_API int pt_add_box(pt_context* ctx, const float p0[3], const float p1[3], uint32_t material,
+                      const float xform[12], uint32_t* prim_id);
+/* Mesh(file, folder, BRDF*) after loading: indexed triangles with optional
+ * per-vertex normals and uvs and a per-triangle material (mesh.hpp:49-204).
+ * mat_per_tri may be NULL (then every triangle uses `material`). */
+PT_API int pt_add_mesh(pt_context* ctx, const float* verts, size_t nv, const uint32_t* idx,
+                       size_t nt, const uint32_t* mat_per_tri, uint32_t material,
+                       const float* normals, const float* uvs, const float xform[12],
+                       uint32_t* first_prim_id);
+
+/* ---- lights (host_includes/pdfs.hpp + Light_Sampler, host_common.hpp:65-68) */
+/* Rectangle_PDF(a0,a1,b0,b1,k,axis) + emission  pdfs.hpp:17-80 */
+PT_API int pt_add_light_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k,
+                             int axis, const float emission[3]);
+/* Sphere_PDF(center, radius) + emission         pdfs.hpp:82-109 */
+PT_API int pt_add_light_sphere(pt_context* ctx, const float center[3], float radius,
+                               const float emission[3]);
+
+/* ---- miss programs (setMissProgram, host_includes/programs.hpp:32-92) -- */
+PT_API int pt_set_env_gradient(pt_context* ctx, const float c1[3], const float c2[3]);
+PT_API int pt_set_env_constant(pt_context* ctx, const float c[3]);
+/* HDR_Texture(file) / Image_Texture(file) after loading: RGBA float w*h,
+ * row 0 at v = 0, bilinear with repeat wrap.  kind = PT_MISS_HDR or PT_MISS_IMG. */
+PT_API int pt_set_env_map(pt_context* ctx, int kind, const float* rgba, int w, int h,
+                          int spherical);
+
+/* ---- camera (Camera(...).set(Context&), host_includes/camera.hpp:13-51) */
+PT_API int pt_set_camera(pt_context* ctx, const float lookfrom[3], const float lookat[3],
+                         const float vup[3], float vfov_deg, float aspect, float aperture,
+                         float focus_dist, float t0, float t1);
+
+/* ---- build: BVH8 over all primitives (replaces Trbvh) -------------------- */
+PT_API int pt_commit(pt_context* ctx);
+
+/* ---- render (renderFrame / Context::launch, main.cpp:26-39,264) ----------
+ * Accumulates frames frame0 .. frame0+spp-1 into accum_rgba (W*H float4,
+ * y-flipped as programs/raygen.cu:153; zeroed first when frame0 == 0). */
+PT_API int pt_render(pt_context* ctx, const pt_render_params* params, float* accum_rgba,
+                     void* stream);
+
+/* Per-path colour of one frame (W*H*3 floats, row y*W+x, not flipped): the
+ * value renderPixel adds to the accumulator, for parity checks. */
+PT_API int pt_render_paths(pt_context* ctx, const pt_render_params* params, float* out_rgb,
+                           void* stream);
+
+/* First hit of the camera rays of frame `frame`: primitive id (UINT32_MAX on
+ * a miss), material id and t, each W*H, row y*W+x. */
+PT_API int pt_trace_first_hits(pt_context* ctx, int width, int height, int frame, uint32_t* prim,
+                               uint32_t* mat, float* t, void* stream);
+
+/* Display conversion of programs/raygen.cu:136-146: sqrt(acc/(frame+1)),
+ * clamp, x255.99 -> RGBA8 (W*H*4 bytes). */
+PT_API int pt_resolve_display(pt_context* ctx, const float* accum_rgba, int width, int height,
+                              int frame, uint8_t* rgba8, void* stream);
+
+PT_API int pt_get_stats(pt_context* ctx, pt_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_H */

@@ -1,0 +1,1007 @@
+/*
+ * pt_api.cu - implementation of the C ABI declared in include/pt.h.
+ *
+ * Host side of the drop-in boundary: it takes over what the reference's
+ * host_includes/ hand to OptiX (materials.hpp, hitables.hpp, mesh.hpp,
+ * pdfs.hpp, programs.hpp, camera.hpp, transforms.hpp), keeps a flat scene,
+ * builds the BVH8 at pt_commit and drives the wavefront kernels in
+ * pt_render (the per-sample Context::launch of main.cpp:26-39,264).
+ */
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pt.h"
+#include "bvh_build.h"
+#include "pt_internal.h"
+#include "ptmath.h"
+
+namespace {
+
+const float PI_F = 3.141592654f;
+
+struct HostPrim {
+  int type, axis, flip, xform;
+  uint32_t material;
+  float f[9];
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const T* h, size_t count, cudaStream_t st) {
+    cudaError_t e = ensure(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct pt_context {
+  int device = 0;
+  std::string err;
+  pt_options opt{};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // ---- host scene
+  std::vector<GpuMaterial> mats;
+  std::vector<HostPrim> prims;
+  std::vector<float> xforms;  // 24 floats each: m rows, inv rows (float4-padded 3x4)
+  std::vector<uint4> tri_attr;
+  std::vector<float> normals, uvs;
+  std::vector<GpuLight> lights;
+  GpuMiss miss{};
+  std::vector<float4> env;
+  GpuCamera cam{};
+  bool committed = false;
+  // ---- device scene
+  DevBuf<uint4> d_nodes;
+  DevBuf<float4> d_prims, d_xforms, d_env;
+  DevBuf<GpuMaterial> d_mats;
+  DevBuf<GpuLight> d_lights;
+  DevBuf<uint4> d_tri_attr;
+  DevBuf<float> d_normals, d_uvs;
+  DevScene scene{};
+  int bvh_depth = 0;
+  size_t bvh_nodes = 0;
+  // ---- wavefront state
+  int slots = 0;
+  WaveState W{};
+  DevBuf<float4> d_slot_f4;   // 10 float4 arrays
+  DevBuf<uint4> d_st;
+  DevBuf<uint32_t> d_queues;  // 4 queues
+  DevBuf<WaveCounters> d_ctr;
+  DevBuf<WaveCtl> d_ctl;
+  DevBuf<float4> d_results;
+  DevBuf<float4> d_acc;
+  DevBuf<float> d_tmp;
+  DevBuf<uint32_t> d_tmpu;
+  WaveCounters* h_ctr = nullptr;  // pinned
+  WaveCtl* h_ctl = nullptr;       // pinned
+  cudaGraphExec_t graph = nullptr;
+  bool graph_counters = false;
+  bool graph_timing = false;
+  std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
+  bool wave_dirty = false;  // free-slot ring must be rebuilt (a render failed)
+  int max_stack = 0;
+  int trace_grid = 0, shade_grid = 0;
+  pt_stats stats{};
+};
+
+static int fail(pt_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+static int cuda_fail(pt_context* ctx, cudaError_t e, const char* where) {
+  return fail(ctx, PT_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                          \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+// ----------------------------------------------------------------- helpers --
+static void affine_inverse(const float* m, float* out) {
+  // same expression as the oracle: adjugate in double, rounded once
+  double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9],
+         i = m[10];
+  double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+  double det = a * A + b * B + c * C;
+  double inv_det = 1.0 / det;
+  double r[9] = {A * inv_det, -(b * i - c * h) * inv_det, (b * f - c * e) * inv_det,
+                 B * inv_det, (a * i - c * g) * inv_det, -(a * f - c * d) * inv_det,
+                 C * inv_det, -(a * h - b * g) * inv_det, (a * e - b * d) * inv_det};
+  double tx = m[3], ty = m[7], tz = m[11];
+  for (int row = 0; row < 3; row++) {
+    out[row * 4 + 0] = (float)r[row * 3 + 0];
+    out[row * 4 + 1] = (float)r[row * 3 + 1];
+    out[row * 4 + 2] = (float)r[row * 3 + 2];
+    out[row * 4 + 3] = (float)(-(r[row * 3 + 0] * tx + r[row * 3 + 1] * ty + r[row * 3 + 2] * tz));
+  }
+}
+
+static bool affine_ok(const float* m) {
+  double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9],
+         i = m[10];
+  double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+  for (int k = 0; k < 12; k++)
+    if (!std::isfinite(m[k])) return false;
+  return std::isfinite(det) && std::fabs(det) > 1e-30;
+}
+
+static int add_xform(pt_context* ctx, const float* x) {
+  if (!x) return -1;
+  float inv[12];
+  affine_inverse(x, inv);
+  for (int k = 0; k < 12; k++) ctx->xforms.push_back(x[k]);
+  for (int k = 0; k < 12; k++) ctx->xforms.push_back(inv[k]);
+  return (int)(ctx->xforms.size() / 24) - 1;
+}
+
+static inline void xpoint_h(const float* m, const float* p, float* o) {
+  o[0] = m[0] * p[0] + m[1] * p[1] + m[2] * p[2] + m[3];
+  o[1] = m[4] * p[0] + m[5] * p[1] + m[6] * p[2] + m[7];
+  o[2] = m[8] * p[0] + m[9] * p[1] + m[10] * p[2] + m[11];
+}
+
+static bool finite3(const float* v) {
+  return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
+}
+
+static bool is_device_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// World-space AABB of a primitive, padded so that rounding in the primitive
+// tests can never place a reported hit outside its box.
+static pt::Box prim_box(const pt_context* ctx, const HostPrim& p) {
+  float lo[3], hi[3];
+  const float* f = p.f;
+  if (p.type == PT_PRIM_TRIANGLE) {
+    for (int a = 0; a < 3; a++) {
+      lo[a] = fminf(fminf(f[a], f[3 + a]), f[6 + a]);
+      hi[a] = fmaxf(fmaxf(f[a], f[3 + a]), f[6 + a]);
+    }
+  } else if (p.type == PT_PRIM_SPHERE) {
+    for (int a = 0; a < 3; a++) {
+      lo[a] = f[a] - f[3];
+      hi[a] = f[a] + f[3];
+    }
+  } else if (p.type == PT_PRIM_RECT) {
+    int ka = p.axis, ia = (p.axis == 0) ? 1 : 0, ib = (p.axis == 2) ? 1 : 2;
+    lo[ka] = hi[ka] = f[4];
+    lo[ia] = f[0];
+    hi[ia] = f[1];
+    lo[ib] = f[2];
+    hi[ib] = f[3];
+  } else {
+    for (int a = 0; a < 3; a++) {
+      lo[a] = f[a];
+      hi[a] = f[3 + a];
+    }
+  }
+  if (p.xform >= 0) {
+    const float* M = &ctx->xforms[(size_t)p.xform * 24];
+    float nlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int c = 0; c < 8; c++) {
+      float q[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};
+      float w[3];
+      xpoint_h(M, q, w);
+      for (int a = 0; a < 3; a++) {
+        nlo[a] = fminf(nlo[a], w[a]);
+        nhi[a] = fmaxf(nhi[a], w[a]);
+      }
+    }
+    for (int a = 0; a < 3; a++) {
+      lo[a] = nlo[a];
+      hi[a] = nhi[a];
+    }
+  }
+  pt::Box b;
+  for (int a = 0; a < 3; a++) {
+    float mag = fmaxf(1.0f, fmaxf(fabsf(lo[a]), fabsf(hi[a])));
+    float pad = mag * 9.5367431640625e-07f;  // 2^-20 relative
+    if (p.xform >= 0) pad *= 16.f;
+    b.lo[a] = lo[a] - pad;
+    b.hi[a] = hi[a] + pad;
+  }
+  return b;
+}
+
+// ====================================================================== ABI ==
+extern "C" {
+
+PT_API const char* pt_version(void) { return "gb300-pathtracer 0.1 (sm_103a)"; }
+
+PT_API const char* pt_last_error(pt_context* ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+PT_API int pt_context_create(const pt_options* opt, pt_context** out) {
+  if (!out) return PT_EINVAL;
+  *out = nullptr;
+  pt_context* ctx = new (std::nothrow) pt_context();
+  if (!ctx) return PT_ENOMEM;
+  if (opt) ctx->opt = *opt;
+  ctx->device = opt ? opt->device : 0;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_ctr, sizeof(WaveCounters));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_ctl, sizeof(WaveCtl));
+  if (e != cudaSuccess) {
+    int rc = (e == cudaErrorMemoryAllocation) ? PT_ENOMEM : PT_ECUDA;
+    delete ctx;
+    return rc;
+  }
+  ctx->miss.type = PT_MISS_CONSTANT;
+  *out = ctx;
+  return PT_OK;
+}
+
+PT_API int pt_context_destroy(pt_context* ctx) {
+  if (!ctx) return PT_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
+  ctx->d_nodes.release();
+  ctx->d_prims.release();
+  ctx->d_xforms.release();
+  ctx->d_env.release();
+  ctx->d_mats.release();
+  ctx->d_lights.release();
+  ctx->d_tri_attr.release();
+  ctx->d_normals.release();
+  ctx->d_uvs.release();
+  ctx->d_slot_f4.release();
+  ctx->d_st.release();
+  ctx->d_queues.release();
+  ctx->d_ctr.release();
+  ctx->d_ctl.release();
+  ctx->d_results.release();
+  ctx->d_acc.release();
+  ctx->d_tmp.release();
+  ctx->d_tmpu.release();
+  if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+  if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return PT_OK;
+}
+
+// ---------------------------------------------------------------- materials
+static int add_material(pt_context* ctx, int type, const float* c0, const float* c1, float p0,
+                        float p1, uint32_t* id) {
+  if (!ctx || !id) return fail(ctx, PT_EINVAL, "null argument");
+  if (!finite3(c0) || (c1 && !finite3(c1)) || !std::isfinite(p0) || !std::isfinite(p1))
+    return fail(ctx, PT_EINVAL, "material parameters must be finite");
+  GpuMaterial m;
+  memset(&m, 0, sizeof(m));
+  m.type = type;
+  m.c0x = c0[0];
+  m.c0y = c0[1];
+  m.c0z = c0[2];
+  if (c1) {
+    m.c1x = c1[0];
+    m.c1y = c1[1];
+    m.c1z = c1[2];
+  }
+  m.p0 = p0;
+  m.p1 = p1;
+  ctx->mats.push_back(m);
+  ctx->committed = false;
+  *id = (uint32_t)ctx->mats.size() - 1;
+  return PT_OK;
+}
+
+PT_API int pt_material_lambertian(pt_context* ctx, const float albedo[3], uint32_t* id) {
+  return add_material(ctx, PT_MAT_LAMBERTIAN, albedo, nullptr, 0.f, 0.f, id);
+}
+PT_API int pt_material_metal(pt_context* ctx, const float albedo[3], float fuzz, uint32_t* id) {
+  return add_material(ctx, PT_MAT_METAL, albedo, nullptr, fuzz, 0.f, id);
+}
+PT_API int pt_material_dielectric(pt_context* ctx, const float base[3], const float extinction[3],
+                                  float ref_idx, float density, uint32_t* id) {
+  if (ctx && !(ref_idx > 0.f)) return fail(ctx, PT_EINVAL, "ref_idx must be > 0");
+  return add_material(ctx, PT_MAT_DIELECTRIC, base, extinction, ref_idx, density, id);
+}
+PT_API int pt_material_diffuse_light(pt_context* ctx, const float emission[3], uint32_t* id) {
+  return add_material(ctx, PT_MAT_DIFFUSE_LIGHT, emission, nullptr, 0.f, 0.f, id);
+}
+PT_API int pt_material_oren_nayar(pt_context* ctx, const float albedo[3], float roughness,
+                                  uint32_t* id) {
+  // host_includes/materials.hpp:192-198
+  float R = roughness;
+  float sigma = (0.f > (1.f < R ? 1.f : R)) ? 0.f : (1.f < R ? 1.f : R);  // saturate
+  float div = 1.f / (PI_F + ((3.f * PI_F - 4.f) / 6.f) * sigma);
+  return add_material(ctx, PT_MAT_OREN_NAYAR, albedo, nullptr, 1.0f * div, sigma * div, id);
+}
+PT_API int pt_material_torrance_sparrow(pt_context* ctx, const float color[3], float nu, float nv,
+                                        uint32_t* id) {
+  // host_includes/materials.hpp:235-238
+  float R0 = fmaxf(nu, 1e-3f), R1 = fmaxf(nv, 1e-3f);
+  return add_material(ctx, PT_MAT_TORRANCE_SPARROW, color, nullptr, R0 * R0, R1 * R1, id);
+}
+PT_API int pt_material_ashikhmin_shirley(pt_context* ctx, const float diffuse[3],
+                                         const float specular[3], float nu, float nv,
+                                         uint32_t* id) {
+  if (ctx && !specular) return fail(ctx, PT_EINVAL, "specular colour required");
+  // host_includes/materials.hpp:173-174
+  return add_material(ctx, PT_MAT_ASHIKHMIN_SHIRLEY, diffuse, specular, fmaxf(1.f, nu),
+                      fmaxf(1.f, nv), id);
+}
+
+// ----------------------------------------------------------------- geometry
+static int push_prim(pt_context* ctx, HostPrim& p, const float* xform, uint32_t* prim_id) {
+  if (p.material >= ctx->mats.size()) return fail(ctx, PT_EINVAL, "unknown material id");
+  if (xform && !affine_ok(xform)) return fail(ctx, PT_EINVAL, "transform is singular or not finite");
+  p.xform = add_xform(ctx, xform);
+  ctx->prims.push_back(p);
+  ctx->tri_attr.push_back(make_uint4(0, 0, 0, 0));
+  ctx->committed = false;
+  if (prim_id) *prim_id = (uint32_t)ctx->prims.size() - 1;
+  return PT_OK;
+}
+
+PT_API int pt_add_sphere(pt_context* ctx, const float center[3], float radius, uint32_t material,
+                         const float xform[12], uint32_t* prim_id) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(center) || !std::isfinite(radius) || !(radius > 0.f))
+    return fail(ctx, PT_EINVAL, "sphere needs a finite centre and radius > 0");
+  HostPrim p;
+  memset(&p, 0, sizeof(p));
+  p.type = PT_PRIM_SPHERE;
+  p.material = material;
+  p.f[0] = center[0];
+  p.f[1] = center[1];
+  p.f[2] = center[2];
+  p.f[3] = radius;
+  return push_prim(ctx, p, xform, prim_id);
+}
+
+PT_API int pt_add_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k, int flip,
+                       int axis, uint32_t material, const float xform[12], uint32_t* prim_id) {
+  if (!ctx) return PT_EINVAL;
+  if (axis < 0 || axis > 2) return fail(ctx, PT_EINVAL, "invalid axis");
+  float v[5] = {a0, a1, b0, b1, k};
+  for (float x : v)
+    if (!std::isfinite(x)) return fail(ctx, PT_EINVAL, "rect bounds must be finite");
+  if (!(a1 >= a0) || !(b1 >= b0)) return fail(ctx, PT_EINVAL, "rect needs a0 <= a1, b0 <= b1");
+  HostPrim p;
+  memset(&p, 0, sizeof(p));
+  p.type = PT_PRIM_RECT;
+  p.axis = axis;
+  p.flip = flip ? 1 : 0;
+  p.material = material;
+  for (int i = 0; i < 5; i++) p.f[i] = v[i];
+  return push_prim(ctx, p, xform, prim_id);
+}
+
+PT_API int pt_add_box(pt_context* ctx, const float p0[3], const float p1[3], uint32_t material,
+                      const float xform[12], uint32_t* prim_id) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(p0) || !finite3(p1)) return fail(ctx, PT_EINVAL, "box corners must be finite");
+  HostPrim p;
+  memset(&p, 0, sizeof(p));
+  p.type = PT_PRIM_BOX;
+  p.material = material;
+  for (int i = 0; i < 3; i++) {
+    p.f[i] = p0[i];
+    p.f[3 + i] = p1[i];
+  }
+  return push_prim(ctx, p, xform, prim_id);
+}
+
+PT_API int pt_add_mesh(pt_context* ctx, const float* verts, size_t nv, const uint32_t* idx,
+                       size_t nt, const uint32_t* mat_per_tri, uint32_t material,
+                       const float* normals, const float* uvs, const float xform[12],
+                       uint32_t* first_prim_id) {
+  if (!ctx) return PT_EINVAL;
+  if (!verts || !idx || nv == 0 || nt == 0) return fail(ctx, PT_EINVAL, "empty mesh");
+  if (xform && !affine_ok(xform)) return fail(ctx, PT_EINVAL, "transform is singular or not finite");
+  if (!mat_per_tri && material >= ctx->mats.size())
+    return fail(ctx, PT_EINVAL, "unknown material id");
+  for (size_t t = 0; t < nt; t++) {
+    for (int k = 0; k < 3; k++)
+      if (idx[3 * t + k] >= nv) return fail(ctx, PT_EINVAL, "mesh index out of range");
+    if (mat_per_tri && mat_per_tri[t] >= ctx->mats.size())
+      return fail(ctx, PT_EINVAL, "unknown per-triangle material id");
+  }
+  for (size_t i = 0; i < 3 * nv; i++)
+    if (!std::isfinite(verts[i])) return fail(ctx, PT_EINVAL, "mesh vertices must be finite");
+  // flatten into world space (the oracle flattens the same way)
+  std::vector<float> wv(3 * nv);
+  float inv[12];
+  if (xform) affine_inverse(xform, inv);
+  for (size_t i = 0; i < nv; i++) {
+    if (xform) xpoint_h(xform, verts + 3 * i, &wv[3 * i]);
+    else memcpy(&wv[3 * i], verts + 3 * i, 12);
+  }
+  // attribute vertices: normals and uvs share one index space (the two
+  // arrays always hold the same number of vertices)
+  size_t nattr = ctx->normals.size() / 3;
+  uint32_t abase = (uint32_t)nattr;
+  uint32_t flags = (normals ? 1u : 0u) | (uvs ? 2u : 0u);
+  if (normals || uvs) {
+    ctx->normals.resize(3 * (nattr + nv), 0.f);
+    ctx->uvs.resize(2 * (nattr + nv), 0.f);
+    for (size_t i = 0; i < nv; i++) {
+      if (normals) {
+        const float* n = normals + 3 * i;
+        float* o = &ctx->normals[3 * (nattr + i)];
+        if (xform) {  // transpose of the inverse (the oracle's xnormal)
+          o[0] = inv[0] * n[0] + inv[4] * n[1] + inv[8] * n[2];
+          o[1] = inv[1] * n[0] + inv[5] * n[1] + inv[9] * n[2];
+          o[2] = inv[2] * n[0] + inv[6] * n[1] + inv[10] * n[2];
+        } else {
+          o[0] = n[0];
+          o[1] = n[1];
+          o[2] = n[2];
+        }
+      }
+      if (uvs) {
+        ctx->uvs[2 * (nattr + i)] = uvs[2 * i];
+        ctx->uvs[2 * (nattr + i) + 1] = uvs[2 * i + 1];
+      }
+    }
+  }
+  uint32_t first = (uint32_t)ctx->prims.size();
+  ctx->prims.reserve(ctx->prims.size() + nt);
+  ctx->tri_attr.reserve(ctx->tri_attr.size() + nt);
+  for (size_t t = 0; t < nt; t++) {
+    HostPrim p;
+    memset(&p, 0, sizeof(p));
+    p.type = PT_PRIM_TRIANGLE;
+    p.xform = -1;
+    p.material = mat_per_tri ? mat_per_tri[t] : material;
+    for (int k = 0; k < 3; k++) memcpy(&p.f[3 * k], &wv[3 * idx[3 * t + k]], 12);
+    ctx->prims.push_back(p);
+    ctx->tri_attr.push_back(make_uint4(abase + idx[3 * t], abase + idx[3 * t + 1],
+                                       abase + idx[3 * t + 2], flags));
+  }
+  ctx->committed = false;
+  if (first_prim_id) *first_prim_id = first;
+  return PT_OK;
+}
+
+// ------------------------------------------------------------------- lights
+PT_API int pt_add_light_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k,
+                             int axis, const float emission[3]) {
+  if (!ctx) return PT_EINVAL;
+  if (axis < 0 || axis > 2 || !finite3(emission)) return fail(ctx, PT_EINVAL, "invalid light");
+  GpuLight L;
+  memset(&L, 0, sizeof(L));
+  L.type = PT_LIGHT_RECT;
+  L.axis = axis;
+  L.a0 = a0;
+  L.a1 = a1;
+  L.b0 = b0;
+  L.b1 = b1;
+  L.k = k;
+  L.ex = emission[0];
+  L.ey = emission[1];
+  L.ez = emission[2];
+  ctx->lights.push_back(L);
+  ctx->committed = false;
+  return PT_OK;
+}
+
+PT_API int pt_add_light_sphere(pt_context* ctx, const float center[3], float radius,
+                               const float emission[3]) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(center) || !(radius > 0.f) || !finite3(emission))
+    return fail(ctx, PT_EINVAL, "invalid light");
+  GpuLight L;
+  memset(&L, 0, sizeof(L));
+  L.type = PT_LIGHT_SPHERE;
+  L.cx = center[0];
+  L.cy = center[1];
+  L.cz = center[2];
+  L.r = radius;
+  L.ex = emission[0];
+  L.ey = emission[1];
+  L.ez = emission[2];
+  ctx->lights.push_back(L);
+  ctx->committed = false;
+  return PT_OK;
+}
+
+// ------------------------------------------------------------------- miss
+PT_API int pt_set_env_gradient(pt_context* ctx, const float c1[3], const float c2[3]) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(c1) || !finite3(c2)) return fail(ctx, PT_EINVAL, "invalid colours");
+  ctx->miss.type = PT_MISS_GRADIENT;
+  ctx->miss.c1x = c1[0]; ctx->miss.c1y = c1[1]; ctx->miss.c1z = c1[2];
+  ctx->miss.c2x = c2[0]; ctx->miss.c2y = c2[1]; ctx->miss.c2z = c2[2];
+  ctx->committed = false;
+  return PT_OK;
+}
+
+PT_API int pt_set_env_constant(pt_context* ctx, const float c[3]) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(c)) return fail(ctx, PT_EINVAL, "invalid colour");
+  ctx->miss.type = PT_MISS_CONSTANT;
+  ctx->miss.c1x = c[0]; ctx->miss.c1y = c[1]; ctx->miss.c1z = c[2];
+  ctx->committed = false;
+  return PT_OK;
+}
+
+PT_API int pt_set_env_map(pt_context* ctx, int kind, const float* rgba, int w, int h,
+                          int spherical) {
+  if (!ctx) return PT_EINVAL;
+  if ((kind != PT_MISS_HDR && kind != PT_MISS_IMG) || !rgba || w <= 0 || h <= 0)
+    return fail(ctx, PT_EINVAL, "invalid environment map");
+  ctx->miss.type = kind;
+  ctx->miss.w = w;
+  ctx->miss.h = h;
+  ctx->miss.spherical = spherical ? 1 : 0;
+  ctx->env.resize((size_t)w * h);
+  memcpy(ctx->env.data(), rgba, (size_t)w * h * 16);
+  ctx->committed = false;
+  return PT_OK;
+}
+
+// ------------------------------------------------------------------ camera
+PT_API int pt_set_camera(pt_context* ctx, const float lookfrom[3], const float lookat[3],
+                         const float vup[3], float vfov, float aspect, float aperture,
+                         float focus_dist, float t0, float t1) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(lookfrom) || !finite3(lookat) || !finite3(vup))
+    return fail(ctx, PT_EINVAL, "camera vectors must be finite");
+  // host_includes/camera.hpp:13-38, with the oracle's elementary functions
+  GpuCamera& c = ctx->cam;
+  c.lens_radius = aperture / 2.f;
+  c.time0 = t0;
+  c.time1 = t1;
+  float theta = vfov * PI_F / 180.f;
+  float half_height = pt_tanf(theta / 2.f);
+  float half_width = aspect * half_height;
+  float o[3] = {lookfrom[0], lookfrom[1], lookfrom[2]};
+  float w[3] = {lookfrom[0] - lookat[0], lookfrom[1] - lookat[1], lookfrom[2] - lookat[2]};
+  auto len = [](const float* v) { return ptm_sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+  float lw = len(w);
+  w[0] = w[0] / lw; w[1] = w[1] / lw; w[2] = w[2] / lw;
+  float u[3] = {vup[1] * w[2] - vup[2] * w[1], vup[2] * w[0] - vup[0] * w[2],
+                vup[0] * w[1] - vup[1] * w[0]};
+  float lu = len(u);
+  u[0] = u[0] / lu; u[1] = u[1] / lu; u[2] = u[2] / lu;
+  float v[3] = {w[1] * u[2] - w[2] * u[1], w[2] * u[0] - w[0] * u[2], w[0] * u[1] - w[1] * u[0]};
+  float hf = half_width * focus_dist, vf = half_height * focus_dist;
+  float llc[3], hor[3], ver[3];
+  for (int k = 0; k < 3; k++) {
+    llc[k] = o[k] - hf * u[k] - vf * v[k] - focus_dist * w[k];
+    hor[k] = 2.f * half_width * focus_dist * u[k];
+    ver[k] = 2.f * half_height * focus_dist * v[k];
+  }
+  c.ox = o[0]; c.oy = o[1]; c.oz = o[2];
+  c.lx = llc[0]; c.ly = llc[1]; c.lz = llc[2];
+  c.hx = hor[0]; c.hy = hor[1]; c.hz = hor[2];
+  c.vx = ver[0]; c.vy = ver[1]; c.vz = ver[2];
+  c.ux = u[0]; c.uy = u[1]; c.uz = u[2];
+  c.wx = v[0]; c.wy = v[1]; c.wz = v[2];
+  ctx->committed = false;
+  return PT_OK;
+}
+
+// ------------------------------------------------------------------- commit
+PT_API int pt_commit(pt_context* ctx) {
+  if (!ctx) return PT_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  size_t n = ctx->prims.size();
+  std::vector<pt::Box> boxes(n);
+  for (size_t i = 0; i < n; i++) boxes[i] = prim_box(ctx, ctx->prims[i]);
+  pt::Bvh8Out bvh;
+  if (n) pt::build_bvh8_host(boxes, bvh);
+  if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "BVH8 failed validation");
+  // primitive records in leaf order
+  std::vector<float4> rec(3 * (n ? n : 1));
+  for (size_t k = 0; k < bvh.leaf_order.size(); k++) {
+    const HostPrim& p = ctx->prims[bvh.leaf_order[k]];
+    uint32_t tag = (uint32_t)p.type | ((uint32_t)p.axis << 2) | ((uint32_t)p.flip << 4) |
+                   ((uint32_t)(p.xform + 1) << 8);
+    float tagf, idf, matf;
+    uint32_t id = bvh.leaf_order[k];
+    memcpy(&tagf, &tag, 4);
+    memcpy(&idf, &id, 4);
+    memcpy(&matf, &p.material, 4);
+    rec[3 * k] = make_float4(p.f[0], p.f[1], p.f[2], tagf);
+    rec[3 * k + 1] = make_float4(p.f[3], p.f[4], p.f[5], idf);
+    rec[3 * k + 2] = make_float4(p.f[6], p.f[7], p.f[8], matf);
+  }
+  cudaStream_t st = ctx->stream;
+  if (ctx->graph) {
+    cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  size_t nn = bvh.nodes.size() / 20;
+  std::vector<uint4> nodes(nn ? nn * 5 : 5);
+  if (nn) memcpy(nodes.data(), bvh.nodes.data(), bvh.nodes.size() * 4);
+  CK(ctx->d_nodes.upload(nodes.data(), nodes.size(), st));
+  CK(ctx->d_prims.upload(rec.data(), rec.size(), st));
+  std::vector<float4> xf(ctx->xforms.size() / 4 + 1);
+  if (!ctx->xforms.empty()) memcpy(xf.data(), ctx->xforms.data(), ctx->xforms.size() * 4);
+  CK(ctx->d_xforms.upload(xf.data(), xf.size(), st));
+  std::vector<GpuMaterial> mats = ctx->mats;
+  if (mats.empty()) mats.resize(1);
+  CK(ctx->d_mats.upload(mats.data(), mats.size(), st));
+  std::vector<GpuLight> lights = ctx->lights;
+  if (lights.empty()) lights.resize(1);
+  CK(ctx->d_lights.upload(lights.data(), lights.size(), st));
+  std::vector<uint4> ta = ctx->tri_attr;
+  if (ta.empty()) ta.resize(1);
+  CK(ctx->d_tri_attr.upload(ta.data(), ta.size(), st));
+  std::vector<float> nrm = ctx->normals, uv = ctx->uvs;
+  if (nrm.empty()) nrm.resize(3);
+  if (uv.empty()) uv.resize(2);
+  CK(ctx->d_normals.upload(nrm.data(), nrm.size(), st));
+  CK(ctx->d_uvs.upload(uv.data(), uv.size(), st));
+  std::vector<float4> env = ctx->env;
+  if (env.empty()) env.resize(1);
+  CK(ctx->d_env.upload(env.data(), env.size(), st));
+  CK(cudaStreamSynchronize(st));
+  DevScene& S = ctx->scene;
+  memset(&S, 0, sizeof(S));
+  S.nodes = ctx->d_nodes.p;
+  S.prims = ctx->d_prims.p;
+  S.xforms = ctx->d_xforms.p;
+  S.mats = ctx->d_mats.p;
+  S.lights = ctx->d_lights.p;
+  S.tri_attr = ctx->d_tri_attr.p;
+  S.normals = ctx->d_normals.p;
+  S.uvs = ctx->d_uvs.p;
+  S.num_lights = (int)ctx->lights.size();
+  S.num_prims = (int)n;
+  S.miss = ctx->miss;
+  S.miss.env = ctx->d_env.p;
+  S.cam = ctx->cam;
+  ctx->bvh_depth = bvh.depth;
+  ctx->bvh_nodes = nn;
+  ctx->max_stack = std::max(1, bvh.depth + 1);
+  if ((size_t)ctx->max_stack * PT_TRACE_BLOCK * 8 > 200 * 1024)
+    return fail(ctx, PT_EINVAL, "BVH too deep for the traversal stack");
+  CK(pt::set_trace_smem(ctx->max_stack));
+  ctx->trace_grid = pt::wave_grid(0, ctx->max_stack);
+  ctx->shade_grid = pt::wave_grid(1, ctx->max_stack);
+  auto t1 = std::chrono::steady_clock::now();
+  ctx->stats.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  ctx->stats.bvh_nodes = nn;
+  ctx->stats.bvh_bytes = nn * 80 + n * 48;
+  ctx->stats.bvh_depth = bvh.depth;
+  ctx->committed = true;
+  return PT_OK;
+}
+
+// ------------------------------------------------------------------- render
+static int ensure_wave(pt_context* ctx, size_t results_needed) {
+  int slots = ctx->opt.path_slots > 0 ? ctx->opt.path_slots : (1 << 21);
+  if (ctx->slots != slots || !ctx->d_slot_f4.p) {
+    if (ctx->graph) {
+      cudaGraphExecDestroy(ctx->graph);
+      ctx->graph = nullptr;
+    }
+    CK(ctx->d_slot_f4.ensure((size_t)slots * 10));
+    CK(ctx->d_st.ensure((size_t)slots));
+    CK(ctx->d_queues.ensure((size_t)slots * 4));
+    CK(ctx->d_ctr.ensure(1));
+    CK(ctx->d_ctl.ensure(1));
+    ctx->slots = slots;
+    WaveState& W = ctx->W;
+    float4* f = ctx->d_slot_f4.p;
+    size_t s = (size_t)slots;
+    W.ray_o = f;
+    W.ray_d = f + s;
+    W.thr = f + 2 * s;
+    W.rad = f + 3 * s;
+    W.hit = f + 4 * s;
+    W.nee_P = f + 5 * s;
+    W.nee_N = f + 6 * s;
+    W.nee_Wo = f + 7 * s;
+    W.nee_Wi = f + 8 * s;
+    W.st = ctx->d_st.p;
+    W.q[0] = ctx->d_queues.p;
+    W.q[1] = ctx->d_queues.p + s;
+    W.q_shadow = ctx->d_queues.p + 2 * s;
+    W.q_free = ctx->d_queues.p + 3 * s;
+    W.ctr = ctx->d_ctr.p;
+    W.slots = slots;
+    ctx->wave_dirty = true;
+  }
+  if (ctx->wave_dirty) {
+    pt::launch_init_free(ctx->W, ctx->stream);
+    ctx->wave_dirty = false;
+  }
+  if (ctx->d_results.n < results_needed || !ctx->d_results.p) {
+    if (ctx->graph) {
+      cudaGraphExecDestroy(ctx->graph);
+      ctx->graph = nullptr;
+    }
+    CK(ctx->d_results.ensure(results_needed));
+  }
+  ctx->W.results = ctx->d_results.p;
+  return PT_OK;
+}
+
+static const int kItersPerGraph = 8;
+
+static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int frames) {
+  cudaStream_t st = ctx->stream;
+  WaveCtl& ctl = *ctx->h_ctl;
+  ctl.width = p->width;
+  ctl.height = p->height;
+  ctl.frame0 = frame0;
+  ctl.max_depth = p->max_depth;
+  ctl.rr_enable = p->rr_enable;
+  ctl.rr_depth = p->rr_depth;
+  ctl.mode = p->mode;
+  ctl.guide = p->guide;
+  ctl.chunk_paths = (unsigned long long)p->width * p->height * frames;
+  CK(cudaMemcpyAsync(ctx->d_ctl.p, &ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, st));
+  WaveCounters& c = *ctx->h_ctr;
+  memset(&c, 0, sizeof(c));
+  c.n_free = (uint32_t)ctx->slots;
+  c.free_head = 0;
+  c.free_tail = 0;  // ring full: tail == head (mod slots)
+  CK(cudaMemcpyAsync(ctx->d_ctr.p, &c, sizeof(WaveCounters), cudaMemcpyHostToDevice, st));
+  bool counters = ctx->opt.enable_counters != 0;
+  bool timing = ctx->opt.enable_timing != 0;
+  if (timing && ctx->tev.empty()) {
+    ctx->tev.resize(6 * kItersPerGraph);
+    for (auto& e : ctx->tev) CK(cudaEventCreate(&e));
+  }
+  if (!ctx->graph || ctx->graph_counters != counters || ctx->graph_timing != timing) {
+    if (ctx->graph) {
+      cudaGraphExecDestroy(ctx->graph);
+      ctx->graph = nullptr;
+    }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < kItersPerGraph; i++)
+      pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters,
+                           ctx->trace_grid, ctx->shade_grid, st,
+                           timing ? &ctx->tev[6 * i] : nullptr);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+    cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    ctx->graph_counters = counters;
+    ctx->graph_timing = timing;
+  }
+  // bounded host loop: a path needs at most max_depth iterations after its
+  // generation, and every iteration generates at least one path while any
+  // remain, so this many iterations always suffice
+  unsigned long long max_iters = ctl.chunk_paths + (unsigned long long)p->max_depth + 16;
+  unsigned long long iters = 0;
+  while (true) {
+    CK(cudaGraphLaunch(ctx->graph, st));
+    iters += kItersPerGraph;
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr.p, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    ctx->stats.iterations += kItersPerGraph;
+    ctx->stats.kernel_launches += 7 * kItersPerGraph;
+    if (timing) {
+      for (int i = 0; i < kItersPerGraph; i++)
+        for (int k = 0; k < 5; k++) {
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, ctx->tev[6 * i + k], ctx->tev[6 * i + k + 1]);
+          ctx->stats.stage_ms[k] += ms;
+        }
+    }
+    if (c.error) return fail(ctx, PT_EQUEUE, "traversal stack overflow");
+    if (c.next_path >= ctl.chunk_paths && c.n_cur == 0) break;
+    if (iters > max_iters) return fail(ctx, PT_ETIMEOUT, "wavefront did not drain");
+  }
+  ctx->stats.paths += c.paths_done;
+  ctx->stats.ext_rays += c.ext_rays;
+  ctx->stats.shadow_rays += c.shadow_rays;
+  ctx->stats.node_fetches += c.node_fetches;
+  ctx->stats.prim_tests += c.prim_tests;
+  return PT_OK;
+}
+
+static void reset_render_stats(pt_context* ctx) {
+  pt_stats& s = ctx->stats;
+  s.paths = s.ext_rays = s.shadow_rays = s.node_fetches = s.prim_tests = 0;
+  s.iterations = s.kernel_launches = 0;
+  for (double& x : s.stage_ms) x = 0.0;
+  s.render_ms = 0.0;
+}
+
+static int check_params(pt_context* ctx, const pt_render_params* p) {
+  if (!p) return fail(ctx, PT_EINVAL, "null params");
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->frame0 < 0 || p->max_depth <= 0 ||
+      p->max_depth > 65535)
+    return fail(ctx, PT_EINVAL, "invalid render parameters");
+  if ((unsigned long long)p->width * p->height > (1ull << 30))
+    return fail(ctx, PT_EINVAL, "image too large");
+  if (p->mode != PT_MODE_REF) return fail(ctx, PT_EINVAL, "only PT_MODE_REF is implemented");
+  if (p->guide != 0) return fail(ctx, PT_EINVAL, "guide not available in this build");
+  if (!ctx->committed) return fail(ctx, PT_ESTATE, "scene not committed (call pt_commit)");
+  return PT_OK;
+}
+
+// Render into a device accumulator.
+static int render_device(pt_context* ctx, const pt_render_params* p, float4* d_acc) {
+  cudaStream_t st = ctx->stream;
+  size_t WH = (size_t)p->width * p->height;
+  const size_t results_cap = (size_t)1 << 27;  // 128 M paths = 2 GiB of results
+  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)p->spp, results_cap / WH));
+  int rc = ensure_wave(ctx, (size_t)chunk * WH);
+  if (rc) return rc;
+  if (p->frame0 == 0) CK(cudaMemsetAsync(d_acc, 0, WH * sizeof(float4), st));
+  for (int f = 0; f < p->spp; f += chunk) {
+    int frames = std::min(chunk, p->spp - f);
+    rc = run_chunk(ctx, p, p->frame0 + f, frames);
+    if (rc) {
+      ctx->wave_dirty = true;
+      return rc;
+    }
+    pt::launch_accumulate(ctx->d_results.p, d_acc, p->width, p->height, frames, st);
+    ctx->stats.kernel_launches += 1;
+  }
+  return PT_OK;
+}
+
+PT_API int pt_render(pt_context* ctx, const pt_render_params* params, float* accum_rgba,
+                     void* stream) {
+  if (!ctx) return PT_EINVAL;
+  int rc = check_params(ctx, params);
+  if (rc) return rc;
+  if (!accum_rgba) return fail(ctx, PT_EINVAL, "null accumulator");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t user = (cudaStream_t)stream;
+  cudaStream_t st = ctx->stream;
+  // order after the caller's stream
+  CK(cudaEventRecord(ctx->ev0, user));
+  CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  reset_render_stats(ctx);
+  size_t WH = (size_t)params->width * params->height;
+  bool dev = is_device_ptr(accum_rgba);
+  float4* d_acc = (float4*)accum_rgba;
+  if (!dev) {
+    CK(ctx->d_acc.ensure(WH));
+    d_acc = ctx->d_acc.p;
+    if (params->frame0 != 0)
+      CK(cudaMemcpyAsync(d_acc, accum_rgba, WH * sizeof(float4), cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaEventRecord(ctx->ev0, st));
+  rc = render_device(ctx, params, d_acc);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->ev1, st));
+  if (!dev) CK(cudaMemcpyAsync(accum_rgba, d_acc, WH * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->stats.render_ms = ms;
+  return PT_OK;
+}
+
+PT_API int pt_render_paths(pt_context* ctx, const pt_render_params* params, float* out_rgb,
+                           void* stream) {
+  if (!ctx) return PT_EINVAL;
+  int rc = check_params(ctx, params);
+  if (rc) return rc;
+  if (!out_rgb) return fail(ctx, PT_EINVAL, "null output");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
+  CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  pt_render_params p = *params;
+  p.spp = 1;
+  size_t WH = (size_t)p.width * p.height;
+  CK(ctx->d_acc.ensure(WH));
+  reset_render_stats(ctx);
+  p.frame0 = 0;  // acc scratch zeroed; the frame index goes into the chunk
+  rc = ensure_wave(ctx, WH);
+  if (rc) return rc;
+  p.frame0 = params->frame0;
+  rc = run_chunk(ctx, &p, p.frame0, 1);
+  if (rc) {
+    ctx->wave_dirty = true;
+    return rc;
+  }
+  bool dev = is_device_ptr(out_rgb);
+  float* d_out = out_rgb;
+  if (!dev) {
+    CK(ctx->d_tmp.ensure(3 * WH));
+    d_out = ctx->d_tmp.p;
+  }
+  pt::launch_paths_out(ctx->d_results.p, d_out, (uint32_t)WH, st);
+  if (!dev) CK(cudaMemcpyAsync(out_rgb, d_out, 3 * WH * sizeof(float), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return PT_OK;
+}
+
+PT_API int pt_trace_first_hits(pt_context* ctx, int width, int height, int frame, uint32_t* prim,
+                               uint32_t* mat, float* t, void* stream) {
+  if (!ctx) return PT_EINVAL;
+  if (width <= 0 || height <= 0 || frame < 0 || !prim || !mat || !t)
+    return fail(ctx, PT_EINVAL, "invalid arguments");
+  if (!ctx->committed) return fail(ctx, PT_ESTATE, "scene not committed (call pt_commit)");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
+  CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  size_t WH = (size_t)width * height;
+  CK(ctx->d_tmpu.ensure(2 * WH + 1));
+  CK(ctx->d_tmp.ensure(WH));
+  uint32_t* d_err = ctx->d_tmpu.p + 2 * WH;
+  CK(cudaMemsetAsync(d_err, 0, 4, st));
+  pt::launch_first_hits(ctx->scene, width, height, frame, ctx->d_tmpu.p, ctx->d_tmpu.p + WH,
+                        ctx->d_tmp.p, ctx->max_stack, d_err, st);
+  CK(cudaGetLastError());
+  uint32_t herr = 0;
+  CK(cudaMemcpyAsync(prim, ctx->d_tmpu.p, WH * 4, cudaMemcpyDefault, st));
+  CK(cudaMemcpyAsync(mat, ctx->d_tmpu.p + WH, WH * 4, cudaMemcpyDefault, st));
+  CK(cudaMemcpyAsync(t, ctx->d_tmp.p, WH * 4, cudaMemcpyDefault, st));
+  CK(cudaMemcpyAsync(&herr, d_err, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (herr) return fail(ctx, PT_EQUEUE, "traversal stack overflow");
+  return PT_OK;
+}
+
+PT_API int pt_resolve_display(pt_context* ctx, const float* accum_rgba, int width, int height,
+                              int frame, uint8_t* rgba8, void* stream) {
+  if (!ctx) return PT_EINVAL;
+  if (!accum_rgba || !rgba8 || width <= 0 || height <= 0 || frame < 0)
+    return fail(ctx, PT_EINVAL, "invalid arguments");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
+  CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  size_t WH = (size_t)width * height;
+  const float4* d_acc = (const float4*)accum_rgba;
+  if (!is_device_ptr(accum_rgba)) {
+    CK(ctx->d_acc.ensure(WH));
+    CK(cudaMemcpyAsync(ctx->d_acc.p, accum_rgba, WH * 16, cudaMemcpyHostToDevice, st));
+    d_acc = ctx->d_acc.p;
+  }
+  CK(ctx->d_tmpu.ensure(WH));
+  pt::launch_resolve(d_acc, (uchar4*)ctx->d_tmpu.p, (int)WH, frame, st);
+  CK(cudaMemcpyAsync(rgba8, ctx->d_tmpu.p, WH * 4, cudaMemcpyDefault, st));
+  CK(cudaStreamSynchronize(st));
+  return PT_OK;
+}
+
+PT_API int pt_get_stats(pt_context* ctx, pt_stats* out) {
+  if (!ctx || !out) return PT_EINVAL;
+  *out = ctx->stats;
+  return PT_OK;
+}
+
+}  // extern "C"

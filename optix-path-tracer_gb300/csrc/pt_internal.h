@@ -1,0 +1,78 @@
+/*
+ * pt_internal.h - library-internal structures shared by the host API
+ * (pt_api.cu, bvh_build.cu) and the wavefront kernels (pt_kernels.cu).
+ */
+#ifndef PT_INTERNAL_H
+#define PT_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "pt_types.h"
+
+#define PT_TRACE_BLOCK 128
+#define PT_SHADE_BLOCK 256
+
+struct Ray3 {
+  float3 o, d;
+};
+
+/* Queue counters of the streaming wavefront, in device memory. */
+struct WaveCounters {
+  uint32_t n_cur;        /* paths in the current extension queue (before generation) */
+  uint32_t n_next;       /* paths pushed into the next extension queue */
+  uint32_t n_shadow;     /* shadow rays queued this iteration */
+  uint32_t n_free;       /* free slots in the ring q_free[free_head ...] */
+  uint32_t n_freed;      /* slots freed this iteration (appended at free_tail) */
+  uint32_t free_head, free_tail;
+  uint32_t parity;       /* which of q[0], q[1] is current */
+  uint32_t error;        /* bit 0: traversal stack overflow */
+  uint32_t iter;
+  unsigned long long next_path;   /* next path id of the chunk to generate */
+  unsigned long long paths_done;
+  unsigned long long ext_rays, shadow_rays;
+  unsigned long long node_fetches, prim_tests;
+};
+
+/* Per-chunk render controls, in device memory (kernels read them, so one
+ * captured CUDA graph serves every chunk). */
+struct WaveCtl {
+  int width, height;
+  int frame0;                     /* frame of path id 0 of this chunk */
+  int max_depth, rr_enable, rr_depth, mode, guide;
+  unsigned long long chunk_paths; /* paths in this chunk */
+};
+
+/* Path-state arrays (structure of arrays, one entry per slot). */
+struct WaveState {
+  float4 *ray_o, *ray_d;      /* origin+tmin, direction+tmax */
+  float4 *thr, *rad;          /* throughput, radiance */
+  uint4* st;                  /* seed, path id, depth|prevSpecular<<16 */
+  float4* hit;                /* t, u, v, leaf index */
+  float4 *nee_P, *nee_N, *nee_Wo, *nee_Wi; /* parked Direct_Light context */
+  uint32_t* q[2];             /* extension queues (ping-pong) */
+  uint32_t* q_shadow;
+  uint32_t* q_free;           /* ring of free slots */
+  WaveCounters* ctr;
+  float4* results;            /* per path of the chunk: colour */
+  int slots;
+};
+
+namespace pt {
+size_t trace_smem(int max_stack);
+int wave_grid(int kind, int max_stack);
+cudaError_t set_trace_smem(int max_stack);
+/* One wavefront iteration (7 kernels).  ev, if not null, holds 6 events
+ * recorded between the stages. */
+void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
+                      bool counters, int trace_grid, int shade_grid, cudaStream_t st,
+                      cudaEvent_t* ev);
+void launch_init_free(const WaveState& W, cudaStream_t st);
+void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
+                       cudaStream_t st);
+void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st);
+void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
+                       float* t, int max_stack, uint32_t* err, cudaStream_t st);
+void launch_resolve(const float4* acc, uchar4* out, int n, int frame, cudaStream_t st);
+}  // namespace pt
+
+#endif

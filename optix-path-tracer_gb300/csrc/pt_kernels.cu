@@ -1,0 +1,834 @@
+/*
+ * pt_kernels.cu - wavefront path tracing kernels for sm_103a.
+ *
+ * One path = one (pixel, frame) sample of programs/raygen.cu:148-167.  The
+ * reference runs each path in one OptiX megakernel thread; here a fixed pool
+ * of path slots streams through stage kernels, and a slot whose path ends
+ * is refilled with the next path (regeneration), so the pool stays full:
+ *
+ *   k_generate      renderPixel up to color()'s loop: TEA seed, jitter,
+ *                   thin-lens camera ray, time draw (raygen.cu:148-162,50-69)
+ *   k_trace         closest hit through the BVH8 (replaces rtTrace)
+ *   k_shade         miss programs, Get_HitRecord, closest-hit programs; the
+ *                   NEE of Direct_Light stops at the shadow ray
+ *   k_trace_shadow  shadow rays (programs/hit.cu:16-24, closest-hit rule)
+ *   k_finish        rest of Direct_Light (MIS), BSDF continuation
+ *   k_advance       queue bookkeeping (one thread)
+ * Paths that continue are compacted into the next extension queue with
+ * warp-aggregated atomics (ballot + popc prefix); ended paths write their
+ * colour to a per-path result slot, and k_accumulate adds results to the
+ * accumulator in frame order, so the image does not depend on scheduling.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include "pt_device.cuh"
+#include "pt_internal.h"
+
+using namespace ptd;
+
+// ------------------------------------------------------------ BVH8 trace --
+struct TraceHit {
+  float t, u, v;
+  uint32_t leaf;  // index into the primitive array (leaf order), PT_NO_HIT if none
+  uint32_t id;    // primitive id
+};
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
+  uint32_t lo = min(a, b), hi = max(a, b);
+  a = lo;
+  b = hi;
+}
+
+// Closest hit of (o, d) in (tmin, tmax): lexicographic minimum of (t, id).
+// stk: this thread's column of the block's shared-memory stack (stride
+// blockDim.x), one entry per BVH8 level: (child_base, ranks left | count<<24).
+template <bool COUNT>
+__device__ TraceHit trace_bvh8(const DevScene& S, V3 o, V3 d, float tmin, float tmax, uint2* stk,
+                               int stride, int max_stack, uint32_t* err, uint32_t& n_nodes,
+                               uint32_t& n_prims) {
+  TraceHit h;
+  h.t = tmax;
+  h.u = h.v = 0.f;
+  h.leaf = PT_NO_HIT;
+  h.id = 0xffffffffu;
+  float tbest = tmax;
+  // box-test constants: direction reciprocals kept finite
+  const float eps = 1e-18f;
+  float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
+  float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
+  float dz = fabsf(d.z) < eps ? copysignf(eps, d.z) : d.z;
+  float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  WtRay wt = wt_setup(d);
+
+  int sp = 0;
+  uint32_t cur = 0;
+  bool have = S.num_prims > 0;
+  while (have) {
+    const uint4* np = S.nodes + 5 * (size_t)cur;
+    uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3),
+          n4 = __ldg(np + 4);
+    if (COUNT) n_nodes++;
+    float sx = __uint_as_float((n0.w & 0xffu) << 23);
+    float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
+    float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
+    float ax = sx * ix, ay = sy * iy, az = sz * iz;
+    float bx = (__uint_as_float(n0.x) - o.x) * ix;
+    float by = (__uint_as_float(n0.y) - o.y) * iy;
+    float bz = (__uint_as_float(n0.z) - o.z) * iz;
+    float tlim = tbest * 1.0000005f;
+    uint32_t keys[8];
+    uint32_t leafmask = 0;
+    int nint = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      uint32_t meta = byte_of(i < 4 ? n1.z : n1.w, i & 3);
+      keys[i] = 0xffffffffu;
+      if (meta == 0) continue;
+      int w = i & 3;
+      float qlx = (float)byte_of(i < 4 ? n2.x : n2.y, w);
+      float qly = (float)byte_of(i < 4 ? n2.z : n2.w, w);
+      float qlz = (float)byte_of(i < 4 ? n3.x : n3.y, w);
+      float qhx = (float)byte_of(i < 4 ? n3.z : n3.w, w);
+      float qhy = (float)byte_of(i < 4 ? n4.x : n4.y, w);
+      float qhz = (float)byte_of(i < 4 ? n4.z : n4.w, w);
+      float t0x = __fmaf_rn(qlx, ax, bx), t1x = __fmaf_rn(qhx, ax, bx);
+      float t0y = __fmaf_rn(qly, ay, by), t1y = __fmaf_rn(qhy, ay, by);
+      float t0z = __fmaf_rn(qlz, az, bz), t1z = __fmaf_rn(qhz, az, bz);
+      float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+      float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tlim));
+      if (tn <= tf) {
+        if (meta & 0x80u) {
+          keys[i] = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
+          nint++;
+        } else {
+          leafmask |= 1u << i;
+        }
+      }
+    }
+    // leaves of this node: test their primitives now
+    while (leafmask) {
+      int i = __ffs(leafmask) - 1;
+      leafmask &= leafmask - 1;
+      uint32_t meta = byte_of(i < 4 ? n1.z : n1.w, i & 3);
+      uint32_t first = n1.y + (meta & 31u), cnt = meta >> 5;
+      for (uint32_t k = 0; k < cnt; k++) {
+        uint32_t pi = first + k;
+        PrimRec p = load_prim(S.prims, pi);
+        if (COUNT) n_prims++;
+        int type = prim_type(p);
+        float t = 0.f, bu = 0.f, bv = 0.f;
+        bool ok;
+        if (type == PT_PRIM_TRIANGLE) {
+          ok = tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
+        } else {
+          V3 oo = o, dd = d;
+          int xf = prim_xform(p);
+          if (xf >= 0) {
+            const float4* I = S.xforms + 6 * xf + 3;
+            oo = xpoint(I, o);
+            dd = xvector(I, d);
+          }
+          if (type == PT_PRIM_SPHERE) ok = sphere_candidate(p, oo, dd, tmin, tmax, t);
+          else if (type == PT_PRIM_RECT) ok = rect_candidate(p, oo, dd, tmin, tmax, t);
+          else ok = box_candidate(p, oo, dd, tmin, tmax, t);
+        }
+        if (ok) {
+          uint32_t id = prim_id(p);
+          if (t < tbest || (t == tbest && id < h.id)) {
+            tbest = t;
+            h.t = t;
+            h.u = bu;
+            h.v = bv;
+            h.leaf = pi;
+            h.id = id;
+          }
+        }
+      }
+    }
+    if (nint > 0) {
+      // order internal children near to far (sorting network, 19 exchanges)
+      cswap(keys[0], keys[1]); cswap(keys[2], keys[3]); cswap(keys[4], keys[5]); cswap(keys[6], keys[7]);
+      cswap(keys[0], keys[2]); cswap(keys[1], keys[3]); cswap(keys[4], keys[6]); cswap(keys[5], keys[7]);
+      cswap(keys[1], keys[2]); cswap(keys[5], keys[6]); cswap(keys[0], keys[4]); cswap(keys[3], keys[7]);
+      cswap(keys[1], keys[5]); cswap(keys[2], keys[6]);
+      cswap(keys[1], keys[4]); cswap(keys[3], keys[6]);
+      cswap(keys[2], keys[4]); cswap(keys[3], keys[5]);
+      cswap(keys[3], keys[4]);
+      uint32_t base = n1.x;
+      if (nint > 1) {
+        uint32_t list = 0;
+#pragma unroll
+        for (int j = 7; j >= 1; j--)
+          if (j < nint) list = (list << 3) | (keys[j] & 7u);
+        if (sp >= max_stack) {
+          atomicOr(err, 1u);
+          break;
+        }
+        stk[sp * stride] = make_uint2(base, list | ((uint32_t)(nint - 1) << 24));
+        sp++;
+      }
+      cur = base + (keys[0] & 7u);
+      continue;
+    }
+    // pop the next child of the deepest pending group
+    if (sp == 0) break;
+    uint2 e = stk[(sp - 1) * stride];
+    uint32_t cnt = e.y >> 24, list = e.y & 0xffffffu;
+    cur = e.x + (list & 7u);
+    cnt--;
+    if (cnt == 0) sp--;
+    else stk[(sp - 1) * stride] = make_uint2(e.x, (list >> 3) | (cnt << 24));
+  }
+  return h;
+}
+
+// -------------------------------------------------- warp-aggregated push --
+__device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool active) {
+  uint32_t mask = __ballot_sync(0xffffffffu, active);
+  if (!active) return 0;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------- path state ----
+// st.x = seed, st.y = path id in the chunk, st.z = depth | prevSpecular<<16,
+// st.w = unused
+__device__ __forceinline__ void finalize_path(const WaveState& W, const WaveCounters& c,
+                                              uint32_t slot, uint32_t pid, V3 col, bool done) {
+  // de_nan, programs/raygen.cu:126-134
+  if (done) {
+    if (!(col.x == col.x)) col.x = 0.f;
+    if (!(col.y == col.y)) col.y = 0.f;
+    if (!(col.z == col.z)) col.z = 0.f;
+    W.results[pid] = make_float4(col.x, col.y, col.z, 1.f);
+  }
+  uint32_t pos = warp_push(&W.ctr->n_freed, done);
+  if (done) W.q_free[(c.free_tail + pos) % (uint32_t)W.slots] = slot;
+}
+
+// raygen.cu:81-122 after the closest-hit program: event dispatch, next
+// ray, Russian roulette, depth limit.  Returns true if the path continues.
+struct Tail {
+  int event;  // 0 bounced, 1 cancelled, 2 hit light
+  bool isSpecular;
+  V3 origin, direction;
+};
+
+__device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters& c,
+                                          const WaveCtl& ctl, uint32_t slot, uint4 st, V3 thr,
+                                          V3 rad, const Tail& tl, bool active) {
+  bool done = false, cont = false;
+  V3 col = v3(0.f);
+  if (active) {
+    uint32_t depth = st.z & 0xffffu;
+    bool prevSpec = (st.z >> 16) & 1u;
+    if (tl.event == 2) {
+      if (depth == 0 || prevSpec) rad += thr;
+      col = rad;
+      done = true;
+    } else if (tl.event == 1) {
+      col = rad;
+      done = true;
+    } else {
+      prevSpec = tl.isSpecular;
+      if (ctl.rr_enable) {
+        float prob = max_component(thr);
+        if ((int)depth > ctl.rr_depth) {
+          if (rnd(st.x) >= prob) {
+            col = rad + thr;
+            done = true;
+          } else {
+            thr *= 1.f / prob;
+          }
+        }
+      }
+      if (!done) {
+        depth++;
+        if ((int)depth >= ctl.max_depth) {
+          col = v3(0.f);
+          done = true;
+        } else {
+          cont = true;
+          W.ray_o[slot] = make_float4(tl.origin.x, tl.origin.y, tl.origin.z, 1e-3f);
+          W.ray_d[slot] = make_float4(tl.direction.x, tl.direction.y, tl.direction.z, PT_RAY_TMAX);
+          W.thr[slot] = make_float4(thr.x, thr.y, thr.z, 0.f);
+          W.rad[slot] = make_float4(rad.x, rad.y, rad.z, 0.f);
+          W.st[slot] = make_uint4(st.x, st.y, depth | ((uint32_t)prevSpec << 16), 0u);
+        }
+      }
+    }
+  }
+  finalize_path(W, c, slot, st.y, col, done);
+  uint32_t pos = warp_push(&W.ctr->n_next, cont);
+  if (cont) W.q[(c.parity ^ 1u)][pos] = slot;
+}
+
+// ------------------------------------------------------------- kernels ----
+__device__ __forceinline__ uint32_t gen_count(const WaveCounters& c, const WaveCtl& ctl) {
+  unsigned long long left = ctl.chunk_paths - c.next_path;
+  return (uint32_t)min((unsigned long long)c.n_free, left);
+}
+
+__device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uint32_t y,
+                                           uint32_t Wd, uint32_t Hd, uint32_t& seed) {
+  float u = float((float)x + rnd(seed)) / (float)Wd;
+  float v = float((float)y + rnd(seed)) / (float)Hd;
+  V3 rd = cam.lens_radius * random_in_unit_disk(seed);
+  V3 lens_offset = v3(cam.ux, cam.uy, cam.uz) * rd.x + v3(cam.wx, cam.wy, cam.wz) * rd.y;
+  V3 origin = v3(cam.ox, cam.oy, cam.oz) + lens_offset;
+  V3 direction = v3(cam.lx, cam.ly, cam.lz) + u * v3(cam.hx, cam.hy, cam.hz) +
+                 v * v3(cam.vx, cam.vy, cam.vz) - origin;
+  Ray3 r;
+  r.o = make_float3(origin.x, origin.y, origin.z);
+  r.d = make_float3(direction.x, direction.y, direction.z);
+  return r;
+}
+
+__global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp) {
+  WaveCounters c = *W.ctr;
+  WaveCtl ctl = *ctlp;
+  uint32_t n = gen_count(c, ctl);
+  uint32_t WH = (uint32_t)ctl.width * (uint32_t)ctl.height;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t slot = W.q_free[(c.free_head + i) % (uint32_t)W.slots];
+    uint32_t pid = (uint32_t)(c.next_path + i);
+    uint32_t frame = (uint32_t)ctl.frame0 + pid / WH;
+    uint32_t pix = pid % WH;
+    uint32_t x = pix % (uint32_t)ctl.width, y = pix / (uint32_t)ctl.width;
+    uint32_t seed = tea64((uint32_t)ctl.width * y + x, frame);
+    Ray3 r = camera_ray(S.cam, x, y, ctl.width, ctl.height, seed);
+    // color(): prd.time draw, programs/raygen.cu:69
+    float tm = S.cam.time0 + rnd(seed) * (S.cam.time1 - S.cam.time0);
+    (void)tm;
+    W.ray_o[slot] = make_float4(r.o.x, r.o.y, r.o.z, 1e-6f);
+    W.ray_d[slot] = make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX);
+    W.thr[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+    W.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    W.st[slot] = make_uint4(seed, pid, 0u, 0u);
+    W.q[c.parity][c.n_cur + i] = slot;
+  }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(PT_TRACE_BLOCK) k_trace(DevScene S, WaveState W,
+                                                          const WaveCtl* __restrict__ ctlp,
+                                                          int max_stack) {
+  extern __shared__ uint2 stack_smem[];
+  WaveCounters c = *W.ctr;
+  uint32_t n = c.n_cur + gen_count(c, *ctlp);
+  const uint32_t* q = W.q[c.parity];
+  uint32_t nn = 0, np = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t slot = q[i];
+    float4 ro = W.ray_o[slot], rd = W.ray_d[slot];
+    TraceHit h = trace_bvh8<COUNT>(S, f4xyz(ro), f4xyz(rd), ro.w, rd.w, stack_smem + threadIdx.x,
+                                   blockDim.x, max_stack, &W.ctr->error, nn, np);
+    W.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.leaf));
+  }
+  if (COUNT) {
+    atomicAdd(&W.ctr->node_fetches, (unsigned long long)nn);
+    atomicAdd(&W.ctr->prim_tests, (unsigned long long)np);
+  }
+}
+
+// Direct_Light (programs/materials/light_sample.cuh:36-73) up to the shadow
+// ray.  Returns 0: no contribution, stop here; 1: shadow ray queued.
+__device__ __forceinline__ int nee_begin(const DevScene& S, uint32_t& seed, V3 P, V3 N,
+                                         bool isLight, V3& Wi, float& lightPDF, int& index) {
+  int numLights = S.num_lights;
+  if (numLights == 0) return 0;
+  index = ((int)(rnd(seed) * numLights)) % numLights;
+  if (isLight && numLights == 1) return 0;
+  GpuLight L = S.lights[index];
+  Wi = light_sample(L, P, seed);
+  lightPDF = light_pdf(L, P, Wi);
+  if (dot(Wi, N) < 0.f) return 0;
+  return 1;
+}
+
+// programs/materials/light_sample.cuh:76-103: MIS after the shadow test.
+__device__ __forceinline__ V3 nee_end(const DevScene& S, const GpuMaterial& m, uint32_t& seed,
+                                      V3 P, V3 Wo, V3 N, V3 Wi, float lightPDF, int index,
+                                      bool occluded) {
+  V3 directLight = v3(0.f);
+  if (occluded) return v3(0.f);
+  GpuLight L = S.lights[index];
+  V3 emission = v3(L.ex, L.ey, L.ez);
+  if (lightPDF != 0.f && !isNull(emission)) {
+    float matPDF = 0.f;
+    V3 matValue = brdf_eval(m, Wo, Wi, N, matPDF);
+    if (matPDF != 0.f && !isNull(matValue)) {
+      float f = 1u * lightPDF, g = 1u * matPDF;
+      float weight = (f * f) / (f * f + g * g);
+      directLight += matValue * emission * weight / lightPDF;
+    }
+  }
+  Wi = brdf_sample(m, Wo, N, seed);
+  float matPDF = 0.f;
+  V3 matValue = brdf_eval(m, Wo, Wi, N, matPDF);
+  if (matPDF != 0.f && !isNull(matValue)) {
+    lightPDF = light_pdf(L, P, Wi);
+    if (!lightPDF || isNull(emission)) return directLight;
+    float f = 1u * matPDF, g = 1u * lightPDF;
+    float weight = (f * f) / (f * f + g * g);
+    directLight += matValue * emission * weight / matPDF;
+  }
+  return directLight;
+}
+
+// Closest-hit continuation after Direct_Light for the NEE materials
+// (lambertian.cu:55-72, oren_nayar.cu:56-69, diffuse_light.cu:40-47).
+__device__ __forceinline__ void after_nee(const GpuMaterial& m, uint32_t& seed, V3 P, V3 Wo, V3 N,
+                                          V3 direct, V3& thr, V3& rad, Tail& tl) {
+  rad += thr * direct;
+  if (m.type == PT_MAT_DIFFUSE_LIGHT) {
+    if (dot(N, Wo) < 0.f) thr *= v3(m.c0x, m.c0y, m.c0z);
+    tl.event = 2;
+    return;
+  }
+  V3 Wi = brdf_sample(m, Wo, N, seed);
+  float pdf = 0.f;
+  V3 attenuation = brdf_eval(m, Wo, Wi, N, pdf);
+  tl.event = 0;
+  tl.origin = P;
+  tl.direction = Wi;
+  thr *= clamp3(attenuation / pdf, 0.f, 1.f);
+  tl.isSpecular = false;
+}
+
+__device__ __forceinline__ V3 env_lookup(const GpuMiss& ms, float u, float v) {
+  if (!(u == u) || !(v == v) || fabsf(u) > 1e6f || fabsf(v) > 1e6f) return v3(0.f);
+  float x = u * (float)ms.w - 0.5f, y = v * (float)ms.h - 0.5f;
+  float fx = floorf(x), fy = floorf(y);
+  float ax = x - fx, ay = y - fy;
+  int ix0 = (int)fx % ms.w; if (ix0 < 0) ix0 += ms.w;
+  int iy0 = (int)fy % ms.h; if (iy0 < 0) iy0 += ms.h;
+  int ix1 = ix0 + 1 == ms.w ? 0 : ix0 + 1;
+  int iy1 = iy0 + 1 == ms.h ? 0 : iy0 + 1;
+  float4 e00 = __ldg(ms.env + iy0 * ms.w + ix0), e10 = __ldg(ms.env + iy0 * ms.w + ix1);
+  float4 e01 = __ldg(ms.env + iy1 * ms.w + ix0), e11 = __ldg(ms.env + iy1 * ms.w + ix1);
+  V3 c00 = f4xyz(e00), c10 = f4xyz(e10), c01 = f4xyz(e01), c11 = f4xyz(e11);
+  return (c00 * (1.f - ax) + c10 * ax) * (1.f - ay) + (c01 * (1.f - ax) + c11 * ax) * ay;
+}
+
+// programs/miss.cu:30-95; returns the multiplier applied to throughput.
+__device__ __forceinline__ V3 miss_color(const GpuMiss& ms, V3 d) {
+  if (ms.type == 0) {
+    V3 unit_direction = normalize(d);
+    float t = 0.5f * (unit_direction.y + 1.f);
+    V3 c = (1.f - t) * v3(ms.c1x, ms.c1y, ms.c1z);
+    c += t * v3(ms.c2x, ms.c2y, ms.c2z);
+    return c;
+  }
+  if (ms.type == 1) return v3(ms.c1x, ms.c1y, ms.c1z);
+  if (ms.type == 3) {
+    float theta = pt_atan2f(d.x, d.z);
+    float phi = PTM_PI * 0.5f - pt_acosf(d.y);
+    float u = (theta + PTM_PI) * (0.5f * (1.0f / PTM_PI));
+    float v = 0.5f * (1.f + pt_sinf(phi));
+    return env_lookup(ms, u, v);
+  }
+  float u, v;
+  if (ms.spherical) {
+    float r = length(d);
+    float lon = pt_atan2f(d.z, d.x);
+    float lat = pt_acosf(d.y / r);
+    u = lon * (1.f / (PI_F * 2.f));
+    v = lat * (1.f / PI_F);
+  } else {
+    float theta = pt_atan2f(d.x, d.z);
+    theta = theta < 0.f ? theta + (2.f * PI_F) : theta;
+    float phi = pt_acosf(d.y);
+    u = 1.f - (theta / (2.f * PI_F));
+    v = phi / PI_F;
+  }
+  return 2.f * env_lookup(ms, u, v);
+}
+
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState W,
+                                                          const WaveCtl* __restrict__ ctlp) {
+  WaveCounters c = *W.ctr;
+  WaveCtl ctl = *ctlp;
+  uint32_t n = c.n_cur + gen_count(c, ctl);
+  const uint32_t* q = W.q[c.parity];
+  uint32_t stride = gridDim.x * blockDim.x;
+  // all lanes of a warp iterate together (ballots inside)
+  uint32_t iters = (n + stride - 1) / stride;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t it = 0; it < iters; it++, i += stride) {
+    bool active = i < n;
+    uint32_t slot = active ? q[i] : 0;
+    uint4 st = make_uint4(0, 0, 0, 0);
+    V3 thr = v3(0.f), rad = v3(0.f);
+    Tail tl;
+    tl.event = 1;
+    tl.isSpecular = false;
+    bool tail = false, shadow = false, missed = false;
+    V3 col = v3(0.f);
+    V3 P, N, Wo, Wi;
+    float lightPDF = 0.f;
+    int lindex = 0;
+    uint32_t mid = 0;
+    if (active) {
+      st = W.st[slot];
+      float4 t4 = W.thr[slot], r4 = W.rad[slot];
+      thr = f4xyz(t4);
+      rad = f4xyz(r4);
+      float4 hit = W.hit[slot];
+      float4 ro = W.ray_o[slot], rdv = W.ray_d[slot];
+      uint32_t leaf = __float_as_uint(hit.w);
+      if (leaf == PT_NO_HIT) {
+        thr *= miss_color(S.miss, f4xyz(rdv));
+        col = rad + clamp3(thr, 0.f, 1.f);  // raygen.cu:81-82
+        missed = true;
+      } else {
+        PrimRec p = load_prim(S.prims, leaf);
+        HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z);
+        mid = rec.index;
+        GpuMaterial m = S.mats[mid];
+        P = rec.P;
+        Wo = rec.Wo;
+        N = rec.shading_normal;
+        switch (m.type) {
+          case PT_MAT_LAMBERTIAN:
+          case PT_MAT_OREN_NAYAR:
+          case PT_MAT_DIFFUSE_LIGHT: {
+            bool isLight = m.type == PT_MAT_DIFFUSE_LIGHT;
+            if (nee_begin(S, st.x, P, N, isLight, Wi, lightPDF, lindex)) {
+              shadow = true;
+            } else {
+              after_nee(m, st.x, P, Wo, N, v3(0.f), thr, rad, tl);
+              tail = true;
+            }
+            break;
+          }
+          case PT_MAT_METAL: {  // programs/materials/metal.cu:38-56
+            V3 reflected = reflect(-Wo, N);
+            tl.direction = reflected + m.p0 * random_in_unit_sphere(st.x);
+            tl.event = 0;
+            tl.origin = P;
+            thr *= v3(m.c0x, m.c0y, m.c0z);
+            tl.isSpecular = true;
+            tail = true;
+            break;
+          }
+          case PT_MAT_DIELECTRIC: {  // programs/materials/dielectric.cu:46-96
+            float ref_idx = m.p0;
+            V3 Wd = -rec.Wo;
+            V3 Nd = N;
+            V3 absorption = v3(1.f);
+            float ni_over_nt;
+            float cosine = dot(Wd, Nd);
+            if (cosine > 0.f) {
+              Nd = -Nd;
+              ni_over_nt = ref_idx;
+              cosine = ref_idx * cosine / length(Wd);
+            } else {
+              ni_over_nt = 1.f / ref_idx;
+              cosine = -cosine / length(Wd);
+            }
+            V3 refracted = v3(0.f);
+            float reflect_prob;
+            if (Refract(Wd, Nd, ni_over_nt, refracted))
+              reflect_prob = schlick(cosine, ref_idx);
+            else
+              reflect_prob = 1.f;
+            if (rnd(st.x) < reflect_prob)
+              tl.direction = reflect(Wd, Nd);
+            else
+              tl.direction = normalize(refracted);
+            tl.event = 0;
+            tl.origin = P;
+            thr *= (v3(m.c0x, m.c0y, m.c0z) * absorption);
+            tl.isSpecular = true;
+            tail = true;
+            break;
+          }
+          case PT_MAT_TORRANCE_SPARROW:
+          case PT_MAT_ASHIKHMIN_SHIRLEY: {
+            V3 Wn = brdf_sample(m, Wo, N, st.x);
+            float pdf = 0.f;
+            V3 attenuation = brdf_eval(m, Wo, Wn, N, pdf);
+            tl.event = 0;
+            tl.origin = P;
+            tl.direction = Wn;
+            if (m.type == PT_MAT_TORRANCE_SPARROW)
+              thr *= clamp3(attenuation / pdf, 0.f, 1.f);
+            else
+              thr *= clamp3(attenuation, 0.f, 1.f);
+            tl.isSpecular = true;
+            tail = true;
+            break;
+          }
+          default:
+            tl.event = 1;
+            tail = true;
+        }
+      }
+    }
+    // shadow rays: queue and park the NEE context
+    uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
+    if (shadow) {
+      W.q_shadow[spos] = slot;
+      W.nee_P[slot] = make_float4(P.x, P.y, P.z, lightPDF);
+      W.nee_N[slot] = make_float4(N.x, N.y, N.z, __int_as_float(lindex));
+      W.nee_Wo[slot] = make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid));
+      W.nee_Wi[slot] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
+      W.st[slot] = st;
+      W.thr[slot] = make_float4(thr.x, thr.y, thr.z, 0.f);
+      W.rad[slot] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    }
+    // misses end here
+    finalize_path(W, c, slot, st.y, col, missed);
+    path_tail(W, c, ctl, slot, st, thr, rad, tl, tail);
+  }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(PT_TRACE_BLOCK) k_trace_shadow(DevScene S, WaveState W,
+                                                                 int max_stack) {
+  extern __shared__ uint2 stack_smem[];
+  uint32_t n = W.ctr->n_shadow;
+  uint32_t nn = 0, np = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t slot = W.q_shadow[i];
+    float4 P = W.nee_P[slot], Wi = W.nee_Wi[slot], N = W.nee_N[slot];
+    TraceHit h = trace_bvh8<COUNT>(S, f4xyz(P), f4xyz(Wi), 1e-3f, PT_RAY_TMAX,
+                                   stack_smem + threadIdx.x, blockDim.x, max_stack,
+                                   &W.ctr->error, nn, np);
+    bool occluded = true;
+    if (h.leaf != PT_NO_HIT) {
+      PrimRec p = load_prim(S.prims, h.leaf);
+      bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
+      occluded = !(is_light && dot(f4xyz(N), f4xyz(Wi)) > 0.f);
+    }
+    W.nee_Wi[slot].w = occluded ? 1.f : 0.f;
+  }
+  if (COUNT) {
+    atomicAdd(&W.ctr->node_fetches, (unsigned long long)nn);
+    atomicAdd(&W.ctr->prim_tests, (unsigned long long)np);
+  }
+}
+
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState W,
+                                                           const WaveCtl* __restrict__ ctlp) {
+  WaveCounters c = *W.ctr;
+  WaveCtl ctl = *ctlp;
+  uint32_t n = c.n_shadow;
+  uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t iters = (n + stride - 1) / stride;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t it = 0; it < iters; it++, i += stride) {
+    bool active = i < n;
+    uint32_t slot = active ? W.q_shadow[i] : 0;
+    uint4 st = make_uint4(0, 0, 0, 0);
+    V3 thr = v3(0.f), rad = v3(0.f);
+    Tail tl;
+    tl.event = 1;
+    tl.isSpecular = false;
+    if (active) {
+      st = W.st[slot];
+      thr = f4xyz(W.thr[slot]);
+      rad = f4xyz(W.rad[slot]);
+      float4 P4 = W.nee_P[slot], N4 = W.nee_N[slot], Wo4 = W.nee_Wo[slot], Wi4 = W.nee_Wi[slot];
+      GpuMaterial m = S.mats[__float_as_uint(Wo4.w)];
+      V3 P = f4xyz(P4), N = f4xyz(N4), Wo = f4xyz(Wo4);
+      V3 direct = nee_end(S, m, st.x, P, Wo, N, f4xyz(Wi4), P4.w, __float_as_int(N4.w),
+                          Wi4.w != 0.f);
+      after_nee(m, st.x, P, Wo, N, direct, thr, rad, tl);
+    }
+    path_tail(W, c, ctl, slot, st, thr, rad, tl, active);
+  }
+}
+
+__global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp) {
+  WaveCounters& c = *W.ctr;
+  uint32_t n_gen = gen_count(c, *ctlp);
+  c.ext_rays += c.n_cur + n_gen;
+  c.shadow_rays += c.n_shadow;
+  c.next_path += n_gen;
+  c.free_head = (c.free_head + n_gen) % (uint32_t)W.slots;
+  c.free_tail = (c.free_tail + c.n_freed) % (uint32_t)W.slots;
+  c.n_free = c.n_free - n_gen + c.n_freed;
+  c.paths_done += c.n_freed;
+  c.n_freed = 0;
+  c.n_cur = c.n_next;
+  c.n_next = 0;
+  c.n_shadow = 0;
+  c.parity ^= 1u;
+  c.iter++;
+}
+
+__global__ void k_init_free(WaveState W) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (uint32_t)W.slots;
+       i += gridDim.x * blockDim.x)
+    W.q_free[i] = i;
+}
+
+// acc[x, H-1-y] += (col, 1) in frame order (programs/raygen.cu:153-166)
+__global__ void k_accumulate(const float4* __restrict__ results, float4* acc, int width,
+                             int height, int frames) {
+  uint32_t WH = (uint32_t)width * (uint32_t)height;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < WH; p += gridDim.x * blockDim.x) {
+    uint32_t x = p % (uint32_t)width, y = p / (uint32_t)width;
+    size_t o = (size_t)(height - 1 - y) * width + x;
+    float4 a = acc[o];
+    for (int f = 0; f < frames; f++) {
+      float4 r = results[(size_t)f * WH + p];
+      a.x += r.x;
+      a.y += r.y;
+      a.z += r.z;
+      a.w += 1.f;
+    }
+    acc[o] = a;
+  }
+}
+
+__global__ void k_paths_out(const float4* __restrict__ results, float* out, uint32_t n) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    float4 r = results[p];
+    out[3 * p] = r.x;
+    out[3 * p + 1] = r.y;
+    out[3 * p + 2] = r.z;
+  }
+}
+
+__global__ void __launch_bounds__(PT_TRACE_BLOCK) k_first_hits(DevScene S, int width, int height,
+                                                               int frame, uint32_t* prim,
+                                                               uint32_t* mat, float* tout,
+                                                               int max_stack, uint32_t* err) {
+  extern __shared__ uint2 stack_smem[];
+  uint32_t WH = (uint32_t)width * (uint32_t)height;
+  uint32_t nn = 0, np = 0;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < WH; p += gridDim.x * blockDim.x) {
+    uint32_t x = p % (uint32_t)width, y = p / (uint32_t)width;
+    uint32_t seed = tea64((uint32_t)width * y + x, (uint32_t)frame);
+    Ray3 r = camera_ray(S.cam, x, y, width, height, seed);
+    TraceHit h = trace_bvh8<false>(S, v3(r.o.x, r.o.y, r.o.z), v3(r.d.x, r.d.y, r.d.z),
+                                   1e-6f, PT_RAY_TMAX, stack_smem + threadIdx.x, blockDim.x,
+                                   max_stack, err, nn, np);
+    if (h.leaf == PT_NO_HIT) {
+      prim[p] = PT_NO_HIT;
+      mat[p] = PT_NO_HIT;
+      tout[p] = 0.f;
+    } else {
+      PrimRec pr = load_prim(S.prims, h.leaf);
+      prim[p] = prim_id(pr);
+      mat[p] = prim_material(pr);
+      tout[p] = h.t;
+    }
+  }
+}
+
+// programs/raygen.cu:136-146
+__global__ void k_resolve(const float4* __restrict__ acc, uchar4* out, int n, int frame) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    float4 a = acc[p];
+    float d = (float)(frame + 1);
+    float r = fmaxf(0.f, fminf(ptm_sqrt(a.x / d), 1.f));
+    float g = fmaxf(0.f, fminf(ptm_sqrt(a.y / d), 1.f));
+    float b = fmaxf(0.f, fminf(ptm_sqrt(a.z / d), 1.f));
+    out[p] = make_uchar4((unsigned char)(int)(255.99 * r), (unsigned char)(int)(255.99 * g),
+                         (unsigned char)(int)(255.99 * b), (unsigned char)(int)(255.99 * 1.f));
+  }
+}
+
+// ------------------------------------------------------- host launchers ---
+namespace pt {
+
+static int g_num_sms = 0;
+
+static int num_sms() {
+  if (!g_num_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+size_t trace_smem(int max_stack) { return (size_t)PT_TRACE_BLOCK * max_stack * sizeof(uint2); }
+
+int wave_grid(int kind, int max_stack) {
+  int blocks = 0;
+  cudaError_t e = cudaSuccess;
+  if (kind == 0)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace<false>, PT_TRACE_BLOCK,
+                                                      trace_smem(max_stack));
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade, PT_SHADE_BLOCK, 0);
+  if (e != cudaSuccess || blocks < 1) blocks = 1;
+  return blocks * num_sms();
+}
+
+cudaError_t set_trace_smem(int max_stack) {
+  size_t sm = trace_smem(max_stack);
+  cudaError_t e;
+  e = cudaFuncSetAttribute(k_trace<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_first_hits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+}
+
+// One wavefront iteration (7 launches).
+void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
+                      bool counters, int trace_grid, int shade_grid, cudaStream_t st,
+                      cudaEvent_t* ev) {
+  size_t sm = trace_smem(max_stack);
+  if (ev) cudaEventRecord(ev[0], st);
+  k_generate<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  if (ev) cudaEventRecord(ev[1], st);
+  if (counters)
+    k_trace<true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack);
+  else
+    k_trace<false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack);
+  if (ev) cudaEventRecord(ev[2], st);
+  k_shade<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  if (ev) cudaEventRecord(ev[3], st);
+  if (counters)
+    k_trace_shadow<true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, max_stack);
+  else
+    k_trace_shadow<false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, max_stack);
+  if (ev) cudaEventRecord(ev[4], st);
+  k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  k_advance<<<1, 1, 0, st>>>(W, ctl);
+  if (ev) cudaEventRecord(ev[5], st);
+}
+
+void launch_init_free(const WaveState& W, cudaStream_t st) {
+  k_init_free<<<num_sms() * 4, 256, 0, st>>>(W);
+}
+
+void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
+                       cudaStream_t st) {
+  k_accumulate<<<num_sms() * 8, 256, 0, st>>>(results, acc, w, h, frames);
+}
+
+void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st) {
+  k_paths_out<<<num_sms() * 8, 256, 0, st>>>(results, out, n);
+}
+
+void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
+                       float* t, int max_stack, uint32_t* err, cudaStream_t st) {
+  k_first_hits<<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack), st>>>(
+      S, w, h, frame, prim, mat, t, max_stack, err);
+}
+
+void launch_resolve(const float4* acc, uchar4* out, int n, int frame, cudaStream_t st) {
+  k_resolve<<<num_sms() * 8, 256, 0, st>>>(acc, out, n, frame);
+}
+
+}  // namespace pt

@@ -1,0 +1,159 @@
+"""ctypes harness of the CPU oracle (liboracle.so, built from oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: the parity checker of the CUDA path tracer.  Only
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import
+this module.  It replays a ptgb.Scene into the oracle and exposes its
+first-hit, per-path and progressive render entry points.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_P = ctypes.c_void_p
+_lib = None
+
+
+def build():
+    """Compiles liboracle.so with the committed Makefile."""
+    r = subprocess.run(["make", "-C", HERE, "-s"], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    L.or_create.restype = _P
+    L.or_destroy.argtypes = [_P]
+    L.or_add_material.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float]
+    L.or_add_prim.argtypes = [_P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
+    L.or_add_mesh.argtypes = [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int, _P, _P,
+                              _P]
+    L.or_add_light.argtypes = [_P, ctypes.c_int, _P, ctypes.c_int, _P]
+    L.or_set_miss.argtypes = [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int]
+    L.or_set_camera.argtypes = [_P, _P, _P, _P] + [ctypes.c_float] * 6
+    L.or_commit.argtypes = [_P]
+    L.or_first_hits.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
+                                ctypes.c_int]
+    L.or_render_paths.argtypes = [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int]
+    L.or_render.argtypes = [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
+    L.or_render.restype = ctypes.c_double
+    L.or_tea64.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    L.or_tea64.restype = ctypes.c_uint32
+    L.or_rnd_stream.argtypes = [ctypes.c_uint32, ctypes.c_int, _P]
+    L.or_math.argtypes = [ctypes.c_int, _P, _P, _P, ctypes.c_int]
+    L.or_trace_ray.argtypes = [_P, _P, _P, ctypes.c_float, _P, _P]
+    L.or_hit_record.argtypes = [_P, _P, _P, _P]
+    _lib = L
+    return L
+
+
+def _f(v):
+    return np.ascontiguousarray(v, dtype=np.float32)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+class Oracle:
+    """A scene loaded into the CPU oracle."""
+
+    def __init__(self, scene):
+        self.L = load()
+        self.h = self.L.or_create()
+        self._keep = []
+        self.load(scene)
+
+    def __del__(self):
+        try:
+            self.L.or_destroy(self.h)
+        except Exception:
+            pass
+
+    def load(self, s):
+        L, h = self.L, self.h
+        for kind, c0, c1, p0, p1 in s.materials:
+            c0a = _f(c0)
+            c1a = _f(c1) if c1 is not None else None
+            L.or_add_material(h, kind, _p(c0a), _p(c1a), p0, p1)
+        for it in s.items:
+            if it[0] == "sphere":
+                _, cen, r, m, xf = it
+                f = _f(list(cen) + [r])
+                L.or_add_prim(h, 1, _p(f), 0, 0, m, _p(xf))
+            elif it[0] == "rect":
+                _, v5, flip, axis, m, xf = it
+                f = _f(v5)
+                L.or_add_prim(h, 2, _p(f), axis, flip, m, _p(xf))
+            elif it[0] == "box":
+                _, p0, p1, m, xf = it
+                f = _f(list(p0) + list(p1))
+                L.or_add_prim(h, 3, _p(f), 0, 0, m, _p(xf))
+            else:
+                _, v, idx, m, mpt, nrm, uv, xf = it
+                mpt_i = None if mpt is None else np.ascontiguousarray(mpt, dtype=np.int32)
+                L.or_add_mesh(h, _p(v), len(v), _p(idx), len(idx), _p(mpt_i),
+                              m if m is not None else 0, _p(nrm), _p(uv), _p(xf))
+        for lt in s.lights:
+            if lt[0] == "rect":
+                _, v5, axis, e = lt
+                L.or_add_light(h, 0, _p(_f(v5)), axis, _p(_f(e)))
+            else:
+                _, cen, r, e = lt
+                L.or_add_light(h, 1, _p(_f(list(cen) + [r])), 0, _p(_f(e)))
+        ms = s.miss
+        if ms[0] == "gradient":
+            L.or_set_miss(h, 0, _p(_f(ms[1])), _p(_f(ms[2])), None, 0, 0, 1)
+        elif ms[0] == "constant":
+            L.or_set_miss(h, 1, _p(_f(ms[1])), None, None, 0, 0, 1)
+        else:
+            rgba = ms[1]
+            L.or_set_miss(h, ms[3], None, None, _p(rgba), rgba.shape[1], rgba.shape[0], ms[2])
+        cf, ca, cu, vfov, aspect, ap, fd, t0, t1 = s.camera
+        L.or_set_camera(h, _p(_f(cf)), _p(_f(ca)), _p(_f(cu)), vfov, aspect, ap, fd, t0, t1)
+        L.or_commit(h)
+
+    def first_hits(self, width, height, frame, threads=0):
+        prim = np.zeros(width * height, dtype=np.int32)
+        mat = np.zeros(width * height, dtype=np.int32)
+        t = np.zeros(width * height, dtype=np.float32)
+        self.L.or_first_hits(self.h, width, height, frame, _p(prim), _p(mat), _p(t),
+                             threads or os.cpu_count())
+        return prim.view(np.uint32), mat.view(np.uint32), t
+
+    @staticmethod
+    def _params(width, height, spp, frame0, max_depth, rr_enable, rr_depth, mode=0, guide=0):
+        return np.array([width, height, spp, frame0, max_depth, rr_enable, rr_depth, mode, guide],
+                        dtype=np.int32)
+
+    def render_paths(self, width, height, frame, pixels, max_depth=50, rr_enable=1, rr_depth=10,
+                     threads=0):
+        pix = np.ascontiguousarray(pixels, dtype=np.uint32)
+        out = np.zeros((len(pix), 3), dtype=np.float32)
+        prm = self._params(width, height, 1, frame, max_depth, rr_enable, rr_depth)
+        self.L.or_render_paths(self.h, _p(prm), frame, _p(pix), len(pix), _p(out),
+                               threads or os.cpu_count())
+        return out
+
+    def render(self, width, height, spp, frame0=0, max_depth=50, rr_enable=1, rr_depth=10,
+               acc=None, pixel_stride=1, pixel_offset=0, threads=0):
+        if acc is None:
+            acc = np.zeros((height, width, 4), dtype=np.float32)
+        prm = self._params(width, height, spp, frame0, max_depth, rr_enable, rr_depth)
+        stats = np.zeros(3, dtype=np.uint64)
+        secs = self.L.or_render(self.h, _p(prm), _p(acc), pixel_stride, pixel_offset,
+                                threads or os.cpu_count(), _p(stats))
+        return acc, {"seconds": secs, "ext_rays": int(stats[0]), "shadow_rays": int(stats[1]),
+                     "paths": int(stats[2])}

@@ -1,0 +1,123 @@
+"""GPU path tracer vs the CPU oracle (same scenes, same per-pixel random
+streams).  Contract: first-hit primitive and material ids bit-exact, per-path
+radiance within 1e-4 relative (the arithmetic is shared bit for bit, so the
+kernels in fact reproduce the oracle exactly)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-4
+
+
+def scenes(ptgb):
+    return {
+        "cornell_ref": (ptgb.cornell_reference(64, 64), 64, 64, dict(rr_depth=10)),
+        "cornell_c1": (ptgb.cornell_c1(64, 64), 64, 64, dict(rr_depth=3)),
+        "spheres_c2": (ptgb.random_spheres(96, 54), 96, 54, dict(rr_depth=10)),
+        "zoo": (ptgb.material_zoo(80, 60), 80, 60, dict(rr_depth=10)),
+        "heightfield_c3": (ptgb.heightfield_scene(96, 54, cells=48, env_w=256, env_h=128), 96, 54,
+                           dict(rr_depth=10)),
+    }
+
+
+@pytest.fixture(scope="module")
+def cases(ptgb_mod, oracle_mod):
+    out = {}
+    for name, (s, w, h, kw) in scenes(ptgb_mod).items():
+        out[name] = (ptgb_mod.GpuRenderer(s), oracle_mod.Oracle(s), w, h, kw)
+    yield out
+    for g, *_ in out.values():
+        g.close()
+
+
+NAMES = ["cornell_ref", "cornell_c1", "spheres_c2", "zoo", "heightfield_c3"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("frame", [0, 5])
+def test_first_hits_exact(cases, name, frame):
+    g, o, w, h, _ = cases[name]
+    gp, gm, gt = g.first_hits(w, h, frame)
+    op, om, ot = o.first_hits(w, h, frame)
+    assert np.array_equal(gp, op), f"{(gp != op).sum()} prim ids differ"
+    assert np.array_equal(gm, om)
+    hit = op != 0xFFFFFFFF
+    assert np.array_equal(gt[hit], ot[hit])
+
+
+def rel_err(a, b):
+    return np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-3)
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("frame", [0, 3])
+def test_path_radiance(cases, ptgb_mod, name, frame):
+    g, o, w, h, kw = cases[name]
+    prm = ptgb_mod.GpuRenderer.params(w, h, 1, frame0=frame, **kw)
+    gpu = g.render_paths(prm).reshape(-1, 3)
+    ref = o.render_paths(w, h, frame, np.arange(w * h), **kw)
+    err = rel_err(gpu, ref)
+    assert err.max() <= REL_TOL, f"max rel err {err.max()}, {np.sum(err > REL_TOL)} paths"
+    exact = np.mean(np.all(gpu == ref, axis=1))
+    assert exact > 0.999
+
+
+@pytest.mark.parametrize("name", ["cornell_c1", "spheres_c2", "zoo"])
+def test_accumulation_matches(cases, ptgb_mod, name):
+    g, o, w, h, kw = cases[name]
+    prm = ptgb_mod.GpuRenderer.params(w, h, 6, frame0=0, **kw)
+    acc = g.render(prm)
+    ref, _ = o.render(w, h, 6, frame0=0, **kw)
+    assert np.array_equal(acc[..., 3], ref[..., 3])
+    assert rel_err(acc[..., :3], ref[..., :3]).max() <= REL_TOL
+    # progressive continuation: frames 6..9 on top
+    prm2 = ptgb_mod.GpuRenderer.params(w, h, 4, frame0=6, **kw)
+    acc2 = g.render(prm2, acc.copy())
+    ref2, _ = o.render(w, h, 4, frame0=6, acc=ref.copy(), **kw)
+    assert rel_err(acc2[..., :3], ref2[..., :3]).max() <= REL_TOL
+    assert np.all(acc2[..., 3] == 10)
+
+
+def test_chunked_render_equals_single(ptgb_mod):
+    """Regeneration with few path slots must not change any path."""
+    s = ptgb_mod.material_zoo(40, 30)
+    a = ptgb_mod.GpuRenderer(s, path_slots=1000)
+    b = ptgb_mod.GpuRenderer(s)
+    prm = ptgb_mod.GpuRenderer.params(40, 30, 5)
+    ra, rb = a.render(prm), b.render(prm)
+    assert np.array_equal(ra, rb)
+    st = a.stats()
+    assert st["paths"] == 40 * 30 * 5 and st["ext_rays"] > st["paths"]
+
+
+def test_resolve_display(cases, ptgb_mod):
+    g, o, w, h, kw = cases["cornell_c1"]
+    acc = g.render(ptgb_mod.GpuRenderer.params(w, h, 2, **kw))
+    disp = g.resolve(acc, 1)
+    ref = np.clip(np.sqrt(acc[..., :3] / 2), 0, 1)
+    assert np.abs(disp[..., :3].astype(np.int32) - (255.99 * ref).astype(np.int32)).max() <= 1
+    assert np.all(disp[..., 3] == 255)
+
+
+def test_errors(ptgb_mod):
+    import ctypes
+    L = ptgb_mod.load_library()
+    ctx = ctypes.c_void_p()
+    assert L.pt_context_create(None, ctypes.byref(ctx)) == 0
+    prm = ptgb_mod.GpuRenderer.params(8, 8, 1)
+    acc = np.zeros((8, 8, 4), dtype=np.float32)
+    rc = L.pt_render(ctx, ctypes.byref(prm), acc.ctypes.data_as(ctypes.c_void_p), None)
+    assert rc == -6  # PT_ESTATE: not committed
+    mid = ctypes.c_uint32()
+    assert L.pt_material_lambertian(ctx, ptgb_mod.f3((1, 1, 1)), ctypes.byref(mid)) == 0
+    assert L.pt_add_sphere(ctx, ptgb_mod.f3((0, 0, 0)), -1.0, 0, None, None) == -1
+    assert L.pt_add_sphere(ctx, ptgb_mod.f3((0, 0, 0)), 1.0, 7, None, None) == -1
+    assert L.pt_add_rect(ctx, 0, 1, 0, 1, 0, 0, 5, 0, None, None) == -1
+    assert L.pt_commit(ctx) == 0
+    bad = ptgb_mod.GpuRenderer.params(0, 8, 1)
+    assert L.pt_render(ctx, ctypes.byref(bad), acc.ctypes.data_as(ctypes.c_void_p), None) == -1
+    assert b"invalid" in L.pt_last_error(ctx)
+    # empty scene renders the miss colour
+    assert L.pt_render(ctx, ctypes.byref(prm), acc.ctypes.data_as(ctypes.c_void_p), None) == 0
+    assert L.pt_context_destroy(ctx) == 0

@@ -818,8 +818,11 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
       for (int i = 0; i < kItersPerGraph; i++)
         for (int k = 0; k < 5; k++) {
           float ms = 0.f;
-          cudaEventElapsedTime(&ms, ctx->tev[6 * i + k], ctx->tev[6 * i + k + 1]);
-          ctx->stats.stage_ms[k] += ms;
+          if (cudaEventElapsedTime(&ms, ctx->tev[6 * i + k], ctx->tev[6 * i + k + 1]) ==
+              cudaSuccess)
+            ctx->stats.stage_ms[k] += ms;
+          else
+            cudaGetLastError();  // a missing sample is not an error of the render
         }
     }
     if (c.error) return fail(ctx, PT_EQUEUE, "traversal stack overflow");
@@ -906,7 +909,7 @@ PT_API int pt_render(pt_context* ctx, const pt_render_params* params, float* acc
   if (!dev) CK(cudaMemcpyAsync(accum_rgba, d_acc, WH * sizeof(float4), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->stats.render_ms = ms;
   return PT_OK;
 }

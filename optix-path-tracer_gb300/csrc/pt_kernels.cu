@@ -788,24 +788,24 @@ void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                       bool counters, int trace_grid, int shade_grid, cudaStream_t st,
                       cudaEvent_t* ev) {
   size_t sm = trace_smem(max_stack);
-  if (ev) cudaEventRecord(ev[0], st);
+  if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
   k_generate<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  if (ev) cudaEventRecord(ev[1], st);
+  if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
   if (counters)
     k_trace<true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack);
   else
     k_trace<false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack);
-  if (ev) cudaEventRecord(ev[2], st);
+  if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
   k_shade<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  if (ev) cudaEventRecord(ev[3], st);
+  if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
   if (counters)
     k_trace_shadow<true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, max_stack);
   else
     k_trace_shadow<false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, max_stack);
-  if (ev) cudaEventRecord(ev[4], st);
+  if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
   k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   k_advance<<<1, 1, 0, st>>>(W, ctl);
-  if (ev) cudaEventRecord(ev[5], st);
+  if (ev) cudaEventRecordWithFlags(ev[5], st, cudaEventRecordExternal);
 }
 
 void launch_init_free(const WaveState& W, cudaStream_t st) {

@@ -330,8 +330,11 @@ def main():
     ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--spp", type=int, default=0, help="override spp (small profiling cases)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
+    if args.spp:
+        wl = wl[:3] + (args.spp,) + wl[4:5] + (wl[5].replace(f"{wl[3]} spp", f"{args.spp} spp"),)
     if args.impl == "reference":
         run_reference(args, wl)
     else:

@@ -66,6 +66,13 @@ def build(verbose=False, force=False):
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB) or _stale(LIB, objs):
         run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    # the C++ facade example (host_includes-style scene code over the C ABI)
+    ex_src = os.path.join(HERE, "examples", "cornell.cpp")
+    ex_bin = os.path.join(HERE, "examples", "cornell")
+    inc = os.path.join(HERE, "..", "include")
+    if _stale(ex_bin, [ex_src, LIB, os.path.join(inc, "pt_scene.hpp")]):
+        run([os.environ.get("CXX", "g++"), "-O2", "-std=c++14", "-I", inc, ex_src, "-o", ex_bin,
+             "-L", HERE, "-lpt", "-Wl,-rpath,$ORIGIN/.."])
     return LIB
 
 

@@ -1,0 +1,68 @@
+"""The C++ facade (include/pt_scene.hpp): it compiles on the host, and the
+reference's Cornell scene written against it (examples/cornell.cpp) renders
+the same image as the Python harness's statement of that scene."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "optix-path-tracer_gb300")
+
+
+def test_facade_header_compiles(tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text('#include "pt_scene.hpp"\nint main(){ pt::Hitable_List l; (void)l; return 0; }\n')
+    r = subprocess.run(["g++", "-std=c++14", "-fsyntax-only", "-Wall", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_compose_matches_python(ptgb_mod, tmp_path):
+    src = tmp_path / "c.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "pt_scene.hpp"
+using namespace pt;
+int main(){
+  std::vector<TransformParameter> ts;
+  ts.emplace_back(Translate_Transform, 0.f, X_AXIS, make_float3(0.f), make_float3(265.f, 0.f, 295.f));
+  ts.emplace_back(Rotate_Transform, 15.f, Y_AXIS, make_float3(0.f), make_float3(0.f));
+  ts.emplace_back(Scale_Transform, 0.f, X_AXIS, make_float3(1.f, 2.f, 3.f), make_float3(0.f));
+  float m[12]; compose(ts, m);
+  for (int i = 0; i < 12; i++) printf("%.9g\n", m[i]);
+}''')
+    exe = tmp_path / "c"
+    subprocess.run(["g++", "-std=c++14", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    out = np.array([float(x) for x in subprocess.check_output([str(exe)]).split()])
+    ref = ptgb_mod.compose([ptgb_mod.mat_translate((265.0, 0.0, 295.0)),
+                            ptgb_mod.mat_rotate(15.0, 1), ptgb_mod.mat_scale((1, 2, 3))])
+    assert np.allclose(out, ref, rtol=1e-6, atol=1e-5)
+
+
+def read_pfm(path):
+    with open(path, "rb") as f:
+        assert f.readline().strip() == b"PF"
+        w, h = map(int, f.readline().split())
+        f.readline()
+        data = np.frombuffer(f.read(), dtype="<f4").reshape(h, w, 3)
+    return data[::-1]
+
+
+@pytest.mark.gpu
+def test_cornell_example_matches_harness(ptgb_mod, tmp_path):
+    exe = os.path.join(PKG, "examples", "cornell")
+    out = tmp_path / "c.pfm"
+    r = subprocess.run([exe, "64", "64", "8", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    img = read_pfm(out)
+    g = ptgb_mod.GpuRenderer(ptgb_mod.cornell_reference(64, 64))
+    acc = g.render(ptgb_mod.GpuRenderer.params(64, 64, 8))
+    g.close()
+    # output rows are stored y-flipped like acc_buffer (raygen.cu:153)
+    ref = acc[..., :3]
+    err = np.abs(img - ref) / np.maximum(np.maximum(np.abs(img), np.abs(ref)), 1e-3)
+    assert err.max() <= 1e-4

@@ -194,6 +194,19 @@ PT_API int pt_resolve_display(pt_context* ctx, const float* accum_rgba, int widt
 
 PT_API int pt_get_stats(pt_context* ctx, pt_stats* out);
 
+/* pt_render for callers that cannot allocate device memory while rendering
+ * (a strict memory pool, or an application that allocates only at start-up).
+ * No counterpart in the reference.  It calls no cudaMalloc/cudaFree: its
+ * wavefront scratch is a fixed 9.5 MiB device array inside libpt.so that
+ * every GPU loading the library holds until exit.  Same results as
+ * pt_render.  accum_rgba must be device memory; images of at most 262144
+ * pixels (PT_EINVAL beyond); fewer paths in flight, so slower.  All calls
+ * share the array: calls whose GPU work overlaps race and must be
+ * serialised.  The first call on a device resolves the array's address
+ * (cudaGetSymbolAddress); make it before any stream capture. */
+PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params* params, float* accum_rgba,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

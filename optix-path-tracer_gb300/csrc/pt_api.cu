@@ -1008,3 +1008,153 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// pt_render_noalloc: rendering for callers that cannot allocate device memory
+// at call time (for example code running under a memory pool that forbids
+// cudaMalloc, or an application that allocates everything at start-up and
+// then only launches).  It performs no cudaMalloc, cudaFree or other
+// allocating call: the wavefront scratch (path-state slots, queues, counters
+// and per-path results) lives in the fixed file-scope device array below,
+// which every GPU that loads this library holds until the process exits.
+//
+// Limits: images of at most PT_NOALLOC_MAX_PIXELS pixels (the per-path
+// result area holds one frame of that size); PT_NOALLOC_SLOTS paths in
+// flight, so it is slower than pt_render on large images.  All calls share
+// the array and it keeps the last call's contents: each call re-initialises
+// the free-slot ring and the counters it needs.  Calls whose GPU work
+// overlaps (several host threads, streams or contexts on one device) race
+// on the array and must be serialised by the caller.
+// The first call on a device resolves the array's device address with
+// cudaGetSymbolAddress; make that first call before any stream capture.
+// ============================================================================
+namespace {
+
+constexpr size_t kNoAllocSlots = 32768;
+constexpr size_t kNoAllocMaxPixels = 262144;  // e.g. 512 x 512
+constexpr size_t kNoAllocBytes =
+    kNoAllocSlots * (9 * sizeof(float4) + sizeof(uint4) + 4 * sizeof(uint32_t)) +
+    256 /* WaveCounters */ + 256 /* WaveCtl */ + kNoAllocMaxPixels * sizeof(float4);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+static void* g_noalloc_ptr[kMaxDevices];  // device address of the array, per device
+
+// Once per device, with that device current: the host-side name of the
+// array is a stand-in, not a device address, so kernels get this pointer.
+static int noalloc_setup(pt_context* ctx, unsigned char** out) {
+  if (ctx->device < 0 || ctx->device >= kMaxDevices) return fail(ctx, PT_EINVAL, "device ordinal");
+  if (!g_noalloc_ptr[ctx->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(ctx, e, "cudaGetSymbolAddress(noalloc scratch)");
+    g_noalloc_ptr[ctx->device] = p;
+  }
+  *out = (unsigned char*)g_noalloc_ptr[ctx->device];
+  return PT_OK;
+}
+
+static WaveState noalloc_wave(unsigned char* base, WaveCtl** ctl) {
+  WaveState W;
+  memset(&W, 0, sizeof(W));
+  size_t s = kNoAllocSlots;
+  float4* f = (float4*)base;
+  W.ray_o = f;
+  W.ray_d = f + s;
+  W.thr = f + 2 * s;
+  W.rad = f + 3 * s;
+  W.hit = f + 4 * s;
+  W.nee_P = f + 5 * s;
+  W.nee_N = f + 6 * s;
+  W.nee_Wo = f + 7 * s;
+  W.nee_Wi = f + 8 * s;
+  W.st = (uint4*)(f + 9 * s);
+  uint32_t* q = (uint32_t*)(W.st + s);
+  W.q[0] = q;
+  W.q[1] = q + s;
+  W.q_shadow = q + 2 * s;
+  W.q_free = q + 3 * s;
+  unsigned char* tail = (unsigned char*)(q + 4 * s);
+  W.ctr = (WaveCounters*)tail;
+  *ctl = (WaveCtl*)(tail + 256);
+  W.results = (float4*)(tail + 512);
+  W.slots = (int)s;
+  return W;
+}
+
+}  // namespace
+
+extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params* p,
+                                        float* accum_rgba, void* stream) {
+  static_assert(sizeof(WaveCounters) <= 256 && sizeof(WaveCtl) <= 256, "scratch layout");
+  if (!ctx) return PT_EINVAL;
+  int rc = check_params(ctx, p);
+  if (rc) return rc;
+  size_t WH = (size_t)p->width * p->height;
+  if (WH > kNoAllocMaxPixels)
+    return fail(ctx, PT_EINVAL,
+                "pt_render_noalloc: image has " + std::to_string(WH) + " pixels, its static "
+                "scratch holds at most " + std::to_string(kNoAllocMaxPixels) + "; use pt_render");
+  if (!accum_rgba || !is_device_ptr(accum_rgba))
+    return fail(ctx, PT_EINVAL, "pt_render_noalloc needs a device accumulator");
+  CK(cudaSetDevice(ctx->device));
+  unsigned char* base = nullptr;
+  rc = noalloc_setup(ctx, &base);
+  if (rc) return rc;
+  WaveCtl* d_ctl = nullptr;
+  WaveState W = noalloc_wave(base, &d_ctl);
+  cudaStream_t st = ctx->stream;
+  CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
+  CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  reset_render_stats(ctx);
+  float4* acc = (float4*)accum_rgba;
+  if (p->frame0 == 0) CK(cudaMemsetAsync(acc, 0, WH * sizeof(float4), st));
+  pt::launch_init_free(W, st);
+  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)p->spp, kNoAllocMaxPixels / WH));
+  WaveCounters& c = *ctx->h_ctr;
+  WaveCtl& ctl = *ctx->h_ctl;
+  for (int f = 0; f < p->spp; f += chunk) {
+    int frames = std::min(chunk, p->spp - f);
+    ctl.width = p->width;
+    ctl.height = p->height;
+    ctl.frame0 = p->frame0 + f;
+    ctl.max_depth = p->max_depth;
+    ctl.rr_enable = p->rr_enable;
+    ctl.rr_depth = p->rr_depth;
+    ctl.mode = p->mode;
+    ctl.guide = p->guide;
+    ctl.chunk_paths = (unsigned long long)WH * frames;
+    CK(cudaMemcpyAsync(d_ctl, &ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, st));
+    memset(&c, 0, sizeof(c));
+    c.n_free = (uint32_t)kNoAllocSlots;  // ring full; every slot is free between chunks
+    CK(cudaMemcpyAsync(W.ctr, &c, sizeof(WaveCounters), cudaMemcpyHostToDevice, st));
+    unsigned long long max_iters = ctl.chunk_paths + (unsigned long long)p->max_depth + 16;
+    unsigned long long iters = 0;
+    while (true) {
+      for (int i = 0; i < kItersPerGraph; i++)
+        pt::launch_iteration(ctx->scene, W, d_ctl, ctx->max_stack, false, ctx->trace_grid,
+                             ctx->shade_grid, st, nullptr);
+      CK(cudaGetLastError());
+      iters += kItersPerGraph;
+      ctx->stats.iterations += kItersPerGraph;
+      ctx->stats.kernel_launches += 7 * kItersPerGraph;
+      CK(cudaMemcpyAsync(ctx->h_ctr, W.ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (c.error) return fail(ctx, PT_EQUEUE, "traversal stack overflow");
+      if (c.next_path >= ctl.chunk_paths && c.n_cur == 0) break;
+      if (iters > max_iters) return fail(ctx, PT_ETIMEOUT, "wavefront did not drain");
+    }
+    ctx->stats.paths += c.paths_done;
+    ctx->stats.ext_rays += c.ext_rays;
+    ctx->stats.shadow_rays += c.shadow_rays;
+    pt::launch_accumulate(W.results, acc, p->width, p->height, frames, st);
+    ctx->stats.kernel_launches += 1;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev1, st));
+  CK(cudaStreamWaitEvent((cudaStream_t)stream, ctx->ev1, 0));
+  CK(cudaStreamSynchronize(st));
+  return PT_OK;
+}
+

@@ -92,6 +92,7 @@ SIGNATURES = {
     "pt_trace_first_hits": [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P],
     "pt_resolve_display": [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P],
     "pt_get_stats": [_P, ctypes.POINTER(Stats)],
+    "pt_render_noalloc": [_P, ctypes.POINTER(RenderParams), _P, _P],
 }
 
 _lib = None

@@ -770,6 +770,8 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   ctl.mode = p->mode;
   ctl.guide = p->guide;
   ctl.chunk_paths = (unsigned long long)p->width * p->height * frames;
+  fastdiv_magic((uint32_t)(p->width * p->height), &ctl.wh_m, &ctl.wh_l);
+  fastdiv_magic((uint32_t)p->width, &ctl.w_m, &ctl.w_l);
   CK(cudaMemcpyAsync(ctx->d_ctl.p, &ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, st));
   WaveCounters& c = *ctx->h_ctr;
   memset(&c, 0, sizeof(c));
@@ -1125,6 +1127,8 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
     ctl.mode = p->mode;
     ctl.guide = p->guide;
     ctl.chunk_paths = (unsigned long long)WH * frames;
+    fastdiv_magic((uint32_t)WH, &ctl.wh_m, &ctl.wh_l);
+    fastdiv_magic((uint32_t)p->width, &ctl.w_m, &ctl.w_l);
     CK(cudaMemcpyAsync(d_ctl, &ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, st));
     memset(&c, 0, sizeof(c));
     c.n_free = (uint32_t)kNoAllocSlots;  // ring full; every slot is free between chunks

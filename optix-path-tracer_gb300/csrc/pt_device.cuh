@@ -311,8 +311,11 @@ struct HitRecord {
 
 // Get_HitRecord of each primitive: programs/hitables/{sphere,aarect,box,
 // triangle}.cu, from the object-space ray, mapped to world space once.
+// need_uv: texture coordinates are computed only when a texture reads them
+// (the materials here use constant colours, so the shading kernels pass
+// false; u, v feed nothing else).
 PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, float t_hit,
-                         float bu, float bv) {
+                         float bu, float bv, bool need_uv = true) {
   HitRecord rec;
   rec.Wo = normalize(-rd);
   int xf = prim_xform(p);
@@ -333,10 +336,13 @@ PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, floa
     V3 T = (rec.P - center) / radius;
     V3 normal = normalize(I ? xnormal(I, T) : T);
     rec.shading_normal = rec.geometric_normal = normal;
-    float phi = pt_atan2f(T.z, T.x);
-    float theta = pt_asinf(T.y);
-    rec.u = 1.f - (phi + PI_F) / (2.f * PI_F);
-    rec.v = (theta + PI_F / 2.f) / PI_F;
+    rec.u = rec.v = 0.f;
+    if (need_uv) {
+      float phi = pt_atan2f(T.z, T.x);
+      float theta = pt_asinf(T.y);
+      rec.u = 1.f - (phi + PI_F) / (2.f * PI_F);
+      rec.v = (theta + PI_F / 2.f) / PI_F;
+    }
   } else if (type == PT_PRIM_RECT) {
     float a0 = p.r0.x, a1 = p.r0.y, b0 = p.r0.z, b1 = p.r1.x;
     int axis = prim_axis(p);
@@ -393,7 +399,7 @@ PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, floa
       V3 Ns = na * b0 + nb * b1 + nc * b2;
       rec.shading_normal = normalize(Ns);
     }
-    if (!(at.w & 2u)) {
+    if (!(at.w & 2u) || !need_uv) {
       rec.u = rec.v = 0.f;
     } else {
       const float* uv = S.uvs;

@@ -10,6 +10,9 @@
 #include "pt_types.h"
 
 #define PT_TRACE_BLOCK 128
+#ifndef PT_TRACE_MINBLOCKS
+#define PT_TRACE_MINBLOCKS 8  /* 64 registers per thread: 32 warps per SM */
+#endif
 #define PT_SHADE_BLOCK 256
 
 struct Ray3 {
@@ -40,7 +43,25 @@ struct WaveCtl {
   int frame0;                     /* frame of path id 0 of this chunk */
   int max_depth, rr_enable, rr_depth, mode, guide;
   unsigned long long chunk_paths; /* paths in this chunk */
+  uint32_t wh_m, wh_l, w_m, w_l;  /* invariant-divisor constants for W*H and W */
 };
+
+/* Unsigned division by an invariant 32-bit divisor d >= 1 (Granlund &
+ * Montgomery 1994, "Division by invariant integers using multiplication",
+ * fig. 4.1): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, then
+ * n / d = (t + ((n - t) >> min(l,1))) >> max(l-1,0) with t = mulhi(m, n). */
+static inline void fastdiv_magic(uint32_t d, uint32_t* m, uint32_t* l) {
+  uint32_t ll = 0;
+  while (ll < 32 && (1ull << ll) < d) ll++;
+  *l = ll;
+  *m = (uint32_t)((((1ull << 32) * ((1ull << ll) - d)) / d) + 1);
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t fastdiv(uint32_t n, uint32_t m, uint32_t l) {
+  uint32_t t = __umulhi(m, n);
+  return (t + ((n - t) >> (l > 0 ? 1u : 0u))) >> (l > 0 ? l - 1 : 0u);
+}
+#endif
 
 /* Path-state arrays (structure of arrays, one entry per slot). */
 struct WaveState {

@@ -63,6 +63,10 @@ __device__ TraceHit trace_bvh8(const DevScene& S, V3 o, V3 d, float tmin, float 
   float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
   WtRay wt = wt_setup(d);
 
+  // per-ray sign selection: the near plane of each axis is the low bound for
+  // a positive direction and the high bound for a negative one
+  const bool negx = ix < 0.f, negy = iy < 0.f, negz = iz < 0.f;
+
   int sp = 0;
   uint32_t cur = 0;
   bool have = S.num_prims > 0;
@@ -71,37 +75,44 @@ __device__ TraceHit trace_bvh8(const DevScene& S, V3 o, V3 d, float tmin, float 
     uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3),
           n4 = __ldg(np + 4);
     if (COUNT) n_nodes++;
+    // child bound q (8 bits) is read as the float f = 1 + q * 2^-15 built by
+    // one byte permute; t = q*a + b = f*A + B with A = 2^15 a, B = b - A
     float sx = __uint_as_float((n0.w & 0xffu) << 23);
     float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
     float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
-    float ax = sx * ix, ay = sy * iy, az = sz * iz;
-    float bx = (__uint_as_float(n0.x) - o.x) * ix;
-    float by = (__uint_as_float(n0.y) - o.y) * iy;
-    float bz = (__uint_as_float(n0.z) - o.z) * iz;
+    float Ax = 32768.0f * (sx * ix), Ay = 32768.0f * (sy * iy), Az = 32768.0f * (sz * iz);
+    float Bx = (__uint_as_float(n0.x) - o.x) * ix - Ax;
+    float By = (__uint_as_float(n0.y) - o.y) * iy - Ay;
+    float Bz = (__uint_as_float(n0.z) - o.z) * iz - Az;
+    // near/far bound words per axis (lo word pair, hi word pair)
+    uint32_t nx0 = negx ? n3.z : n2.x, nx1 = negx ? n3.w : n2.y;
+    uint32_t fx0 = negx ? n2.x : n3.z, fx1 = negx ? n2.y : n3.w;
+    uint32_t ny0 = negy ? n4.x : n2.z, ny1 = negy ? n4.y : n2.w;
+    uint32_t fy0 = negy ? n2.z : n4.x, fy1 = negy ? n2.w : n4.y;
+    uint32_t nz0 = negz ? n4.z : n3.x, nz1 = negz ? n4.w : n3.y;
+    uint32_t fz0 = negz ? n3.x : n4.z, fz1 = negz ? n3.y : n4.w;
     float tlim = tbest * 1.0000005f;
     uint32_t keys[8];
-    uint32_t leafmask = 0;
+    uint32_t leafmask = 0, kmin = 0xffffffffu;
     int nint = 0;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
+      const uint32_t sel = 0x7604u | ((uint32_t)(i & 3) << 4);
       uint32_t meta = byte_of(i < 4 ? n1.z : n1.w, i & 3);
       keys[i] = 0xffffffffu;
-      if (meta == 0) continue;
-      int w = i & 3;
-      float qlx = (float)byte_of(i < 4 ? n2.x : n2.y, w);
-      float qly = (float)byte_of(i < 4 ? n2.z : n2.w, w);
-      float qlz = (float)byte_of(i < 4 ? n3.x : n3.y, w);
-      float qhx = (float)byte_of(i < 4 ? n3.z : n3.w, w);
-      float qhy = (float)byte_of(i < 4 ? n4.x : n4.y, w);
-      float qhz = (float)byte_of(i < 4 ? n4.z : n4.w, w);
-      float t0x = __fmaf_rn(qlx, ax, bx), t1x = __fmaf_rn(qhx, ax, bx);
-      float t0y = __fmaf_rn(qly, ay, by), t1y = __fmaf_rn(qhy, ay, by);
-      float t0z = __fmaf_rn(qlz, az, bz), t1z = __fmaf_rn(qhz, az, bz);
-      float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-      float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tlim));
-      if (tn <= tf) {
+      float tnx = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? nx0 : nx1, 0x3F800000u, sel)), Ax, Bx);
+      float tfx = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? fx0 : fx1, 0x3F800000u, sel)), Ax, Bx);
+      float tny = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? ny0 : ny1, 0x3F800000u, sel)), Ay, By);
+      float tfy = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? fy0 : fy1, 0x3F800000u, sel)), Ay, By);
+      float tnz = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? nz0 : nz1, 0x3F800000u, sel)), Az, Bz);
+      float tfz = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
+      float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+      float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
+      if (meta != 0 && tn <= tf) {
         if (meta & 0x80u) {
-          keys[i] = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
+          uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
+          keys[i] = key;
+          kmin = min(kmin, key);
           nint++;
         } else {
           leafmask |= 1u << i;
@@ -148,7 +159,11 @@ __device__ TraceHit trace_bvh8(const DevScene& S, V3 o, V3 d, float tmin, float 
         }
       }
     }
-    if (nint > 0) {
+    if (nint == 1) {
+      cur = n1.x + (kmin & 7u);
+      continue;
+    }
+    if (nint > 1) {
       // order internal children near to far (sorting network, 19 exchanges)
       cswap(keys[0], keys[1]); cswap(keys[2], keys[3]); cswap(keys[4], keys[5]); cswap(keys[6], keys[7]);
       cswap(keys[0], keys[2]); cswap(keys[1], keys[3]); cswap(keys[4], keys[6]); cswap(keys[5], keys[7]);
@@ -210,7 +225,10 @@ __device__ __forceinline__ void finalize_path(const WaveState& W, const WaveCoun
     W.results[pid] = make_float4(col.x, col.y, col.z, 1.f);
   }
   uint32_t pos = warp_push(&W.ctr->n_freed, done);
-  if (done) W.q_free[(c.free_tail + pos) % (uint32_t)W.slots] = slot;
+  if (done) {
+    uint32_t fi = c.free_tail + pos;  // < 2 * slots
+    W.q_free[fi >= (uint32_t)W.slots ? fi - (uint32_t)W.slots : fi] = slot;
+  }
 }
 
 // raygen.cu:81-122 after the closest-hit program: event dispatch, next
@@ -296,12 +314,16 @@ __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ 
   WaveCtl ctl = *ctlp;
   uint32_t n = gen_count(c, ctl);
   uint32_t WH = (uint32_t)ctl.width * (uint32_t)ctl.height;
+  uint32_t slots = (uint32_t)W.slots;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t slot = W.q_free[(c.free_head + i) % (uint32_t)W.slots];
+    uint32_t fi = c.free_head + i;  // < 2 * slots
+    uint32_t slot = W.q_free[fi >= slots ? fi - slots : fi];
     uint32_t pid = (uint32_t)(c.next_path + i);
-    uint32_t frame = (uint32_t)ctl.frame0 + pid / WH;
-    uint32_t pix = pid % WH;
-    uint32_t x = pix % (uint32_t)ctl.width, y = pix / (uint32_t)ctl.width;
+    uint32_t fr = fastdiv(pid, ctl.wh_m, ctl.wh_l);
+    uint32_t frame = (uint32_t)ctl.frame0 + fr;
+    uint32_t pix = pid - fr * WH;
+    uint32_t y = fastdiv(pix, ctl.w_m, ctl.w_l);
+    uint32_t x = pix - y * (uint32_t)ctl.width;
     uint32_t seed = tea64((uint32_t)ctl.width * y + x, frame);
     Ray3 r = camera_ray(S.cam, x, y, ctl.width, ctl.height, seed);
     // color(): prd.time draw, programs/raygen.cu:69
@@ -317,7 +339,7 @@ __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ 
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(PT_TRACE_BLOCK) k_trace(DevScene S, WaveState W,
+__global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS) k_trace(DevScene S, WaveState W,
                                                           const WaveCtl* __restrict__ ctlp,
                                                           int max_stack) {
   extern __shared__ uint2 stack_smem[];
@@ -490,7 +512,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
         missed = true;
       } else {
         PrimRec p = load_prim(S.prims, leaf);
-        HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z);
+        HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, false);
         mid = rec.index;
         GpuMaterial m = S.mats[mid];
         P = rec.P;
@@ -592,7 +614,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(PT_TRACE_BLOCK) k_trace_shadow(DevScene S, WaveState W,
+__global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS) k_trace_shadow(DevScene S, WaveState W,
                                                                  int max_stack) {
   extern __shared__ uint2 stack_smem[];
   uint32_t n = W.ctr->n_shadow;

@@ -16,7 +16,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpt.so")
+# PT_LIB overrides the library path (A/B builds of the same sources)
+LIB_PATH = os.environ.get("PT_LIB") or os.path.join(HERE, "libpt.so")
 
 PT_X_AXIS, PT_Y_AXIS, PT_Z_AXIS = 0, 1, 2
 MISS_GRADIENT, MISS_CONSTANT, MISS_HDR, MISS_IMG = 0, 1, 2, 3

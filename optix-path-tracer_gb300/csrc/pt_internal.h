@@ -11,7 +11,7 @@
 
 #define PT_TRACE_BLOCK 128
 #ifndef PT_TRACE_MINBLOCKS
-#define PT_TRACE_MINBLOCKS 8  /* 64 registers per thread: 32 warps per SM */
+#define PT_TRACE_MINBLOCKS 6  /* <= 80 registers per thread, no spills */
 #endif
 #define PT_SHADE_BLOCK 256
 

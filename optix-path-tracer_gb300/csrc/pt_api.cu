@@ -84,6 +84,7 @@ struct pt_context {
   DevBuf<GpuLight> d_lights;
   DevBuf<uint4> d_tri_attr;
   DevBuf<float> d_normals, d_uvs;
+  DevBuf<uint32_t> d_leaf_of_id;
   DevScene scene{};
   int bvh_depth = 0;
   size_t bvh_nodes = 0;
@@ -285,6 +286,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_tri_attr.release();
   ctx->d_normals.release();
   ctx->d_uvs.release();
+  ctx->d_leaf_of_id.release();
   ctx->d_slot_f4.release();
   ctx->d_st.release();
   ctx->d_queues.release();
@@ -673,6 +675,9 @@ PT_API int pt_commit(pt_context* ctx) {
   std::vector<float4> env = ctx->env;
   if (env.empty()) env.resize(1);
   CK(ctx->d_env.upload(env.data(), env.size(), st));
+  std::vector<uint32_t> leaf_of_id(n ? n : 1, 0);
+  for (size_t k = 0; k < bvh.leaf_order.size(); k++) leaf_of_id[bvh.leaf_order[k]] = (uint32_t)k;
+  CK(ctx->d_leaf_of_id.upload(leaf_of_id.data(), leaf_of_id.size(), st));
   CK(cudaStreamSynchronize(st));
   DevScene& S = ctx->scene;
   memset(&S, 0, sizeof(S));
@@ -684,6 +689,7 @@ PT_API int pt_commit(pt_context* ctx) {
   S.tri_attr = ctx->d_tri_attr.p;
   S.normals = ctx->d_normals.p;
   S.uvs = ctx->d_uvs.p;
+  S.leaf_of_id = ctx->d_leaf_of_id.p;
   S.num_lights = (int)ctx->lights.size();
   S.num_prims = (int)n;
   S.miss = ctx->miss;
@@ -692,7 +698,7 @@ PT_API int pt_commit(pt_context* ctx) {
   ctx->bvh_depth = bvh.depth;
   ctx->bvh_nodes = nn;
   ctx->max_stack = std::max(1, bvh.depth + 1);
-  if ((size_t)ctx->max_stack * PT_TRACE_BLOCK * 8 > 200 * 1024)
+  if (pt::trace_smem(ctx->max_stack) > 200 * 1024)
     return fail(ctx, PT_EINVAL, "BVH too deep for the traversal stack");
   CK(pt::set_trace_smem(ctx->max_stack));
   ctx->trace_grid = pt::wave_grid(0, ctx->max_stack);

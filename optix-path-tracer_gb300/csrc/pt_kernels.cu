@@ -27,11 +27,48 @@
 
 using namespace ptd;
 
+__device__ __forceinline__ uint32_t gen_count(const WaveCounters& c, const WaveCtl& ctl) {
+  unsigned long long left = ctl.chunk_paths - c.next_path;
+  return (uint32_t)min((unsigned long long)c.n_free, left);
+}
+
+__device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uint32_t y,
+                                           uint32_t Wd, uint32_t Hd, uint32_t& seed) {
+  float u = float((float)x + rnd(seed)) / (float)Wd;
+  float v = float((float)y + rnd(seed)) / (float)Hd;
+  V3 rd = cam.lens_radius * random_in_unit_disk(seed);
+  V3 lens_offset = v3(cam.ux, cam.uy, cam.uz) * rd.x + v3(cam.wx, cam.wy, cam.wz) * rd.y;
+  V3 origin = v3(cam.ox, cam.oy, cam.oz) + lens_offset;
+  V3 direction = v3(cam.lx, cam.ly, cam.lz) + u * v3(cam.hx, cam.hy, cam.hz) +
+                 v * v3(cam.vx, cam.vy, cam.vz) - origin;
+  Ray3 r;
+  r.o = make_float3(origin.x, origin.y, origin.z);
+  r.d = make_float3(direction.x, direction.y, direction.z);
+  return r;
+}
+
 // ------------------------------------------------------------ BVH8 trace --
-struct TraceHit {
-  float t, u, v;
-  uint32_t leaf;  // index into the primitive array (leaf order), PT_NO_HIT if none
-  uint32_t id;    // primitive id
+// Closest hit through the BVH8 with warp-collective leaf tests.
+//
+// Each lane traverses its own ray (node by node, near-to-far, one stack entry
+// per level: the group of a node's remaining internal children).  Primitive
+// tests are not run by the lane that reaches a leaf: after every node step
+// the warp gathers all (ray, primitive) pairs its lanes produced into shared
+// memory and the 32 lanes test them together, merging the results per ray
+// with a 64-bit atomicMin on (t, primitive id) - the order-independent
+// closest-hit rule of the oracle.  Per-lane leaf loops of 1..24 triangles
+// would otherwise serialise the warp.  A lane whose ray is done takes its
+// next ray at once (persistent threads), and a stack group whose nearest
+// child lies beyond the closest hit is dropped without visiting it.
+#define PT_MAX_PAIRS (32 * 24)
+
+struct WarpShared {
+  float4 ro[32];                  // origin, tmin
+  float4 rd[32];                  // direction, tmax
+  float4 wt[32];                  // watertight-test constants Sx, Sy, Sz, axes
+  unsigned long long best[32];    // (t bits << 32) | primitive id
+  uint32_t pair_prim[PT_MAX_PAIRS];
+  uint8_t pair_owner[PT_MAX_PAIRS];
 };
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
@@ -42,162 +79,344 @@ __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
   b = hi;
 }
 
-// Closest hit of (o, d) in (tmin, tmax): lexicographic minimum of (t, id).
-// stk: this thread's column of the block's shared-memory stack (stride
-// blockDim.x), one entry per BVH8 level: (child_base, ranks left | count<<24).
-template <bool COUNT>
-__device__ TraceHit trace_bvh8(const DevScene& S, V3 o, V3 d, float tmin, float tmax, uint2* stk,
-                               int stride, int max_stack, uint32_t* err, uint32_t& n_nodes,
-                               uint32_t& n_prims) {
-  TraceHit h;
-  h.t = tmax;
-  h.u = h.v = 0.f;
-  h.leaf = PT_NO_HIT;
-  h.id = 0xffffffffu;
-  float tbest = tmax;
-  // box-test constants: direction reciprocals kept finite
-  const float eps = 1e-18f;
-  float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
-  float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
-  float dz = fabsf(d.z) < eps ? copysignf(eps, d.z) : d.z;
-  float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-  WtRay wt = wt_setup(d);
+__device__ __forceinline__ WtRay wt_unpack(float4 w) {
+  WtRay r;
+  uint32_t k = __float_as_uint(w.w);
+  r.kx = (int)(k & 3u);
+  r.ky = (int)((k >> 2) & 3u);
+  r.kz = (int)((k >> 4) & 3u);
+  r.Sx = w.x;
+  r.Sy = w.y;
+  r.Sz = w.z;
+  return r;
+}
 
-  // per-ray sign selection: the near plane of each axis is the low bound for
-  // a positive direction and the high bound for a negative one
-  const bool negx = ix < 0.f, negy = iy < 0.f, negz = iz < 0.f;
+// Candidate of one primitive for a world-space ray (object space inside).
+__device__ __forceinline__ bool prim_test(const DevScene& S, const PrimRec& p, V3 o, V3 d,
+                                          const WtRay& wt, float tmin, float tmax, float& t,
+                                          float& bu, float& bv) {
+  int type = prim_type(p);
+  bu = bv = 0.f;
+  if (type == PT_PRIM_TRIANGLE) return tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
+  V3 oo = o, dd = d;
+  int xf = prim_xform(p);
+  if (xf >= 0) {
+    const float4* I = S.xforms + 6 * xf + 3;
+    oo = xpoint(I, o);
+    dd = xvector(I, d);
+  }
+  if (type == PT_PRIM_SPHERE) return sphere_candidate(p, oo, dd, tmin, tmax, t);
+  if (type == PT_PRIM_RECT) return rect_candidate(p, oo, dd, tmin, tmax, t);
+  return box_candidate(p, oo, dd, tmin, tmax, t);
+}
 
+struct FirstHitOut {
+  uint32_t* prim;
+  uint32_t* mat;
+  float* t;
+  int width, height, frame;
+  uint32_t* err;
+};
+
+enum { TRACE_EXT = 0, TRACE_SHADOW = 1, TRACE_FIRST = 2 };
+
+size_t trace_smem_bytes(int max_stack) {
+  return (size_t)(PT_TRACE_BLOCK / 32) * sizeof(WarpShared) +
+         (size_t)PT_TRACE_BLOCK * max_stack * (sizeof(uint2) + sizeof(float));
+}
+
+template <int MODE, bool COUNT>
+__global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
+    k_trace_t(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp, int max_stack,
+              FirstHitOut fo) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  WarpShared& ws = ((WarpShared*)smem)[threadIdx.x >> 5];
+  uint2* stk = (uint2*)(smem + (PT_TRACE_BLOCK / 32) * sizeof(WarpShared)) + threadIdx.x;
+  float* stkt = (float*)((uint2*)(smem + (PT_TRACE_BLOCK / 32) * sizeof(WarpShared)) +
+                         (size_t)max_stack * blockDim.x) + threadIdx.x;
+  const int bd = blockDim.x;
+
+  uint32_t n;
+  WaveCounters c;
+  if (MODE == TRACE_EXT) {
+    c = *W.ctr;
+    n = c.n_cur + gen_count(c, *ctlp);
+  } else if (MODE == TRACE_SHADOW) {
+    n = W.ctr->n_shadow;
+  } else {
+    n = (uint32_t)fo.width * (uint32_t)fo.height;
+  }
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t nn = 0, np = 0;
+
+  // per-lane ray state
+  V3 o = v3(0.f), d = v3(0.f);
+  float tmin = 0.f, tmax = 0.f, ix = 0.f, iy = 0.f, iz = 0.f, tbest = 0.f;
+  bool negx = false, negy = false, negz = false;
+  uint32_t cur = 0, best_id = PT_NO_HIT, slot = 0;
   int sp = 0;
-  uint32_t cur = 0;
-  bool have = S.num_prims > 0;
-  while (have) {
-    const uint4* np = S.nodes + 5 * (size_t)cur;
-    uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3),
-          n4 = __ldg(np + 4);
-    if (COUNT) n_nodes++;
-    // child bound q (8 bits) is read as the float f = 1 + q * 2^-15 built by
-    // one byte permute; t = q*a + b = f*A + B with A = 2^15 a, B = b - A
-    float sx = __uint_as_float((n0.w & 0xffu) << 23);
-    float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
-    float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
-    float Ax = 32768.0f * (sx * ix), Ay = 32768.0f * (sy * iy), Az = 32768.0f * (sz * iz);
-    float Bx = (__uint_as_float(n0.x) - o.x) * ix - Ax;
-    float By = (__uint_as_float(n0.y) - o.y) * iy - Ay;
-    float Bz = (__uint_as_float(n0.z) - o.z) * iz - Az;
-    // near/far bound words per axis (lo word pair, hi word pair)
-    uint32_t nx0 = negx ? n3.z : n2.x, nx1 = negx ? n3.w : n2.y;
-    uint32_t fx0 = negx ? n2.x : n3.z, fx1 = negx ? n2.y : n3.w;
-    uint32_t ny0 = negy ? n4.x : n2.z, ny1 = negy ? n4.y : n2.w;
-    uint32_t fy0 = negy ? n2.z : n4.x, fy1 = negy ? n2.w : n4.y;
-    uint32_t nz0 = negz ? n4.z : n3.x, nz1 = negz ? n4.w : n3.y;
-    uint32_t fz0 = negz ? n3.x : n4.z, fz1 = negz ? n3.y : n4.w;
-    float tlim = tbest * 1.0000005f;
+  bool active = false;
+
+  auto fetch = [&]() {
+    for (; i < n && S.num_prims == 0; i += stride) {
+      // empty scene: every ray misses
+      if (MODE == TRACE_EXT) {
+        uint32_t sl = W.q[c.parity][i];
+        W.hit[sl] = make_float4(W.ray_d[sl].w, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
+      } else if (MODE == TRACE_SHADOW) {
+        W.nee_Wi[W.q_shadow[i]].w = 1.f;
+      } else {
+        fo.prim[i] = PT_NO_HIT;
+        fo.mat[i] = PT_NO_HIT;
+        fo.t[i] = 0.f;
+      }
+    }
+    active = i < n;
+    if (!active) return;
+    if (MODE == TRACE_EXT) {
+      slot = W.q[c.parity][i];
+      float4 ro = W.ray_o[slot], rdv = W.ray_d[slot];
+      o = f4xyz(ro);
+      d = f4xyz(rdv);
+      tmin = ro.w;
+      tmax = rdv.w;
+    } else if (MODE == TRACE_SHADOW) {
+      slot = W.q_shadow[i];
+      o = f4xyz(W.nee_P[slot]);
+      d = f4xyz(W.nee_Wi[slot]);
+      tmin = 1e-3f;
+      tmax = PT_RAY_TMAX;
+    } else {
+      uint32_t x = i % (uint32_t)fo.width, y = i / (uint32_t)fo.width;
+      uint32_t seed = tea64((uint32_t)fo.width * y + x, (uint32_t)fo.frame);
+      Ray3 r = camera_ray(S.cam, x, y, fo.width, fo.height, seed);
+      o = v3(r.o.x, r.o.y, r.o.z);
+      d = v3(r.d.x, r.d.y, r.d.z);
+      tmin = 1e-6f;
+      tmax = PT_RAY_TMAX;
+    }
+    const float eps = 1e-18f;
+    float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
+    float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
+    float dz = fabsf(d.z) < eps ? copysignf(eps, d.z) : d.z;
+    ix = 1.0f / dx;
+    iy = 1.0f / dy;
+    iz = 1.0f / dz;
+    negx = ix < 0.f;
+    negy = iy < 0.f;
+    negz = iz < 0.f;
+    WtRay w = wt_setup(d);
+    ws.ro[lane] = make_float4(o.x, o.y, o.z, tmin);
+    ws.rd[lane] = make_float4(d.x, d.y, d.z, tmax);
+    ws.wt[lane] = make_float4(w.Sx, w.Sy, w.Sz,
+                              __uint_as_float((uint32_t)w.kx | ((uint32_t)w.ky << 2) |
+                                              ((uint32_t)w.kz << 4)));
+    tbest = tmax;
+    best_id = PT_NO_HIT;
+    ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
+    cur = 0;
+    sp = 0;
+  };
+
+  auto finish = [&]() {
+    if (MODE == TRACE_EXT) {
+      float4 h = make_float4(tmax, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
+      if (best_id != PT_NO_HIT) {
+        uint32_t leaf = __ldg(S.leaf_of_id + best_id);
+        PrimRec p = load_prim(S.prims, leaf);
+        float t = tbest, bu = 0.f, bv = 0.f;
+        if (prim_type(p) == PT_PRIM_TRIANGLE) tri_candidate(p, o, wt_setup(d), tmin, tmax, t, bu, bv);
+        h = make_float4(tbest, bu, bv, __uint_as_float(leaf));
+      }
+      W.hit[slot] = h;
+    } else if (MODE == TRACE_SHADOW) {
+      bool occluded = true;
+      if (best_id != PT_NO_HIT) {
+        PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
+        bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
+        occluded = !(is_light && dot(f4xyz(W.nee_N[slot]), d) > 0.f);
+      }
+      W.nee_Wi[slot].w = occluded ? 1.f : 0.f;
+    } else {
+      if (best_id == PT_NO_HIT) {
+        fo.prim[i] = PT_NO_HIT;
+        fo.mat[i] = PT_NO_HIT;
+        fo.t[i] = 0.f;
+      } else {
+        PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
+        fo.prim[i] = best_id;
+        fo.mat[i] = prim_material(p);
+        fo.t[i] = tbest;
+      }
+    }
+  };
+
+  fetch();
+  while (__any_sync(0xffffffffu, active)) {
+    uint32_t leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0, kmin = 0xffffffffu;
     uint32_t keys[8];
-    uint32_t leafmask = 0, kmin = 0xffffffffu;
     int nint = 0;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-      const uint32_t sel = 0x7604u | ((uint32_t)(i & 3) << 4);
-      uint32_t meta = byte_of(i < 4 ? n1.z : n1.w, i & 3);
-      keys[i] = 0xffffffffu;
-      float tnx = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? nx0 : nx1, 0x3F800000u, sel)), Ax, Bx);
-      float tfx = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? fx0 : fx1, 0x3F800000u, sel)), Ax, Bx);
-      float tny = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? ny0 : ny1, 0x3F800000u, sel)), Ay, By);
-      float tfy = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? fy0 : fy1, 0x3F800000u, sel)), Ay, By);
-      float tnz = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? nz0 : nz1, 0x3F800000u, sel)), Az, Bz);
-      float tfz = __fmaf_rn(__uint_as_float(__byte_perm(i < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
-      float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-      float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
-      if (meta != 0 && tn <= tf) {
-        if (meta & 0x80u) {
-          uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
-          keys[i] = key;
-          kmin = min(kmin, key);
-          nint++;
-        } else {
-          leafmask |= 1u << i;
+    for (int k = 0; k < 8; k++) keys[k] = 0xffffffffu;
+    if (active) {
+      const uint4* nptr = S.nodes + 5 * (size_t)cur;
+      uint4 n0 = __ldg(nptr), n1 = __ldg(nptr + 1), n2 = __ldg(nptr + 2), n3 = __ldg(nptr + 3),
+            n4 = __ldg(nptr + 4);
+      if (COUNT) nn++;
+      child_base = n1.x;
+      pbase = n1.y;
+      mlo = n1.z;
+      mhi = n1.w;
+      // child bound q (8 bits) is read as the float f = 1 + q * 2^-15 built by
+      // one byte permute; t = q*a + b = f*A + B with A = 2^15 a, B = b - A
+      float sx = __uint_as_float((n0.w & 0xffu) << 23);
+      float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
+      float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
+      float Ax = 32768.0f * (sx * ix), Ay = 32768.0f * (sy * iy), Az = 32768.0f * (sz * iz);
+      float Bx = (__uint_as_float(n0.x) - o.x) * ix - Ax;
+      float By = (__uint_as_float(n0.y) - o.y) * iy - Ay;
+      float Bz = (__uint_as_float(n0.z) - o.z) * iz - Az;
+      uint32_t nx0 = negx ? n3.z : n2.x, nx1 = negx ? n3.w : n2.y;
+      uint32_t fx0 = negx ? n2.x : n3.z, fx1 = negx ? n2.y : n3.w;
+      uint32_t ny0 = negy ? n4.x : n2.z, ny1 = negy ? n4.y : n2.w;
+      uint32_t fy0 = negy ? n2.z : n4.x, fy1 = negy ? n2.w : n4.y;
+      uint32_t nz0 = negz ? n4.z : n3.x, nz1 = negz ? n4.w : n3.y;
+      uint32_t fz0 = negz ? n3.x : n4.z, fz1 = negz ? n3.y : n4.w;
+      float tlim = tbest * 1.0000005f;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const uint32_t sel = 0x7604u | ((uint32_t)(k & 3) << 4);
+        uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
+        float tnx = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x3F800000u, sel)), Ax, Bx);
+        float tfx = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x3F800000u, sel)), Ax, Bx);
+        float tny = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x3F800000u, sel)), Ay, By);
+        float tfy = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x3F800000u, sel)), Ay, By);
+        float tnz = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x3F800000u, sel)), Az, Bz);
+        float tfz = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
+        float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
+        if (meta != 0 && tn <= tf) {
+          if (meta & 0x80u) {
+            uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
+            keys[k] = key;
+            kmin = min(kmin, key);
+            nint++;
+          } else {
+            leafmask |= 1u << k;
+          }
         }
       }
     }
-    // leaves of this node: test their primitives now
-    while (leafmask) {
-      int i = __ffs(leafmask) - 1;
-      leafmask &= leafmask - 1;
-      uint32_t meta = byte_of(i < 4 ? n1.z : n1.w, i & 3);
-      uint32_t first = n1.y + (meta & 31u), cnt = meta >> 5;
-      for (uint32_t k = 0; k < cnt; k++) {
-        uint32_t pi = first + k;
+    // ---- warp-collective primitive tests
+    uint32_t cnt = 0;
+    {
+      uint32_t m = leafmask;
+      while (m) {
+        int k = __ffs(m) - 1;
+        m &= m - 1;
+        cnt += byte_of(k < 4 ? mlo : mhi, k & 3) >> 5;
+      }
+    }
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, incl, dd);
+      if (lane >= dd) incl += t;
+    }
+    uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total) {
+      uint32_t off = incl - cnt;
+      uint32_t m = leafmask;
+      while (m) {
+        int k = __ffs(m) - 1;
+        m &= m - 1;
+        uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
+        uint32_t first = pbase + (meta & 31u);
+        for (uint32_t q = 0; q < (meta >> 5); q++) {
+          ws.pair_prim[off] = first + q;
+          ws.pair_owner[off] = (uint8_t)lane;
+          off++;
+        }
+      }
+      __syncwarp();
+      for (uint32_t j = lane; j < total; j += 32) {
+        uint32_t pi = ws.pair_prim[j];
+        uint32_t ow = ws.pair_owner[j];
         PrimRec p = load_prim(S.prims, pi);
-        if (COUNT) n_prims++;
-        int type = prim_type(p);
-        float t = 0.f, bu = 0.f, bv = 0.f;
-        bool ok;
-        if (type == PT_PRIM_TRIANGLE) {
-          ok = tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
-        } else {
-          V3 oo = o, dd = d;
-          int xf = prim_xform(p);
-          if (xf >= 0) {
-            const float4* I = S.xforms + 6 * xf + 3;
-            oo = xpoint(I, o);
-            dd = xvector(I, d);
-          }
-          if (type == PT_PRIM_SPHERE) ok = sphere_candidate(p, oo, dd, tmin, tmax, t);
-          else if (type == PT_PRIM_RECT) ok = rect_candidate(p, oo, dd, tmin, tmax, t);
-          else ok = box_candidate(p, oo, dd, tmin, tmax, t);
-        }
-        if (ok) {
-          uint32_t id = prim_id(p);
-          if (t < tbest || (t == tbest && id < h.id)) {
-            tbest = t;
-            h.t = t;
-            h.u = bu;
-            h.v = bv;
-            h.leaf = pi;
-            h.id = id;
-          }
+        if (COUNT) np++;
+        float4 ro = ws.ro[ow], rdv = ws.rd[ow];
+        float t, bu, bv;
+        if (prim_test(S, p, f4xyz(ro), f4xyz(rdv), wt_unpack(ws.wt[ow]), ro.w, rdv.w, t, bu, bv)) {
+          unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
+          atomicMin(&ws.best[ow], key);
         }
       }
+      __syncwarp();
+      if (active) {
+        unsigned long long k = ws.best[lane];
+        tbest = __uint_as_float((uint32_t)(k >> 32));
+        best_id = (uint32_t)k;
+      }
     }
-    if (nint == 1) {
-      cur = n1.x + (kmin & 7u);
-      continue;
-    }
-    if (nint > 1) {
-      // order internal children near to far (sorting network, 19 exchanges)
-      cswap(keys[0], keys[1]); cswap(keys[2], keys[3]); cswap(keys[4], keys[5]); cswap(keys[6], keys[7]);
-      cswap(keys[0], keys[2]); cswap(keys[1], keys[3]); cswap(keys[4], keys[6]); cswap(keys[5], keys[7]);
-      cswap(keys[1], keys[2]); cswap(keys[5], keys[6]); cswap(keys[0], keys[4]); cswap(keys[3], keys[7]);
-      cswap(keys[1], keys[5]); cswap(keys[2], keys[6]);
-      cswap(keys[1], keys[4]); cswap(keys[3], keys[6]);
-      cswap(keys[2], keys[4]); cswap(keys[3], keys[5]);
-      cswap(keys[3], keys[4]);
-      uint32_t base = n1.x;
-      if (nint > 1) {
+    // ---- next node: nearest internal child, else the deepest pending group
+    if (active) {
+      if (nint == 1) {
+        cur = child_base + (kmin & 7u);
+      } else if (nint > 1) {
+        cswap(keys[0], keys[1]); cswap(keys[2], keys[3]); cswap(keys[4], keys[5]); cswap(keys[6], keys[7]);
+        cswap(keys[0], keys[2]); cswap(keys[1], keys[3]); cswap(keys[4], keys[6]); cswap(keys[5], keys[7]);
+        cswap(keys[1], keys[2]); cswap(keys[5], keys[6]); cswap(keys[0], keys[4]); cswap(keys[3], keys[7]);
+        cswap(keys[1], keys[5]); cswap(keys[2], keys[6]);
+        cswap(keys[1], keys[4]); cswap(keys[3], keys[6]);
+        cswap(keys[2], keys[4]); cswap(keys[3], keys[5]);
+        cswap(keys[3], keys[4]);
         uint32_t list = 0;
 #pragma unroll
         for (int j = 7; j >= 1; j--)
           if (j < nint) list = (list << 3) | (keys[j] & 7u);
         if (sp >= max_stack) {
-          atomicOr(err, 1u);
+          atomicOr(MODE == TRACE_FIRST ? fo.err : &W.ctr->error, 1u);
+          sp = 0;  // abandon this ray (the host reports the error)
+          finish();
+          i += stride;
+          fetch();
+        } else {
+          stk[sp * bd] = make_uint2(child_base, list | ((uint32_t)(nint - 1) << 24));
+          stkt[sp * bd] = __uint_as_float(keys[1] & 0xfffffff8u);  // nearest remaining child
+          sp++;
+          cur = child_base + (keys[0] & 7u);
+        }
+      } else {
+        bool found = false;
+        float tlim = tbest * 1.0000005f;
+        while (sp > 0) {
+          uint2 e = stk[(sp - 1) * bd];
+          if (stkt[(sp - 1) * bd] > tlim) {  // every child of the group starts beyond the hit
+            sp--;
+            continue;
+          }
+          uint32_t cn = e.y >> 24, list = e.y & 0xffffffu;
+          cur = e.x + (list & 7u);
+          cn--;
+          if (cn == 0) sp--;
+          else stk[(sp - 1) * bd] = make_uint2(e.x, (list >> 3) | (cn << 24));
+          found = true;
           break;
         }
-        stk[sp * stride] = make_uint2(base, list | ((uint32_t)(nint - 1) << 24));
-        sp++;
+        if (!found) {
+          finish();
+          i += stride;
+          fetch();
+        }
       }
-      cur = base + (keys[0] & 7u);
-      continue;
     }
-    // pop the next child of the deepest pending group
-    if (sp == 0) break;
-    uint2 e = stk[(sp - 1) * stride];
-    uint32_t cnt = e.y >> 24, list = e.y & 0xffffffu;
-    cur = e.x + (list & 7u);
-    cnt--;
-    if (cnt == 0) sp--;
-    else stk[(sp - 1) * stride] = make_uint2(e.x, (list >> 3) | (cnt << 24));
   }
-  return h;
+  if (COUNT) {
+    atomicAdd(&W.ctr->node_fetches, (unsigned long long)nn);
+    atomicAdd(&W.ctr->prim_tests, (unsigned long long)np);
+  }
 }
 
 // -------------------------------------------------- warp-aggregated push --
@@ -289,26 +508,6 @@ __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters
 }
 
 // ------------------------------------------------------------- kernels ----
-__device__ __forceinline__ uint32_t gen_count(const WaveCounters& c, const WaveCtl& ctl) {
-  unsigned long long left = ctl.chunk_paths - c.next_path;
-  return (uint32_t)min((unsigned long long)c.n_free, left);
-}
-
-__device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uint32_t y,
-                                           uint32_t Wd, uint32_t Hd, uint32_t& seed) {
-  float u = float((float)x + rnd(seed)) / (float)Wd;
-  float v = float((float)y + rnd(seed)) / (float)Hd;
-  V3 rd = cam.lens_radius * random_in_unit_disk(seed);
-  V3 lens_offset = v3(cam.ux, cam.uy, cam.uz) * rd.x + v3(cam.wx, cam.wy, cam.wz) * rd.y;
-  V3 origin = v3(cam.ox, cam.oy, cam.oz) + lens_offset;
-  V3 direction = v3(cam.lx, cam.ly, cam.lz) + u * v3(cam.hx, cam.hy, cam.hz) +
-                 v * v3(cam.vx, cam.vy, cam.vz) - origin;
-  Ray3 r;
-  r.o = make_float3(origin.x, origin.y, origin.z);
-  r.d = make_float3(direction.x, direction.y, direction.z);
-  return r;
-}
-
 __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
@@ -335,28 +534,6 @@ __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ 
     W.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
     W.st[slot] = make_uint4(seed, pid, 0u, 0u);
     W.q[c.parity][c.n_cur + i] = slot;
-  }
-}
-
-template <bool COUNT>
-__global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS) k_trace(DevScene S, WaveState W,
-                                                          const WaveCtl* __restrict__ ctlp,
-                                                          int max_stack) {
-  extern __shared__ uint2 stack_smem[];
-  WaveCounters c = *W.ctr;
-  uint32_t n = c.n_cur + gen_count(c, *ctlp);
-  const uint32_t* q = W.q[c.parity];
-  uint32_t nn = 0, np = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t slot = q[i];
-    float4 ro = W.ray_o[slot], rd = W.ray_d[slot];
-    TraceHit h = trace_bvh8<COUNT>(S, f4xyz(ro), f4xyz(rd), ro.w, rd.w, stack_smem + threadIdx.x,
-                                   blockDim.x, max_stack, &W.ctr->error, nn, np);
-    W.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.leaf));
-  }
-  if (COUNT) {
-    atomicAdd(&W.ctr->node_fetches, (unsigned long long)nn);
-    atomicAdd(&W.ctr->prim_tests, (unsigned long long)np);
   }
 }
 
@@ -613,32 +790,6 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
   }
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS) k_trace_shadow(DevScene S, WaveState W,
-                                                                 int max_stack) {
-  extern __shared__ uint2 stack_smem[];
-  uint32_t n = W.ctr->n_shadow;
-  uint32_t nn = 0, np = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t slot = W.q_shadow[i];
-    float4 P = W.nee_P[slot], Wi = W.nee_Wi[slot], N = W.nee_N[slot];
-    TraceHit h = trace_bvh8<COUNT>(S, f4xyz(P), f4xyz(Wi), 1e-3f, PT_RAY_TMAX,
-                                   stack_smem + threadIdx.x, blockDim.x, max_stack,
-                                   &W.ctr->error, nn, np);
-    bool occluded = true;
-    if (h.leaf != PT_NO_HIT) {
-      PrimRec p = load_prim(S.prims, h.leaf);
-      bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
-      occluded = !(is_light && dot(f4xyz(N), f4xyz(Wi)) > 0.f);
-    }
-    W.nee_Wi[slot].w = occluded ? 1.f : 0.f;
-  }
-  if (COUNT) {
-    atomicAdd(&W.ctr->node_fetches, (unsigned long long)nn);
-    atomicAdd(&W.ctr->prim_tests, (unsigned long long)np);
-  }
-}
-
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState W,
                                                            const WaveCtl* __restrict__ ctlp) {
   WaveCounters c = *W.ctr;
@@ -722,33 +873,6 @@ __global__ void k_paths_out(const float4* __restrict__ results, float* out, uint
   }
 }
 
-__global__ void __launch_bounds__(PT_TRACE_BLOCK) k_first_hits(DevScene S, int width, int height,
-                                                               int frame, uint32_t* prim,
-                                                               uint32_t* mat, float* tout,
-                                                               int max_stack, uint32_t* err) {
-  extern __shared__ uint2 stack_smem[];
-  uint32_t WH = (uint32_t)width * (uint32_t)height;
-  uint32_t nn = 0, np = 0;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < WH; p += gridDim.x * blockDim.x) {
-    uint32_t x = p % (uint32_t)width, y = p / (uint32_t)width;
-    uint32_t seed = tea64((uint32_t)width * y + x, (uint32_t)frame);
-    Ray3 r = camera_ray(S.cam, x, y, width, height, seed);
-    TraceHit h = trace_bvh8<false>(S, v3(r.o.x, r.o.y, r.o.z), v3(r.d.x, r.d.y, r.d.z),
-                                   1e-6f, PT_RAY_TMAX, stack_smem + threadIdx.x, blockDim.x,
-                                   max_stack, err, nn, np);
-    if (h.leaf == PT_NO_HIT) {
-      prim[p] = PT_NO_HIT;
-      mat[p] = PT_NO_HIT;
-      tout[p] = 0.f;
-    } else {
-      PrimRec pr = load_prim(S.prims, h.leaf);
-      prim[p] = prim_id(pr);
-      mat[p] = prim_material(pr);
-      tout[p] = h.t;
-    }
-  }
-}
-
 // programs/raygen.cu:136-146
 __global__ void k_resolve(const float4* __restrict__ acc, uchar4* out, int n, int frame) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
@@ -777,32 +901,33 @@ static int num_sms() {
   return g_num_sms;
 }
 
-size_t trace_smem(int max_stack) { return (size_t)PT_TRACE_BLOCK * max_stack * sizeof(uint2); }
+size_t trace_smem(int max_stack) { return trace_smem_bytes(max_stack); }
 
 int wave_grid(int kind, int max_stack) {
   int blocks = 0;
   cudaError_t e = cudaSuccess;
   if (kind == 0)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace<false>, PT_TRACE_BLOCK,
-                                                      trace_smem(max_stack));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace_t<TRACE_EXT, false>,
+                                                      PT_TRACE_BLOCK, trace_smem(max_stack));
   else
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade, PT_SHADE_BLOCK, 0);
   if (e != cudaSuccess || blocks < 1) blocks = 1;
   return blocks * num_sms();
 }
 
+template <typename K>
+static cudaError_t smem_attr(K k, size_t sm) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+}
+
 cudaError_t set_trace_smem(int max_stack) {
   size_t sm = trace_smem(max_stack);
   cudaError_t e;
-  e = cudaFuncSetAttribute(k_trace<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_first_hits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if ((e = smem_attr(k_trace_t<TRACE_EXT, false>, sm)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_EXT, true>, sm)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false>, sm)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true>, sm)) != cudaSuccess) return e;
+  return smem_attr(k_trace_t<TRACE_FIRST, false>, sm);
 }
 
 // One wavefront iteration (7 launches).
@@ -810,20 +935,21 @@ void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                       bool counters, int trace_grid, int shade_grid, cudaStream_t st,
                       cudaEvent_t* ev) {
   size_t sm = trace_smem(max_stack);
+  FirstHitOut none{};
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
   k_generate<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
   if (counters)
-    k_trace<true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack);
+    k_trace_t<TRACE_EXT, true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   else
-    k_trace<false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack);
+    k_trace_t<TRACE_EXT, false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
   k_shade<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
   if (counters)
-    k_trace_shadow<true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, max_stack);
+    k_trace_t<TRACE_SHADOW, true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   else
-    k_trace_shadow<false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, max_stack);
+    k_trace_t<TRACE_SHADOW, false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
   k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   k_advance<<<1, 1, 0, st>>>(W, ctl);
@@ -845,8 +971,10 @@ void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_
 
 void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
                        float* t, int max_stack, uint32_t* err, cudaStream_t st) {
-  k_first_hits<<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack), st>>>(
-      S, w, h, frame, prim, mat, t, max_stack, err);
+  FirstHitOut fo{prim, mat, t, w, h, frame, err};
+  WaveState none{};
+  k_trace_t<TRACE_FIRST, false><<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack), st>>>(
+      S, none, nullptr, max_stack, fo);
 }
 
 void launch_resolve(const float4* acc, uchar4* out, int n, int frame, cudaStream_t st) {

@@ -90,6 +90,7 @@ struct DevScene {
                                .w bit0 = has normals, bit1 = has uvs */
   const float* normals;     /* 3 floats per attribute vertex */
   const float* uvs;         /* 2 floats per attribute vertex */
+  const uint32_t* leaf_of_id; /* primitive id -> position in the leaf-ordered records */
   int num_lights;
   int num_prims;
   int root_leaf;            /* 1 if the root is a single leaf (<= 3 prims): node 0 still exists */

@@ -254,7 +254,20 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
   };
 
   fetch();
-  while (__any_sync(0xffffffffu, active)) {
+  bool idle = false;  // finished a ray, next one not loaded yet
+  while (true) {
+    // idle lanes load their next rays together once half the warp waits
+    // (or nothing else runs), so the warp pays one load latency per batch
+    uint32_t busy = __ballot_sync(0xffffffffu, active);
+    uint32_t waiting = __ballot_sync(0xffffffffu, idle);
+    if (waiting && (__popc(waiting) >= 16 || busy == 0)) {
+      if (idle) {
+        idle = false;
+        fetch();
+      }
+      busy = __ballot_sync(0xffffffffu, active);
+    }
+    if (!busy) break;
     uint32_t leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0, kmin = 0xffffffffu;
     uint32_t keys[8];
     int nint = 0;
@@ -326,7 +339,36 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
       if (lane >= dd) incl += t;
     }
     uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total) {
+    uint32_t mx = __reduce_max_sync(0xffffffffu, cnt);
+    if (total && mx * 32u <= 2u * total) {
+      // balanced: each lane tests its own primitives (at least half the
+      // lane-slots do work)
+      uint32_t m = leafmask;
+      float4 w4 = ws.wt[lane];
+      WtRay wt = wt_unpack(w4);
+      unsigned long long bk = ws.best[lane];
+      while (m) {
+        int k = __ffs(m) - 1;
+        m &= m - 1;
+        uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
+        uint32_t first = pbase + (meta & 31u);
+        for (uint32_t q = 0; q < (meta >> 5); q++) {
+          PrimRec p = load_prim(S.prims, first + q);
+          if (COUNT) np++;
+          float t, bu, bv;
+          if (prim_test(S, p, o, d, wt, tmin, tmax, t, bu, bv)) {
+            unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
+            bk = min(bk, key);
+          }
+        }
+      }
+      if (cnt) {
+        ws.best[lane] = bk;
+        tbest = __uint_as_float((uint32_t)(bk >> 32));
+        best_id = (uint32_t)bk;
+      }
+    } else if (total) {
+      // unbalanced: spread the (ray, primitive) pairs over the warp
       uint32_t off = incl - cnt;
       uint32_t m = leafmask;
       while (m) {
@@ -381,7 +423,8 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
           sp = 0;  // abandon this ray (the host reports the error)
           finish();
           i += stride;
-          fetch();
+          active = false;
+          idle = true;
         } else {
           stk[sp * bd] = make_uint2(child_base, list | ((uint32_t)(nint - 1) << 24));
           stkt[sp * bd] = __uint_as_float(keys[1] & 0xfffffff8u);  // nearest remaining child
@@ -408,7 +451,8 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
         if (!found) {
           finish();
           i += stride;
-          fetch();
+          active = false;
+          idle = true;
         }
       }
     }

@@ -61,6 +61,9 @@ __device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uin
 // next ray at once (persistent threads), and a stack group whose nearest
 // child lies beyond the closest hit is dropped without visiting it.
 #define PT_MAX_PAIRS (32 * 24)
+#ifndef PT_REFETCH_MIN
+#define PT_REFETCH_MIN 16  // idle lanes that trigger loading new rays
+#endif
 
 struct WarpShared {
   float4 ro[32];                  // origin, tmin
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
       // empty scene: every ray misses
       if (MODE == TRACE_EXT) {
         uint32_t sl = W.q[c.parity][i];
-        W.hit[sl] = make_float4(W.ray_d[sl].w, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
+        __stcs(&W.hit[sl], make_float4(W.ray_d[sl].w, 0.f, 0.f, __uint_as_float(PT_NO_HIT)));
       } else if (MODE == TRACE_SHADOW) {
         W.nee_Wi[W.q_shadow[i]].w = 1.f;
       } else {
@@ -177,15 +180,15 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
     if (!active) return;
     if (MODE == TRACE_EXT) {
       slot = W.q[c.parity][i];
-      float4 ro = W.ray_o[slot], rdv = W.ray_d[slot];
+      float4 ro = __ldcs(&W.ray_o[slot]), rdv = __ldcs(&W.ray_d[slot]);
       o = f4xyz(ro);
       d = f4xyz(rdv);
       tmin = ro.w;
       tmax = rdv.w;
     } else if (MODE == TRACE_SHADOW) {
       slot = W.q_shadow[i];
-      o = f4xyz(W.nee_P[slot]);
-      d = f4xyz(W.nee_Wi[slot]);
+      o = f4xyz(__ldcs(&W.nee_P[slot]));
+      d = f4xyz(__ldcs(&W.nee_Wi[slot]));
       tmin = 1e-3f;
       tmax = PT_RAY_TMAX;
     } else {
@@ -230,13 +233,13 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
         if (prim_type(p) == PT_PRIM_TRIANGLE) tri_candidate(p, o, wt_setup(d), tmin, tmax, t, bu, bv);
         h = make_float4(tbest, bu, bv, __uint_as_float(leaf));
       }
-      W.hit[slot] = h;
+      __stcs(&W.hit[slot], h);
     } else if (MODE == TRACE_SHADOW) {
       bool occluded = true;
       if (best_id != PT_NO_HIT) {
         PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
         bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
-        occluded = !(is_light && dot(f4xyz(W.nee_N[slot]), d) > 0.f);
+        occluded = !(is_light && dot(f4xyz(__ldcs(&W.nee_N[slot])), d) > 0.f);
       }
       W.nee_Wi[slot].w = occluded ? 1.f : 0.f;
     } else {
@@ -260,7 +263,7 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
     // (or nothing else runs), so the warp pays one load latency per batch
     uint32_t busy = __ballot_sync(0xffffffffu, active);
     uint32_t waiting = __ballot_sync(0xffffffffu, idle);
-    if (waiting && (__popc(waiting) >= 16 || busy == 0)) {
+    if (waiting && (__popc(waiting) >= PT_REFETCH_MIN || busy == 0)) {
       if (idle) {
         idle = false;
         fetch();
@@ -485,7 +488,7 @@ __device__ __forceinline__ void finalize_path(const WaveState& W, const WaveCoun
     if (!(col.x == col.x)) col.x = 0.f;
     if (!(col.y == col.y)) col.y = 0.f;
     if (!(col.z == col.z)) col.z = 0.f;
-    W.results[pid] = make_float4(col.x, col.y, col.z, 1.f);
+    __stcs(&W.results[pid], make_float4(col.x, col.y, col.z, 1.f));
   }
   uint32_t pos = warp_push(&W.ctr->n_freed, done);
   if (done) {
@@ -537,11 +540,11 @@ __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters
           done = true;
         } else {
           cont = true;
-          W.ray_o[slot] = make_float4(tl.origin.x, tl.origin.y, tl.origin.z, 1e-3f);
-          W.ray_d[slot] = make_float4(tl.direction.x, tl.direction.y, tl.direction.z, PT_RAY_TMAX);
-          W.thr[slot] = make_float4(thr.x, thr.y, thr.z, 0.f);
-          W.rad[slot] = make_float4(rad.x, rad.y, rad.z, 0.f);
-          W.st[slot] = make_uint4(st.x, st.y, depth | ((uint32_t)prevSpec << 16), 0u);
+          __stcs(&W.ray_o[slot], make_float4(tl.origin.x, tl.origin.y, tl.origin.z, 1e-3f));
+          __stcs(&W.ray_d[slot], make_float4(tl.direction.x, tl.direction.y, tl.direction.z, PT_RAY_TMAX));
+          __stcs(&W.thr[slot], make_float4(thr.x, thr.y, thr.z, 0.f));
+          __stcs(&W.rad[slot], make_float4(rad.x, rad.y, rad.z, 0.f));
+          __stcs(&W.st[slot], make_uint4(st.x, st.y, depth | ((uint32_t)prevSpec << 16), 0u));
         }
       }
     }
@@ -572,11 +575,11 @@ __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ 
     // color(): prd.time draw, programs/raygen.cu:69
     float tm = S.cam.time0 + rnd(seed) * (S.cam.time1 - S.cam.time0);
     (void)tm;
-    W.ray_o[slot] = make_float4(r.o.x, r.o.y, r.o.z, 1e-6f);
-    W.ray_d[slot] = make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX);
-    W.thr[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-    W.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    W.st[slot] = make_uint4(seed, pid, 0u, 0u);
+    __stcs(&W.ray_o[slot], make_float4(r.o.x, r.o.y, r.o.z, 1e-6f));
+    __stcs(&W.ray_d[slot], make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX));
+    __stcs(&W.thr[slot], make_float4(1.f, 1.f, 1.f, 0.f));
+    __stcs(&W.rad[slot], make_float4(0.f, 0.f, 0.f, 0.f));
+    __stcs(&W.st[slot], make_uint4(seed, pid, 0u, 0u));
     W.q[c.parity][c.n_cur + i] = slot;
   }
 }
@@ -720,12 +723,12 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
     int lindex = 0;
     uint32_t mid = 0;
     if (active) {
-      st = W.st[slot];
-      float4 t4 = W.thr[slot], r4 = W.rad[slot];
+      st = __ldcs(&W.st[slot]);
+      float4 t4 = __ldcs(&W.thr[slot]), r4 = __ldcs(&W.rad[slot]);
       thr = f4xyz(t4);
       rad = f4xyz(r4);
-      float4 hit = W.hit[slot];
-      float4 ro = W.ray_o[slot], rdv = W.ray_d[slot];
+      float4 hit = __ldcs(&W.hit[slot]);
+      float4 ro = __ldcs(&W.ray_o[slot]), rdv = __ldcs(&W.ray_d[slot]);
       uint32_t leaf = __float_as_uint(hit.w);
       if (leaf == PT_NO_HIT) {
         thr *= miss_color(S.miss, f4xyz(rdv));
@@ -820,13 +823,13 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
     uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
     if (shadow) {
       W.q_shadow[spos] = slot;
-      W.nee_P[slot] = make_float4(P.x, P.y, P.z, lightPDF);
-      W.nee_N[slot] = make_float4(N.x, N.y, N.z, __int_as_float(lindex));
-      W.nee_Wo[slot] = make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid));
-      W.nee_Wi[slot] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
-      W.st[slot] = st;
-      W.thr[slot] = make_float4(thr.x, thr.y, thr.z, 0.f);
-      W.rad[slot] = make_float4(rad.x, rad.y, rad.z, 0.f);
+      __stcs(&W.nee_P[slot], make_float4(P.x, P.y, P.z, lightPDF));
+      __stcs(&W.nee_N[slot], make_float4(N.x, N.y, N.z, __int_as_float(lindex)));
+      __stcs(&W.nee_Wo[slot], make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid)));
+      __stcs(&W.nee_Wi[slot], make_float4(Wi.x, Wi.y, Wi.z, 0.f));
+      __stcs(&W.st[slot], st);
+      __stcs(&W.thr[slot], make_float4(thr.x, thr.y, thr.z, 0.f));
+      __stcs(&W.rad[slot], make_float4(rad.x, rad.y, rad.z, 0.f));
     }
     // misses end here
     finalize_path(W, c, slot, st.y, col, missed);
@@ -851,10 +854,10 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState
     tl.event = 1;
     tl.isSpecular = false;
     if (active) {
-      st = W.st[slot];
-      thr = f4xyz(W.thr[slot]);
-      rad = f4xyz(W.rad[slot]);
-      float4 P4 = W.nee_P[slot], N4 = W.nee_N[slot], Wo4 = W.nee_Wo[slot], Wi4 = W.nee_Wi[slot];
+      st = __ldcs(&W.st[slot]);
+      thr = f4xyz(__ldcs(&W.thr[slot]));
+      rad = f4xyz(__ldcs(&W.rad[slot]));
+      float4 P4 = __ldcs(&W.nee_P[slot]), N4 = __ldcs(&W.nee_N[slot]), Wo4 = __ldcs(&W.nee_Wo[slot]), Wi4 = __ldcs(&W.nee_Wi[slot]);
       GpuMaterial m = S.mats[__float_as_uint(Wo4.w)];
       V3 P = f4xyz(P4), N = f4xyz(N4), Wo = f4xyz(Wo4);
       V3 direct = nee_end(S, m, st.x, P, Wo, N, f4xyz(Wi4), P4.w, __float_as_int(N4.w),

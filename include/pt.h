@@ -197,7 +197,7 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out);
 /* pt_render for callers that cannot allocate device memory while rendering
  * (a strict memory pool, or an application that allocates only at start-up).
  * No counterpart in the reference.  It calls no cudaMalloc/cudaFree: its
- * wavefront scratch is a fixed 9.5 MiB device array inside libpt.so that
+ * wavefront scratch is a fixed 8.5 MiB device array inside libpt.so that
  * every GPU loading the library holds until exit.  Same results as
  * pt_render.  accum_rgba must be device memory; images of at most 262144
  * pixels (PT_EINVAL beyond); fewer paths in flight, so slower.  All calls

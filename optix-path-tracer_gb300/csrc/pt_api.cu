@@ -91,9 +91,8 @@ struct pt_context {
   // ---- wavefront state
   int slots = 0;
   WaveState W{};
-  DevBuf<float4> d_slot_f4;   // 10 float4 arrays
-  DevBuf<uint4> d_st;
-  DevBuf<uint32_t> d_queues;  // 4 queues
+  DevBuf<float4> d_slot_f4;   // PT_SLOT_F4 float4 arrays of `slots` entries
+  DevBuf<uint4> d_slot_u4;    // PT_SLOT_U4 uint4 arrays
   DevBuf<WaveCounters> d_ctr;
   DevBuf<WaveCtl> d_ctl;
   DevBuf<float4> d_results;
@@ -106,7 +105,6 @@ struct pt_context {
   bool graph_counters = false;
   bool graph_timing = false;
   std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
-  bool wave_dirty = false;  // free-slot ring must be rebuilt (a render failed)
   int max_stack = 0;
   int trace_grid = 0, shade_grid = 0;
   pt_stats stats{};
@@ -288,8 +286,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_uvs.release();
   ctx->d_leaf_of_id.release();
   ctx->d_slot_f4.release();
-  ctx->d_st.release();
-  ctx->d_queues.release();
+  ctx->d_slot_u4.release();
   ctx->d_ctr.release();
   ctx->d_ctl.release();
   ctx->d_results.release();
@@ -713,6 +710,27 @@ PT_API int pt_commit(pt_context* ctx) {
 }
 
 // ------------------------------------------------------------------- render
+// Carves the wavefront arrays out of one float4 block and one uint4 block.
+static void carve_wave(WaveState& W, float4* f, uint4* u, size_t s) {
+  for (int k = 0; k < 2; k++) {
+    PathBuf& b = W.path[k];
+    b.ray_o = f + (4 * k + 0) * s;
+    b.ray_d = f + (4 * k + 1) * s;
+    b.thr = f + (4 * k + 2) * s;
+    b.rad = f + (4 * k + 3) * s;
+    b.st = u + k * s;
+  }
+  W.hit = f + 8 * s;
+  W.sh.P = f + 9 * s;
+  W.sh.N = f + 10 * s;
+  W.sh.Wo = f + 11 * s;
+  W.sh.Wi = f + 12 * s;
+  W.sh.thr = f + 13 * s;
+  W.sh.rad = f + 14 * s;
+  W.sh.st = u + 2 * s;
+  W.slots = (int)s;
+}
+
 static int ensure_wave(pt_context* ctx, size_t results_needed) {
   int slots = ctx->opt.path_slots > 0 ? ctx->opt.path_slots : (1 << 21);
   if (ctx->slots != slots || !ctx->d_slot_f4.p) {
@@ -720,36 +738,13 @@ static int ensure_wave(pt_context* ctx, size_t results_needed) {
       cudaGraphExecDestroy(ctx->graph);
       ctx->graph = nullptr;
     }
-    CK(ctx->d_slot_f4.ensure((size_t)slots * 10));
-    CK(ctx->d_st.ensure((size_t)slots));
-    CK(ctx->d_queues.ensure((size_t)slots * 4));
+    CK(ctx->d_slot_f4.ensure((size_t)slots * PT_SLOT_F4));
+    CK(ctx->d_slot_u4.ensure((size_t)slots * PT_SLOT_U4));
     CK(ctx->d_ctr.ensure(1));
     CK(ctx->d_ctl.ensure(1));
     ctx->slots = slots;
-    WaveState& W = ctx->W;
-    float4* f = ctx->d_slot_f4.p;
-    size_t s = (size_t)slots;
-    W.ray_o = f;
-    W.ray_d = f + s;
-    W.thr = f + 2 * s;
-    W.rad = f + 3 * s;
-    W.hit = f + 4 * s;
-    W.nee_P = f + 5 * s;
-    W.nee_N = f + 6 * s;
-    W.nee_Wo = f + 7 * s;
-    W.nee_Wi = f + 8 * s;
-    W.st = ctx->d_st.p;
-    W.q[0] = ctx->d_queues.p;
-    W.q[1] = ctx->d_queues.p + s;
-    W.q_shadow = ctx->d_queues.p + 2 * s;
-    W.q_free = ctx->d_queues.p + 3 * s;
-    W.ctr = ctx->d_ctr.p;
-    W.slots = slots;
-    ctx->wave_dirty = true;
-  }
-  if (ctx->wave_dirty) {
-    pt::launch_init_free(ctx->W, ctx->stream);
-    ctx->wave_dirty = false;
+    carve_wave(ctx->W, ctx->d_slot_f4.p, ctx->d_slot_u4.p, (size_t)slots);
+    ctx->W.ctr = ctx->d_ctr.p;
   }
   if (ctx->d_results.n < results_needed || !ctx->d_results.p) {
     if (ctx->graph) {
@@ -781,9 +776,6 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   CK(cudaMemcpyAsync(ctx->d_ctl.p, &ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, st));
   WaveCounters& c = *ctx->h_ctr;
   memset(&c, 0, sizeof(c));
-  c.n_free = (uint32_t)ctx->slots;
-  c.free_head = 0;
-  c.free_tail = 0;  // ring full: tail == head (mod slots)
   CK(cudaMemcpyAsync(ctx->d_ctr.p, &c, sizeof(WaveCounters), cudaMemcpyHostToDevice, st));
   bool counters = ctx->opt.enable_counters != 0;
   bool timing = ctx->opt.enable_timing != 0;
@@ -837,7 +829,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     if (c.next_path >= ctl.chunk_paths && c.n_cur == 0) break;
     if (iters > max_iters) return fail(ctx, PT_ETIMEOUT, "wavefront did not drain");
   }
-  ctx->stats.paths += c.paths_done;
+  ctx->stats.paths += ctl.chunk_paths;
   ctx->stats.ext_rays += c.ext_rays;
   ctx->stats.shadow_rays += c.shadow_rays;
   ctx->stats.node_fetches += c.node_fetches;
@@ -878,10 +870,7 @@ static int render_device(pt_context* ctx, const pt_render_params* p, float4* d_a
   for (int f = 0; f < p->spp; f += chunk) {
     int frames = std::min(chunk, p->spp - f);
     rc = run_chunk(ctx, p, p->frame0 + f, frames);
-    if (rc) {
-      ctx->wave_dirty = true;
-      return rc;
-    }
+    if (rc) return rc;
     pt::launch_accumulate(ctx->d_results.p, d_acc, p->width, p->height, frames, st);
     ctx->stats.kernel_launches += 1;
   }
@@ -942,10 +931,7 @@ PT_API int pt_render_paths(pt_context* ctx, const pt_render_params* params, floa
   if (rc) return rc;
   p.frame0 = params->frame0;
   rc = run_chunk(ctx, &p, p.frame0, 1);
-  if (rc) {
-    ctx->wave_dirty = true;
-    return rc;
-  }
+  if (rc) return rc;
   bool dev = is_device_ptr(out_rgb);
   float* d_out = out_rgb;
   if (!dev) {
@@ -1029,8 +1015,8 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out) {
 // Limits: images of at most PT_NOALLOC_MAX_PIXELS pixels (the per-path
 // result area holds one frame of that size); PT_NOALLOC_SLOTS paths in
 // flight, so it is slower than pt_render on large images.  All calls share
-// the array and it keeps the last call's contents: each call re-initialises
-// the free-slot ring and the counters it needs.  Calls whose GPU work
+// the array and it keeps the last call's contents: each call resets the
+// counters it needs; the path arrays are written before they are read.  Calls whose GPU work
 // overlaps (several host threads, streams or contexts on one device) race
 // on the array and must be serialised by the caller.
 // The first call on a device resolves the array's device address with
@@ -1038,10 +1024,10 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out) {
 // ============================================================================
 namespace {
 
-constexpr size_t kNoAllocSlots = 32768;
+constexpr size_t kNoAllocSlots = 16384;
 constexpr size_t kNoAllocMaxPixels = 262144;  // e.g. 512 x 512
 constexpr size_t kNoAllocBytes =
-    kNoAllocSlots * (9 * sizeof(float4) + sizeof(uint4) + 4 * sizeof(uint32_t)) +
+    kNoAllocSlots * (PT_SLOT_F4 * sizeof(float4) + PT_SLOT_U4 * sizeof(uint4)) +
     256 /* WaveCounters */ + 256 /* WaveCtl */ + kNoAllocMaxPixels * sizeof(float4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
@@ -1068,26 +1054,12 @@ static WaveState noalloc_wave(unsigned char* base, WaveCtl** ctl) {
   memset(&W, 0, sizeof(W));
   size_t s = kNoAllocSlots;
   float4* f = (float4*)base;
-  W.ray_o = f;
-  W.ray_d = f + s;
-  W.thr = f + 2 * s;
-  W.rad = f + 3 * s;
-  W.hit = f + 4 * s;
-  W.nee_P = f + 5 * s;
-  W.nee_N = f + 6 * s;
-  W.nee_Wo = f + 7 * s;
-  W.nee_Wi = f + 8 * s;
-  W.st = (uint4*)(f + 9 * s);
-  uint32_t* q = (uint32_t*)(W.st + s);
-  W.q[0] = q;
-  W.q[1] = q + s;
-  W.q_shadow = q + 2 * s;
-  W.q_free = q + 3 * s;
-  unsigned char* tail = (unsigned char*)(q + 4 * s);
+  uint4* u = (uint4*)(f + PT_SLOT_F4 * s);
+  carve_wave(W, f, u, s);
+  unsigned char* tail = (unsigned char*)(u + PT_SLOT_U4 * s);
   W.ctr = (WaveCounters*)tail;
   *ctl = (WaveCtl*)(tail + 256);
   W.results = (float4*)(tail + 512);
-  W.slots = (int)s;
   return W;
 }
 
@@ -1118,7 +1090,6 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
   reset_render_stats(ctx);
   float4* acc = (float4*)accum_rgba;
   if (p->frame0 == 0) CK(cudaMemsetAsync(acc, 0, WH * sizeof(float4), st));
-  pt::launch_init_free(W, st);
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)p->spp, kNoAllocMaxPixels / WH));
   WaveCounters& c = *ctx->h_ctr;
   WaveCtl& ctl = *ctx->h_ctl;
@@ -1136,8 +1107,7 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
     fastdiv_magic((uint32_t)WH, &ctl.wh_m, &ctl.wh_l);
     fastdiv_magic((uint32_t)p->width, &ctl.w_m, &ctl.w_l);
     CK(cudaMemcpyAsync(d_ctl, &ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, st));
-    memset(&c, 0, sizeof(c));
-    c.n_free = (uint32_t)kNoAllocSlots;  // ring full; every slot is free between chunks
+    memset(&c, 0, sizeof(c));  // no live path; the counters start at zero
     CK(cudaMemcpyAsync(W.ctr, &c, sizeof(WaveCounters), cudaMemcpyHostToDevice, st));
     unsigned long long max_iters = ctl.chunk_paths + (unsigned long long)p->max_depth + 16;
     unsigned long long iters = 0;
@@ -1155,7 +1125,7 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
       if (c.next_path >= ctl.chunk_paths && c.n_cur == 0) break;
       if (iters > max_iters) return fail(ctx, PT_ETIMEOUT, "wavefront did not drain");
     }
-    ctx->stats.paths += c.paths_done;
+    ctx->stats.paths += ctl.chunk_paths;
     ctx->stats.ext_rays += c.ext_rays;
     ctx->stats.shadow_rays += c.shadow_rays;
     pt::launch_accumulate(W.results, acc, p->width, p->height, frames, st);

@@ -19,19 +19,15 @@ struct Ray3 {
   float3 o, d;
 };
 
-/* Queue counters of the streaming wavefront, in device memory. */
+/* Counters of the streaming wavefront, in device memory. */
 struct WaveCounters {
-  uint32_t n_cur;        /* paths in the current extension queue (before generation) */
-  uint32_t n_next;       /* paths pushed into the next extension queue */
-  uint32_t n_shadow;     /* shadow rays queued this iteration */
-  uint32_t n_free;       /* free slots in the ring q_free[free_head ...] */
-  uint32_t n_freed;      /* slots freed this iteration (appended at free_tail) */
-  uint32_t free_head, free_tail;
-  uint32_t parity;       /* which of q[0], q[1] is current */
+  uint32_t n_cur;        /* live paths at the start of the current buffer (before generation) */
+  uint32_t n_next;       /* paths written to the next buffer */
+  uint32_t n_shadow;     /* paths parked at a shadow ray this iteration */
+  uint32_t parity;       /* which path buffer is current */
   uint32_t error;        /* bit 0: traversal stack overflow */
   uint32_t iter;
   unsigned long long next_path;   /* next path id of the chunk to generate */
-  unsigned long long paths_done;
   unsigned long long ext_rays, shadow_rays;
   unsigned long long node_fetches, prim_tests;
 };
@@ -63,20 +59,37 @@ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, uint32_t m, uint32_t l) 
 }
 #endif
 
-/* Path-state arrays (structure of arrays, one entry per slot). */
-struct WaveState {
+/* Path state, structure of arrays, stored in queue order: entry i of the
+ * current buffer is the i-th live path of this iteration.  Paths that
+ * continue are written compacted into the other buffer of the pair, so
+ * every kernel reads and writes its arrays contiguously. */
+struct PathBuf {
   float4 *ray_o, *ray_d;      /* origin+tmin, direction+tmax */
   float4 *thr, *rad;          /* throughput, radiance */
   uint4* st;                  /* seed, path id, depth|prevSpecular<<16 */
-  float4* hit;                /* t, u, v, leaf index */
-  float4 *nee_P, *nee_N, *nee_Wo, *nee_Wi; /* parked Direct_Light context */
-  uint32_t* q[2];             /* extension queues (ping-pong) */
-  uint32_t* q_shadow;
-  uint32_t* q_free;           /* ring of free slots */
+};
+
+/* Paths parked at a shadow ray (Direct_Light context), in shadow-queue
+ * order. */
+struct ShadowBuf {
+  float4 *P, *N, *Wo, *Wi;    /* P+light pdf, N+light index, Wo+material, Wi+occluded */
+  float4 *thr, *rad;
+  uint4* st;
+};
+
+struct WaveState {
+  PathBuf path[2];            /* ping-pong: path[parity] is current */
+  float4* hit;                /* t, u, v, leaf index: by position in the current buffer */
+  ShadowBuf sh;
   WaveCounters* ctr;
   float4* results;            /* per path of the chunk: colour */
-  int slots;
+  int slots;                  /* capacity of each buffer */
 };
+
+/* float4 arrays per slot: 2 x 4 (path buffers) + 1 (hit) + 6 (shadow), and
+ * 3 uint4 state arrays. */
+#define PT_SLOT_F4 15
+#define PT_SLOT_U4 3
 
 namespace pt {
 size_t trace_smem(int max_stack);
@@ -87,7 +100,6 @@ cudaError_t set_trace_smem(int max_stack);
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
                       bool counters, int trace_grid, int shade_grid, cudaStream_t st,
                       cudaEvent_t* ev);
-void launch_init_free(const WaveState& W, cudaStream_t st);
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
                        cudaStream_t st);
 void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st);

@@ -2,22 +2,24 @@
  * pt_kernels.cu - wavefront path tracing kernels for sm_103a.
  *
  * One path = one (pixel, frame) sample of programs/raygen.cu:148-167.  The
- * reference runs each path in one OptiX megakernel thread; here a fixed pool
- * of path slots streams through stage kernels, and a slot whose path ends
- * is refilled with the next path (regeneration), so the pool stays full:
+ * reference runs each path in one OptiX megakernel thread; here the live
+ * paths stream through stage kernels, and new paths top the buffer up to its
+ * capacity every iteration (regeneration), so the GPU stays full:
  *
  *   k_generate      renderPixel up to color()'s loop: TEA seed, jitter,
  *                   thin-lens camera ray, time draw (raygen.cu:148-162,50-69)
- *   k_trace         closest hit through the BVH8 (replaces rtTrace)
+ *   k_trace_t<EXT>  closest hit through the BVH8 (replaces rtTrace)
  *   k_shade         miss programs, Get_HitRecord, closest-hit programs; the
  *                   NEE of Direct_Light stops at the shadow ray
- *   k_trace_shadow  shadow rays (programs/hit.cu:16-24, closest-hit rule)
+ *   k_trace_t<SHADOW> shadow rays (programs/hit.cu:16-24, closest-hit rule)
  *   k_finish        rest of Direct_Light (MIS), BSDF continuation
- *   k_advance       queue bookkeeping (one thread)
- * Paths that continue are compacted into the next extension queue with
- * warp-aggregated atomics (ballot + popc prefix); ended paths write their
- * colour to a per-path result slot, and k_accumulate adds results to the
- * accumulator in frame order, so the image does not depend on scheduling.
+ *   k_advance       counter bookkeeping (one thread)
+ * Path state is kept in queue order: paths that continue are appended,
+ * compacted with warp-aggregated atomics (ballot + popc prefix), to the other
+ * buffer of a ping-pong pair, so every kernel streams its arrays
+ * contiguously.  Ended paths write their colour to a per-path result slot,
+ * and k_accumulate adds results to the accumulator in frame order, so the
+ * image does not depend on scheduling.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -27,9 +29,10 @@
 
 using namespace ptd;
 
-__device__ __forceinline__ uint32_t gen_count(const WaveCounters& c, const WaveCtl& ctl) {
+__device__ __forceinline__ uint32_t gen_count(const WaveCounters& c, const WaveCtl& ctl,
+                                              uint32_t slots) {
   unsigned long long left = ctl.chunk_paths - c.next_path;
-  return (uint32_t)min((unsigned long long)c.n_free, left);
+  return (uint32_t)min((unsigned long long)(slots - c.n_cur), left);
 }
 
 __device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uint32_t y,
@@ -62,7 +65,7 @@ __device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uin
 // child lies beyond the closest hit is dropped without visiting it.
 #define PT_MAX_PAIRS (32 * 24)
 #ifndef PT_REFETCH_MIN
-#define PT_REFETCH_MIN 16  // idle lanes that trigger loading new rays
+#define PT_REFETCH_MIN 32  // idle lanes that trigger loading new rays (32: the whole warp)
 #endif
 
 struct WarpShared {
@@ -144,7 +147,7 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
   WaveCounters c;
   if (MODE == TRACE_EXT) {
     c = *W.ctr;
-    n = c.n_cur + gen_count(c, *ctlp);
+    n = c.n_cur + gen_count(c, *ctlp, (uint32_t)W.slots);
   } else if (MODE == TRACE_SHADOW) {
     n = W.ctr->n_shadow;
   } else {
@@ -166,10 +169,9 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
     for (; i < n && S.num_prims == 0; i += stride) {
       // empty scene: every ray misses
       if (MODE == TRACE_EXT) {
-        uint32_t sl = W.q[c.parity][i];
-        __stcs(&W.hit[sl], make_float4(W.ray_d[sl].w, 0.f, 0.f, __uint_as_float(PT_NO_HIT)));
+        W.hit[i] = make_float4(W.path[c.parity].ray_d[i].w, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
       } else if (MODE == TRACE_SHADOW) {
-        W.nee_Wi[W.q_shadow[i]].w = 1.f;
+        W.sh.Wi[i].w = 1.f;
       } else {
         fo.prim[i] = PT_NO_HIT;
         fo.mat[i] = PT_NO_HIT;
@@ -179,16 +181,16 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
     active = i < n;
     if (!active) return;
     if (MODE == TRACE_EXT) {
-      slot = W.q[c.parity][i];
-      float4 ro = __ldcs(&W.ray_o[slot]), rdv = __ldcs(&W.ray_d[slot]);
+      slot = i;
+      float4 ro = W.path[c.parity].ray_o[i], rdv = W.path[c.parity].ray_d[i];
       o = f4xyz(ro);
       d = f4xyz(rdv);
       tmin = ro.w;
       tmax = rdv.w;
     } else if (MODE == TRACE_SHADOW) {
-      slot = W.q_shadow[i];
-      o = f4xyz(__ldcs(&W.nee_P[slot]));
-      d = f4xyz(__ldcs(&W.nee_Wi[slot]));
+      slot = i;
+      o = f4xyz(W.sh.P[i]);
+      d = f4xyz(W.sh.Wi[i]);
       tmin = 1e-3f;
       tmax = PT_RAY_TMAX;
     } else {
@@ -233,15 +235,15 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
         if (prim_type(p) == PT_PRIM_TRIANGLE) tri_candidate(p, o, wt_setup(d), tmin, tmax, t, bu, bv);
         h = make_float4(tbest, bu, bv, __uint_as_float(leaf));
       }
-      __stcs(&W.hit[slot], h);
+      W.hit[slot] = h;
     } else if (MODE == TRACE_SHADOW) {
       bool occluded = true;
       if (best_id != PT_NO_HIT) {
         PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
         bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
-        occluded = !(is_light && dot(f4xyz(__ldcs(&W.nee_N[slot])), d) > 0.f);
+        occluded = !(is_light && dot(f4xyz(W.sh.N[slot]), d) > 0.f);
       }
-      W.nee_Wi[slot].w = occluded ? 1.f : 0.f;
+      W.sh.Wi[slot].w = occluded ? 1.f : 0.f;
     } else {
       if (best_id == PT_NO_HIT) {
         fo.prim[i] = PT_NO_HIT;
@@ -479,40 +481,34 @@ __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool active) {
 }
 
 // ---------------------------------------------------------- path state ----
-// st.x = seed, st.y = path id in the chunk, st.z = depth | prevSpecular<<16,
-// st.w = unused
-__device__ __forceinline__ void finalize_path(const WaveState& W, const WaveCounters& c,
-                                              uint32_t slot, uint32_t pid, V3 col, bool done) {
+// st.x = seed, st.y = path id in the chunk, st.z = depth | prevSpecular<<16
+__device__ __forceinline__ void finalize_path(const WaveState& W, uint32_t pid, V3 col) {
   // de_nan, programs/raygen.cu:126-134
-  if (done) {
-    if (!(col.x == col.x)) col.x = 0.f;
-    if (!(col.y == col.y)) col.y = 0.f;
-    if (!(col.z == col.z)) col.z = 0.f;
-    __stcs(&W.results[pid], make_float4(col.x, col.y, col.z, 1.f));
-  }
-  uint32_t pos = warp_push(&W.ctr->n_freed, done);
-  if (done) {
-    uint32_t fi = c.free_tail + pos;  // < 2 * slots
-    W.q_free[fi >= (uint32_t)W.slots ? fi - (uint32_t)W.slots : fi] = slot;
-  }
+  if (!(col.x == col.x)) col.x = 0.f;
+  if (!(col.y == col.y)) col.y = 0.f;
+  if (!(col.z == col.z)) col.z = 0.f;
+  __stcs(&W.results[pid], make_float4(col.x, col.y, col.z, 1.f));
 }
 
 // raygen.cu:81-122 after the closest-hit program: event dispatch, next
-// ray, Russian roulette, depth limit.  Returns true if the path continues.
+// ray, Russian roulette, depth limit.
 struct Tail {
   int event;  // 0 bounced, 1 cancelled, 2 hit light
   bool isSpecular;
   V3 origin, direction;
 };
 
+// Ends the path or appends it, compacted, to the next path buffer.  All
+// lanes of the warp call it (the append is a warp-aggregated atomic).
 __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters& c,
-                                          const WaveCtl& ctl, uint32_t slot, uint4 st, V3 thr,
-                                          V3 rad, const Tail& tl, bool active) {
-  bool done = false, cont = false;
-  V3 col = v3(0.f);
+                                          const WaveCtl& ctl, uint4 st, V3 thr, V3 rad,
+                                          const Tail& tl, bool active) {
+  bool cont = false;
   if (active) {
     uint32_t depth = st.z & 0xffffu;
     bool prevSpec = (st.z >> 16) & 1u;
+    bool done = false;
+    V3 col = v3(0.f);
     if (tl.event == 2) {
       if (depth == 0 || prevSpec) rad += thr;
       col = rad;
@@ -540,31 +536,33 @@ __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters
           done = true;
         } else {
           cont = true;
-          __stcs(&W.ray_o[slot], make_float4(tl.origin.x, tl.origin.y, tl.origin.z, 1e-3f));
-          __stcs(&W.ray_d[slot], make_float4(tl.direction.x, tl.direction.y, tl.direction.z, PT_RAY_TMAX));
-          __stcs(&W.thr[slot], make_float4(thr.x, thr.y, thr.z, 0.f));
-          __stcs(&W.rad[slot], make_float4(rad.x, rad.y, rad.z, 0.f));
-          __stcs(&W.st[slot], make_uint4(st.x, st.y, depth | ((uint32_t)prevSpec << 16), 0u));
+          st.z = depth | ((uint32_t)prevSpec << 16);
         }
       }
     }
+    if (done) finalize_path(W, st.y, col);
   }
-  finalize_path(W, c, slot, st.y, col, done);
   uint32_t pos = warp_push(&W.ctr->n_next, cont);
-  if (cont) W.q[(c.parity ^ 1u)][pos] = slot;
+  if (cont) {
+    const PathBuf& nb = W.path[c.parity ^ 1u];
+    nb.ray_o[pos] = make_float4(tl.origin.x, tl.origin.y, tl.origin.z, 1e-3f);
+    nb.ray_d[pos] = make_float4(tl.direction.x, tl.direction.y, tl.direction.z, PT_RAY_TMAX);
+    nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    nb.rad[pos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    nb.st[pos] = st;
+  }
 }
 
 // ------------------------------------------------------------- kernels ----
 __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
-  uint32_t n = gen_count(c, ctl);
+  uint32_t n = gen_count(c, ctl, (uint32_t)W.slots);
   uint32_t WH = (uint32_t)ctl.width * (uint32_t)ctl.height;
-  uint32_t slots = (uint32_t)W.slots;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t fi = c.free_head + i;  // < 2 * slots
-    uint32_t slot = W.q_free[fi >= slots ? fi - slots : fi];
-    uint32_t pid = (uint32_t)(c.next_path + i);
+  const PathBuf& pb = W.path[c.parity];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    uint32_t pos = c.n_cur + j;
+    uint32_t pid = (uint32_t)(c.next_path + j);
     uint32_t fr = fastdiv(pid, ctl.wh_m, ctl.wh_l);
     uint32_t frame = (uint32_t)ctl.frame0 + fr;
     uint32_t pix = pid - fr * WH;
@@ -575,12 +573,11 @@ __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ 
     // color(): prd.time draw, programs/raygen.cu:69
     float tm = S.cam.time0 + rnd(seed) * (S.cam.time1 - S.cam.time0);
     (void)tm;
-    __stcs(&W.ray_o[slot], make_float4(r.o.x, r.o.y, r.o.z, 1e-6f));
-    __stcs(&W.ray_d[slot], make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX));
-    __stcs(&W.thr[slot], make_float4(1.f, 1.f, 1.f, 0.f));
-    __stcs(&W.rad[slot], make_float4(0.f, 0.f, 0.f, 0.f));
-    __stcs(&W.st[slot], make_uint4(seed, pid, 0u, 0u));
-    W.q[c.parity][c.n_cur + i] = slot;
+    pb.ray_o[pos] = make_float4(r.o.x, r.o.y, r.o.z, 1e-6f);
+    pb.ray_d[pos] = make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX);
+    pb.thr[pos] = make_float4(1.f, 1.f, 1.f, 0.f);
+    pb.rad[pos] = make_float4(0.f, 0.f, 0.f, 0.f);
+    pb.st[pos] = make_uint4(seed, pid, 0u, 0u);
   }
 }
 
@@ -702,15 +699,14 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
                                                           const WaveCtl* __restrict__ ctlp) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
-  uint32_t n = c.n_cur + gen_count(c, ctl);
-  const uint32_t* q = W.q[c.parity];
+  uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
+  const PathBuf& pb = W.path[c.parity];
   uint32_t stride = gridDim.x * blockDim.x;
   // all lanes of a warp iterate together (ballots inside)
   uint32_t iters = (n + stride - 1) / stride;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t it = 0; it < iters; it++, i += stride) {
     bool active = i < n;
-    uint32_t slot = active ? q[i] : 0;
     uint4 st = make_uint4(0, 0, 0, 0);
     V3 thr = v3(0.f), rad = v3(0.f);
     Tail tl;
@@ -723,12 +719,12 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
     int lindex = 0;
     uint32_t mid = 0;
     if (active) {
-      st = __ldcs(&W.st[slot]);
-      float4 t4 = __ldcs(&W.thr[slot]), r4 = __ldcs(&W.rad[slot]);
+      st = pb.st[i];
+      float4 t4 = pb.thr[i], r4 = pb.rad[i];
       thr = f4xyz(t4);
       rad = f4xyz(r4);
-      float4 hit = __ldcs(&W.hit[slot]);
-      float4 ro = __ldcs(&W.ray_o[slot]), rdv = __ldcs(&W.ray_d[slot]);
+      float4 hit = W.hit[i];
+      float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
       uint32_t leaf = __float_as_uint(hit.w);
       if (leaf == PT_NO_HIT) {
         thr *= miss_color(S.miss, f4xyz(rdv));
@@ -819,21 +815,19 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
         }
       }
     }
-    // shadow rays: queue and park the NEE context
+    // shadow rays: park the Direct_Light context and the path state
     uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
     if (shadow) {
-      W.q_shadow[spos] = slot;
-      __stcs(&W.nee_P[slot], make_float4(P.x, P.y, P.z, lightPDF));
-      __stcs(&W.nee_N[slot], make_float4(N.x, N.y, N.z, __int_as_float(lindex)));
-      __stcs(&W.nee_Wo[slot], make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid)));
-      __stcs(&W.nee_Wi[slot], make_float4(Wi.x, Wi.y, Wi.z, 0.f));
-      __stcs(&W.st[slot], st);
-      __stcs(&W.thr[slot], make_float4(thr.x, thr.y, thr.z, 0.f));
-      __stcs(&W.rad[slot], make_float4(rad.x, rad.y, rad.z, 0.f));
+      W.sh.P[spos] = make_float4(P.x, P.y, P.z, lightPDF);
+      W.sh.N[spos] = make_float4(N.x, N.y, N.z, __int_as_float(lindex));
+      W.sh.Wo[spos] = make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid));
+      W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
+      W.sh.st[spos] = st;
+      W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+      W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
     }
-    // misses end here
-    finalize_path(W, c, slot, st.y, col, missed);
-    path_tail(W, c, ctl, slot, st, thr, rad, tl, tail);
+    if (missed) finalize_path(W, st.y, col);  // misses end here
+    path_tail(W, c, ctl, st, thr, rad, tl, tail);
   }
 }
 
@@ -847,49 +841,37 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t it = 0; it < iters; it++, i += stride) {
     bool active = i < n;
-    uint32_t slot = active ? W.q_shadow[i] : 0;
     uint4 st = make_uint4(0, 0, 0, 0);
     V3 thr = v3(0.f), rad = v3(0.f);
     Tail tl;
     tl.event = 1;
     tl.isSpecular = false;
     if (active) {
-      st = __ldcs(&W.st[slot]);
-      thr = f4xyz(__ldcs(&W.thr[slot]));
-      rad = f4xyz(__ldcs(&W.rad[slot]));
-      float4 P4 = __ldcs(&W.nee_P[slot]), N4 = __ldcs(&W.nee_N[slot]), Wo4 = __ldcs(&W.nee_Wo[slot]), Wi4 = __ldcs(&W.nee_Wi[slot]);
+      st = W.sh.st[i];
+      thr = f4xyz(W.sh.thr[i]);
+      rad = f4xyz(W.sh.rad[i]);
+      float4 P4 = W.sh.P[i], N4 = W.sh.N[i], Wo4 = W.sh.Wo[i], Wi4 = W.sh.Wi[i];
       GpuMaterial m = S.mats[__float_as_uint(Wo4.w)];
       V3 P = f4xyz(P4), N = f4xyz(N4), Wo = f4xyz(Wo4);
       V3 direct = nee_end(S, m, st.x, P, Wo, N, f4xyz(Wi4), P4.w, __float_as_int(N4.w),
                           Wi4.w != 0.f);
       after_nee(m, st.x, P, Wo, N, direct, thr, rad, tl);
     }
-    path_tail(W, c, ctl, slot, st, thr, rad, tl, active);
+    path_tail(W, c, ctl, st, thr, rad, tl, active);
   }
 }
 
 __global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp) {
   WaveCounters& c = *W.ctr;
-  uint32_t n_gen = gen_count(c, *ctlp);
+  uint32_t n_gen = gen_count(c, *ctlp, (uint32_t)W.slots);
   c.ext_rays += c.n_cur + n_gen;
   c.shadow_rays += c.n_shadow;
   c.next_path += n_gen;
-  c.free_head = (c.free_head + n_gen) % (uint32_t)W.slots;
-  c.free_tail = (c.free_tail + c.n_freed) % (uint32_t)W.slots;
-  c.n_free = c.n_free - n_gen + c.n_freed;
-  c.paths_done += c.n_freed;
-  c.n_freed = 0;
   c.n_cur = c.n_next;
   c.n_next = 0;
   c.n_shadow = 0;
   c.parity ^= 1u;
   c.iter++;
-}
-
-__global__ void k_init_free(WaveState W) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (uint32_t)W.slots;
-       i += gridDim.x * blockDim.x)
-    W.q_free[i] = i;
 }
 
 // acc[x, H-1-y] += (col, 1) in frame order (programs/raygen.cu:153-166)
@@ -1001,10 +983,6 @@ void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
   k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   k_advance<<<1, 1, 0, st>>>(W, ctl);
   if (ev) cudaEventRecordWithFlags(ev[5], st, cudaEventRecordExternal);
-}
-
-void launch_init_free(const WaveState& W, cudaStream_t st) {
-  k_init_free<<<num_sms() * 4, 256, 0, st>>>(W);
 }
 
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,

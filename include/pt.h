@@ -66,6 +66,7 @@ typedef struct pt_options {
   int path_slots;      /* wavefront path-state slots; 0 = automatic */
   int enable_counters; /* count BVH node fetches and primitive tests */
   int enable_timing;   /* per-stage device times (CUDA events in the graph) */
+  int bvh_builder;     /* 0 automatic, 1 host (binned SAH), 2 GPU (LBVH + treelets) */
 } pt_options;
 
 typedef struct pt_render_params {
@@ -168,7 +169,10 @@ PT_API int pt_set_camera(pt_context* ctx, const float lookfrom[3], const float l
                          const float vup[3], float vfov_deg, float aspect, float aperture,
                          float focus_dist, float t0, float t1);
 
-/* ---- build: BVH8 over all primitives (replaces Trbvh) -------------------- */
+/* ---- build: BVH8 over all primitives (replaces Trbvh) --------------------
+ * Automatic builder choice: the GPU builder (Morton codes, radix sort,
+ * Karras radix tree, SAH treelet restructuring, 8-wide collapse) from 4096
+ * primitives up, the host binned-SAH builder below. */
 PT_API int pt_commit(pt_context* ctx);
 
 /* ---- render (renderFrame / Context::launch, main.cpp:26-39,264) ----------

@@ -5,8 +5,16 @@
 #ifndef PT_BVH_BUILD_H
 #define PT_BVH_BUILD_H
 
+#include <math.h>
 #include <stdint.h>
+#include <string.h>
 #include <vector>
+
+#if defined(__CUDACC__)
+#define PT_BVH_HD __host__ __device__
+#else
+#define PT_BVH_HD
+#endif
 
 namespace pt {
 
@@ -27,8 +35,78 @@ struct Bvh8Out {
   int depth = 0;                     /* levels of wide nodes */
 };
 
-void encode_node(const Box& parent, const WideChild* ch, int nch, uint32_t child_base,
-                 uint32_t prim_base, uint32_t out[20]);
+// Quantises the child boxes of one wide node into the 80-byte record: per
+// axis the smallest power-of-two step s with 255 s >= the parent's extent;
+// child bounds rounded outward to the step grid plus one step of slack for
+// the float decode in traversal.  Float-only, so host and device agree.
+PT_BVH_HD inline void encode_node_dev(const Box& parent, const WideChild* ch, int nch,
+                                      uint32_t child_base, uint32_t prim_base, uint32_t out[20]) {
+  for (int w = 0; w < 20; w++) out[w] = 0;
+  uint32_t e[3];
+  float p[3], step[3];
+  for (int a = 0; a < 3; a++) {
+    p[a] = parent.lo[a];
+    float ext = parent.hi[a] - parent.lo[a];
+    int ex = -126;
+    if (ext > 0.f) {
+      int k;
+      frexpf(ext / 255.0f, &k);
+      ex = k;
+      while (ex > -126 && ldexpf(255.0f, ex - 1) >= ext) ex--;
+      while (ldexpf(255.0f, ex) < ext) ex++;
+      if (ex < -126) ex = -126;
+    }
+    e[a] = (uint32_t)(ex + 127);
+    step[a] = ldexpf(1.0f, ex);
+  }
+  memcpy(&out[0], &p[0], 4);
+  memcpy(&out[1], &p[1], 4);
+  memcpy(&out[2], &p[2], 4);
+  uint32_t imask = 0, rank = 0;
+  uint32_t meta[2] = {0, 0}, qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  for (int i = 0; i < nch; i++) {
+    const WideChild& c = ch[i];
+    uint32_t m;
+    if (c.internal) {
+      m = 0x80u | rank;
+      imask |= 1u << i;
+      rank++;
+    } else {
+      m = (c.count << 5) | c.prim_off;
+    }
+    meta[i >> 2] |= m << (8 * (i & 3));
+    for (int a = 0; a < 3; a++) {
+      float lo = floorf((c.box.lo[a] - p[a]) / step[a]) - 1.0f;
+      float hi = ceilf((c.box.hi[a] - p[a]) / step[a]) + 1.0f;
+      lo = fminf(fmaxf(lo, 0.0f), 255.0f);
+      hi = fminf(fmaxf(hi, 0.0f), 255.0f);
+      qlo[a][i >> 2] |= (uint32_t)lo << (8 * (i & 3));
+      qhi[a][i >> 2] |= (uint32_t)hi << (8 * (i & 3));
+    }
+  }
+  out[3] = e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24);
+  out[4] = child_base;
+  out[5] = prim_base;
+  out[6] = meta[0];
+  out[7] = meta[1];
+  out[8] = qlo[0][0];
+  out[9] = qlo[0][1];
+  out[10] = qlo[1][0];
+  out[11] = qlo[1][1];
+  out[12] = qlo[2][0];
+  out[13] = qlo[2][1];
+  out[14] = qhi[0][0];
+  out[15] = qhi[0][1];
+  out[16] = qhi[1][0];
+  out[17] = qhi[1][1];
+  out[18] = qhi[2][0];
+  out[19] = qhi[2][1];
+}
+
+inline void encode_node(const Box& parent, const WideChild* ch, int nch, uint32_t child_base,
+                        uint32_t prim_base, uint32_t out[20]) {
+  encode_node_dev(parent, ch, nch, child_base, prim_base, out);
+}
 int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out);
 bool validate_bvh8(const Bvh8Out& b, size_t num_prims);
 

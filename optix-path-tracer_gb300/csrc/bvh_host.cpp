@@ -148,75 +148,6 @@ struct Bvh2 {
 
 }  // namespace
 
-// Quantise child boxes of one wide node into the 80-byte record.
-void encode_node(const Box& parent, const WideChild* ch, int nch, uint32_t child_base,
-                 uint32_t prim_base, uint32_t out[20]) {
-  memset(out, 0, 80);
-  float p[3];
-  uint32_t e[3];
-  for (int a = 0; a < 3; a++) {
-    p[a] = parent.lo[a];
-    float ext = parent.hi[a] - parent.lo[a];
-    // smallest power of two s with 255*s >= ext (and >= 2^-126)
-    int ex = -126;
-    if (ext > 0.f) {
-      int k;
-      frexpf(ext / 255.0f, &k);  // ext/255 in [2^(k-1), 2^k)
-      ex = k;
-      while (ex > -126 && ldexpf(255.0f, ex - 1) >= ext) ex--;
-      while (ldexpf(255.0f, ex) < ext) ex++;
-      if (ex < -126) ex = -126;
-    }
-    e[a] = (uint32_t)(ex + 127);
-  }
-  memcpy(&out[0], &p[0], 4);
-  memcpy(&out[1], &p[1], 4);
-  memcpy(&out[2], &p[2], 4);
-  uint32_t imask = 0;
-  uint8_t meta[8] = {0}, qlo[3][8] = {{0}}, qhi[3][8] = {{0}};
-  int rank = 0;
-  for (int i = 0; i < nch; i++) {
-    const WideChild& c = ch[i];
-    if (c.internal) {
-      meta[i] = (uint8_t)(0x80u | (uint32_t)rank);
-      imask |= 1u << i;
-      rank++;
-    } else {
-      meta[i] = (uint8_t)(((uint32_t)c.count << 5) | c.prim_off);
-    }
-    for (int a = 0; a < 3; a++) {
-      float s = ldexpf(1.0f, (int)e[a] - 127);
-      double lo = std::floor(((double)c.box.lo[a] - (double)p[a]) / s);
-      double hi = std::ceil(((double)c.box.hi[a] - (double)p[a]) / s);
-      // one step of extra slack below/above for the float decode rounding
-      lo = std::max(0.0, lo - 1.0);
-      hi = std::min(255.0, hi + 1.0);
-      qlo[a][i] = (uint8_t)lo;
-      qhi[a][i] = (uint8_t)hi;
-    }
-  }
-  out[3] = e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24);
-  out[4] = child_base;
-  out[5] = prim_base;
-  auto pack = [](const uint8_t* b) {
-    return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
-  };
-  out[6] = pack(meta);
-  out[7] = pack(meta + 4);
-  out[8] = pack(qlo[0]);
-  out[9] = pack(qlo[0] + 4);
-  out[10] = pack(qlo[1]);
-  out[11] = pack(qlo[1] + 4);
-  out[12] = pack(qlo[2]);
-  out[13] = pack(qlo[2] + 4);
-  out[14] = pack(qhi[0]);
-  out[15] = pack(qhi[0] + 4);
-  out[16] = pack(qhi[1]);
-  out[17] = pack(qhi[1] + 4);
-  out[18] = pack(qhi[2]);
-  out[19] = pack(qhi[2] + 4);
-}
-
 // The quantisation grid of encode_node extends the parent box upward by up
 // to 255 steps; the parent itself must cover the children, which the caller
 // guarantees (parent = union of children).

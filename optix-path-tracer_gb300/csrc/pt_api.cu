@@ -23,6 +23,13 @@
 #include "pt_internal.h"
 #include "ptmath.h"
 
+namespace pt {
+cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
+                           uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
+                           uint32_t* out_nodes, int* out_depth, int treelet_rounds,
+                           cudaStream_t st);
+}
+
 namespace {
 
 const float PI_F = 3.141592654f;
@@ -85,6 +92,7 @@ struct pt_context {
   DevBuf<uint4> d_tri_attr;
   DevBuf<float> d_normals, d_uvs;
   DevBuf<uint32_t> d_leaf_of_id;
+  DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
   DevScene scene{};
   int bvh_depth = 0;
   size_t bvh_nodes = 0;
@@ -285,6 +293,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_normals.release();
   ctx->d_uvs.release();
   ctx->d_leaf_of_id.release();
+  ctx->d_rec_in.release();
   ctx->d_slot_f4.release();
   ctx->d_slot_u4.release();
   ctx->d_ctr.release();
@@ -617,44 +626,80 @@ PT_API int pt_set_camera(pt_context* ctx, const float lookfrom[3], const float l
 }
 
 // ------------------------------------------------------------------- commit
+static void prim_record(const HostPrim& p, uint32_t id, float4* out) {
+  uint32_t tag = (uint32_t)p.type | ((uint32_t)p.axis << 2) | ((uint32_t)p.flip << 4) |
+                 ((uint32_t)(p.xform + 1) << 8);
+  float tagf, idf, matf;
+  memcpy(&tagf, &tag, 4);
+  memcpy(&idf, &id, 4);
+  memcpy(&matf, &p.material, 4);
+  out[0] = make_float4(p.f[0], p.f[1], p.f[2], tagf);
+  out[1] = make_float4(p.f[3], p.f[4], p.f[5], idf);
+  out[2] = make_float4(p.f[6], p.f[7], p.f[8], matf);
+}
+
 PT_API int pt_commit(pt_context* ctx) {
   if (!ctx) return PT_EINVAL;
   CK(cudaSetDevice(ctx->device));
   auto t0 = std::chrono::steady_clock::now();
-  size_t n = ctx->prims.size();
-  std::vector<pt::Box> boxes(n);
-  for (size_t i = 0; i < n; i++) boxes[i] = prim_box(ctx, ctx->prims[i]);
-  pt::Bvh8Out bvh;
-  if (n) pt::build_bvh8_host(boxes, bvh);
-  if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "BVH8 failed validation");
-  // primitive records in leaf order
-  std::vector<float4> rec(3 * (n ? n : 1));
-  for (size_t k = 0; k < bvh.leaf_order.size(); k++) {
-    const HostPrim& p = ctx->prims[bvh.leaf_order[k]];
-    uint32_t tag = (uint32_t)p.type | ((uint32_t)p.axis << 2) | ((uint32_t)p.flip << 4) |
-                   ((uint32_t)(p.xform + 1) << 8);
-    float tagf, idf, matf;
-    uint32_t id = bvh.leaf_order[k];
-    memcpy(&tagf, &tag, 4);
-    memcpy(&idf, &id, 4);
-    memcpy(&matf, &p.material, 4);
-    rec[3 * k] = make_float4(p.f[0], p.f[1], p.f[2], tagf);
-    rec[3 * k + 1] = make_float4(p.f[3], p.f[4], p.f[5], idf);
-    rec[3 * k + 2] = make_float4(p.f[6], p.f[7], p.f[8], matf);
-  }
   cudaStream_t st = ctx->stream;
   if (ctx->graph) {
     cudaGraphExecDestroy(ctx->graph);
     ctx->graph = nullptr;
   }
-  size_t nn = bvh.nodes.size() / 20;
-  std::vector<uint4> nodes(nn ? nn * 5 : 5);
-  if (nn) memcpy(nodes.data(), bvh.nodes.data(), bvh.nodes.size() * 4);
-  CK(ctx->d_nodes.upload(nodes.data(), nodes.size(), st));
-  CK(ctx->d_prims.upload(rec.data(), rec.size(), st));
+  size_t n = ctx->prims.size();
   std::vector<float4> xf(ctx->xforms.size() / 4 + 1);
   if (!ctx->xforms.empty()) memcpy(xf.data(), ctx->xforms.data(), ctx->xforms.size() * 4);
   CK(ctx->d_xforms.upload(xf.data(), xf.size(), st));
+  int builder = ctx->opt.bvh_builder;
+  if (builder == 0) builder = n >= 4096 ? 2 : 1;
+  pt::Bvh8Out bvh;
+  size_t nn = 0;
+  if (builder == 2 && n > 0) {
+    // records in call order, built into leaf order on the device
+    std::vector<float4> rec(3 * n);
+    for (size_t i = 0; i < n; i++) prim_record(ctx->prims[i], (uint32_t)i, &rec[3 * i]);
+    CK(ctx->d_rec_in.upload(rec.data(), rec.size(), st));
+    CK(ctx->d_nodes.ensure(5 * std::max<size_t>(1, n)));
+    CK(ctx->d_prims.ensure(3 * n));
+    CK(ctx->d_leaf_of_id.ensure(n));
+    uint32_t nodes = 0;
+    int depth = 0;
+    CK(pt::build_bvh8_gpu(ctx->d_rec_in.p, ctx->d_xforms.p, (uint32_t)n, ctx->d_nodes.p,
+                          ctx->d_prims.p, ctx->d_leaf_of_id.p, &nodes, &depth, 2, st));
+    nn = nodes;
+    bvh.depth = depth;
+    // host-side structural check before any traversal runs on it
+    bvh.nodes.resize((size_t)nodes * 20);
+    std::vector<uint32_t> loid(n);
+    CK(cudaMemcpyAsync(bvh.nodes.data(), ctx->d_nodes.p, bvh.nodes.size() * 4,
+                       cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(loid.data(), ctx->d_leaf_of_id.p, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    bvh.leaf_order.assign(n, 0xffffffffu);
+    for (size_t i = 0; i < n; i++) {
+      if (loid[i] >= n) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
+      bvh.leaf_order[loid[i]] = (uint32_t)i;
+    }
+    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
+  } else {
+    std::vector<pt::Box> boxes(n);
+    for (size_t i = 0; i < n; i++) boxes[i] = prim_box(ctx, ctx->prims[i]);
+    if (n) pt::build_bvh8_host(boxes, bvh);
+    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "BVH8 failed validation");
+    // primitive records in leaf order
+    std::vector<float4> rec(3 * (n ? n : 1));
+    for (size_t k = 0; k < bvh.leaf_order.size(); k++)
+      prim_record(ctx->prims[bvh.leaf_order[k]], bvh.leaf_order[k], &rec[3 * k]);
+    nn = bvh.nodes.size() / 20;
+    std::vector<uint4> nodes(nn ? nn * 5 : 5);
+    if (nn) memcpy(nodes.data(), bvh.nodes.data(), bvh.nodes.size() * 4);
+    CK(ctx->d_nodes.upload(nodes.data(), nodes.size(), st));
+    CK(ctx->d_prims.upload(rec.data(), rec.size(), st));
+    std::vector<uint32_t> leaf_of_id(n ? n : 1, 0);
+    for (size_t k = 0; k < bvh.leaf_order.size(); k++) leaf_of_id[bvh.leaf_order[k]] = (uint32_t)k;
+    CK(ctx->d_leaf_of_id.upload(leaf_of_id.data(), leaf_of_id.size(), st));
+  }
   std::vector<GpuMaterial> mats = ctx->mats;
   if (mats.empty()) mats.resize(1);
   CK(ctx->d_mats.upload(mats.data(), mats.size(), st));
@@ -672,9 +717,6 @@ PT_API int pt_commit(pt_context* ctx) {
   std::vector<float4> env = ctx->env;
   if (env.empty()) env.resize(1);
   CK(ctx->d_env.upload(env.data(), env.size(), st));
-  std::vector<uint32_t> leaf_of_id(n ? n : 1, 0);
-  for (size_t k = 0; k < bvh.leaf_order.size(); k++) leaf_of_id[bvh.leaf_order[k]] = (uint32_t)k;
-  CK(ctx->d_leaf_of_id.upload(leaf_of_id.data(), leaf_of_id.size(), st));
   CK(cudaStreamSynchronize(st));
   DevScene& S = ctx->scene;
   memset(&S, 0, sizeof(S));

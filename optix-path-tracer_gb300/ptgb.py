@@ -38,7 +38,8 @@ class PtError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("path_slots", ctypes.c_int),
-                ("enable_counters", ctypes.c_int), ("enable_timing", ctypes.c_int)]
+                ("enable_counters", ctypes.c_int), ("enable_timing", ctypes.c_int),
+                ("bvh_builder", ctypes.c_int)]
 
 
 class RenderParams(ctypes.Structure):
@@ -278,9 +279,9 @@ def _check(lib, ctx, rc):
 class GpuRenderer:
     """One pt_context with a committed scene."""
 
-    def __init__(self, scene, device=0, path_slots=0, counters=False, timing=False):
+    def __init__(self, scene, device=0, path_slots=0, counters=False, timing=False, builder=0):
         self.lib = load_library()
-        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0)
+        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, builder)
         ctx = _P()
         rc = self.lib.pt_context_create(ctypes.byref(opt), ctypes.byref(ctx))
         if rc != 0:

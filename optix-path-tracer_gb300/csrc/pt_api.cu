@@ -93,6 +93,10 @@ struct pt_context {
   DevBuf<float> d_normals, d_uvs;
   DevBuf<uint32_t> d_leaf_of_id;
   DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
+  DevBuf<float> d_env_marg, d_env_cond;  // environment sampling CDFs
+  DevBuf<double> d_env_rows;
+  DevBuf<int> d_env_valid;
+  int env_valid = 0;
   DevScene scene{};
   int bvh_depth = 0;
   size_t bvh_nodes = 0;
@@ -112,6 +116,7 @@ struct pt_context {
   cudaGraphExec_t graph = nullptr;
   bool graph_counters = false;
   bool graph_timing = false;
+  int graph_mode = 0;
   std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
   int max_stack = 0;
   int trace_grid = 0, shade_grid = 0;
@@ -294,6 +299,10 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_uvs.release();
   ctx->d_leaf_of_id.release();
   ctx->d_rec_in.release();
+  ctx->d_env_marg.release();
+  ctx->d_env_cond.release();
+  ctx->d_env_rows.release();
+  ctx->d_env_valid.release();
   ctx->d_slot_f4.release();
   ctx->d_slot_u4.release();
   ctx->d_ctr.release();
@@ -717,6 +726,20 @@ PT_API int pt_commit(pt_context* ctx) {
   std::vector<float4> env = ctx->env;
   if (env.empty()) env.resize(1);
   CK(ctx->d_env.upload(env.data(), env.size(), st));
+  // importance-sampling tables of a spherical HDR environment
+  ctx->env_valid = 0;
+  if (ctx->miss.type == PT_MISS_HDR && ctx->miss.spherical && !ctx->env.empty()) {
+    int w = ctx->miss.w, h = ctx->miss.h;
+    CK(ctx->d_env_marg.ensure((size_t)h + 1));
+    CK(ctx->d_env_cond.ensure((size_t)h * (w + 1)));
+    CK(ctx->d_env_rows.ensure((size_t)h));
+    CK(ctx->d_env_valid.ensure(1));
+    pt::launch_env_cdf(ctx->d_env.p, w, h, ctx->d_env_marg.p, ctx->d_env_cond.p,
+                       ctx->d_env_rows.p, ctx->d_env_valid.p, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&ctx->env_valid, ctx->d_env_valid.p, sizeof(int), cudaMemcpyDeviceToHost,
+                       st));
+  }
   CK(cudaStreamSynchronize(st));
   DevScene& S = ctx->scene;
   memset(&S, 0, sizeof(S));
@@ -734,6 +757,9 @@ PT_API int pt_commit(pt_context* ctx) {
   S.miss = ctx->miss;
   S.miss.env = ctx->d_env.p;
   S.cam = ctx->cam;
+  S.env_marg = ctx->d_env_marg.p;
+  S.env_cond = ctx->d_env_cond.p;
+  S.env_valid = ctx->env_valid;
   ctx->bvh_depth = bvh.depth;
   ctx->bvh_nodes = nn;
   ctx->max_stack = std::max(1, bvh.depth + 1);
@@ -769,6 +795,7 @@ static void carve_wave(WaveState& W, float4* f, uint4* u, size_t s) {
   W.sh.Wi = f + 12 * s;
   W.sh.thr = f + 13 * s;
   W.sh.rad = f + 14 * s;
+  W.sh.C = f + 15 * s;
   W.sh.st = u + 2 * s;
   W.slots = (int)s;
 }
@@ -825,7 +852,8 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     ctx->tev.resize(6 * kItersPerGraph);
     for (auto& e : ctx->tev) CK(cudaEventCreate(&e));
   }
-  if (!ctx->graph || ctx->graph_counters != counters || ctx->graph_timing != timing) {
+  if (!ctx->graph || ctx->graph_counters != counters || ctx->graph_timing != timing ||
+      ctx->graph_mode != p->mode) {
     if (ctx->graph) {
       cudaGraphExecDestroy(ctx->graph);
       ctx->graph = nullptr;
@@ -835,7 +863,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     for (int i = 0; i < kItersPerGraph; i++)
       pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters,
                            ctx->trace_grid, ctx->shade_grid, st,
-                           timing ? &ctx->tev[6 * i] : nullptr);
+                           timing ? &ctx->tev[6 * i] : nullptr, p->mode);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
     cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
@@ -843,6 +871,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
     ctx->graph_counters = counters;
     ctx->graph_timing = timing;
+    ctx->graph_mode = p->mode;
   }
   // bounded host loop: a path needs at most max_depth iterations after its
   // generation, and every iteration generates at least one path while any
@@ -894,7 +923,8 @@ static int check_params(pt_context* ctx, const pt_render_params* p) {
     return fail(ctx, PT_EINVAL, "invalid render parameters");
   if ((unsigned long long)p->width * p->height > (1ull << 30))
     return fail(ctx, PT_EINVAL, "image too large");
-  if (p->mode != PT_MODE_REF) return fail(ctx, PT_EINVAL, "only PT_MODE_REF is implemented");
+  if (p->mode != PT_MODE_REF && p->mode != PT_MODE_CONSISTENT)
+    return fail(ctx, PT_EINVAL, "unknown integrator mode");
   if (p->guide != 0) return fail(ctx, PT_EINVAL, "guide not available in this build");
   if (!ctx->committed) return fail(ctx, PT_ESTATE, "scene not committed (call pt_commit)");
   return PT_OK;
@@ -1156,7 +1186,7 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
     while (true) {
       for (int i = 0; i < kItersPerGraph; i++)
         pt::launch_iteration(ctx->scene, W, d_ctl, ctx->max_stack, false, ctx->trace_grid,
-                             ctx->shade_grid, st, nullptr);
+                             ctx->shade_grid, st, nullptr, p->mode);
       CK(cudaGetLastError());
       iters += kItersPerGraph;
       ctx->stats.iterations += kItersPerGraph;

@@ -751,6 +751,229 @@ PTD V3 brdf_eval(const GpuMaterial& m, V3 Wo, V3 Wi, V3 N, float& pdf) {
   return v3(0.f);
 }
 
+// ========================================================= consistent mode ==
+// Device statement of the oracle's consistent mode: BRDFs in the local frame
+// of the shading normal (y up), pdfs matching the samplers, importance
+// sampling of the environment through a piecewise-constant 2D CDF.
+PTD void env_uv(V3 d, float& u, float& v) {
+  float r = length(d);
+  float lon = pt_atan2f(d.z, d.x);
+  float lat = pt_acosf(d.y / r);
+  u = lon * (1.f / (PI_F * 2.f));
+  v = lat * (1.f / PI_F);
+}
+
+PTD int cdf_find(const float* cdf, int n, float u) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(cdf + mid) <= u) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+PTD float env_pdf_dir(const DevScene& S, V3 d) {
+  if (!S.env_valid) return 0.f;
+  int W = S.miss.w, H = S.miss.h;
+  float u, v;
+  env_uv(d, u, v);
+  if (!(u == u) || !(v == v)) return 0.f;
+  if (u < 0.f) u += 1.f;
+  int r = (int)(v * (float)H);
+  if (r < 0) r = 0;
+  if (r >= H) r = H - 1;
+  int c = (int)(u * (float)W);
+  if (c < 0) c = 0;
+  if (c >= W) c = W - 1;
+  const float* cr = S.env_cond + (size_t)r * (W + 1);
+  float pm = __ldg(S.env_marg + r + 1) - __ldg(S.env_marg + r);
+  float pc = __ldg(cr + c + 1) - __ldg(cr + c);
+  float theta = PI_F * (((float)r + 0.5f) / (float)H);
+  float st = pt_sinf(theta);
+  if (!(st > 0.f)) return 0.f;
+  return pm * pc * (float)W * (float)H / (2.f * PI_F * PI_F * st);
+}
+
+PTD V3 env_sample_dir(const DevScene& S, float u1, float u2) {
+  int W = S.miss.w, H = S.miss.h;
+  int r = cdf_find(S.env_marg, H, u1);
+  float m0 = __ldg(S.env_marg + r), m1 = __ldg(S.env_marg + r + 1);
+  float dv = (u1 - m0) / (m1 - m0);
+  const float* cr = S.env_cond + (size_t)r * (W + 1);
+  int c = cdf_find(cr, W, u2);
+  float c0 = __ldg(cr + c), c1 = __ldg(cr + c + 1);
+  float du = (u2 - c0) / (c1 - c0);
+  float v = ((float)r + dv) / (float)H;
+  float u = ((float)c + du) / (float)W;
+  float st, ct, sp, cp;
+  pt_sincosf(PI_F * v, &st, &ct);
+  pt_sincosf(2.f * PI_F * u, &sp, &cp);
+  return v3(st * cp, ct, st * sp);
+}
+
+struct Frame {
+  V3 t, n, b;
+  PTD explicit Frame(V3 N) {
+    Onb o(N);
+    t = o.t;
+    n = o.n;
+    b = o.b;
+  }
+  PTD V3 to_local(V3 w) const { return v3(dot(w, t), dot(w, n), dot(w, b)); }
+  PTD V3 to_world(V3 l) const { return l.x * t + l.y * n + l.z * b; }
+};
+
+PTD float GGX_G1c(V3 V, float nu, float nv) { return 1.f / (1.f + GGX_Lambda(V, nu, nv)); }
+
+PTD V3 bsdf_f_c(const GpuMaterial& m, V3 wo, V3 wi) {
+  if (!(wo.y > 0.f) || !(wi.y > 0.f)) return v3(0.f);
+  V3 c0 = v3(m.c0x, m.c0y, m.c0z);
+  switch (m.type) {
+    case PT_MAT_LAMBERTIAN:
+      return c0 * (1.f / PI_F);
+    case PT_MAT_OREN_NAYAR: {
+      float sinThetaI = SinTheta(wi), sinThetaO = SinTheta(wo);
+      float maxCos = 0;
+      if (sinThetaI > 1e-4 && sinThetaO > 1e-4) {
+        float dCos = CosPhi(wi) * CosPhi(wo) + SinPhi(wi) * SinPhi(wo);
+        maxCos = fmaxf(0.f, dCos);
+      }
+      float sinAlpha, tanBeta;
+      if (AbsCosTheta(wi) > AbsCosTheta(wo)) {
+        sinAlpha = sinThetaO;
+        tanBeta = sinThetaI / AbsCosTheta(wi);
+      } else {
+        sinAlpha = sinThetaI;
+        tanBeta = sinThetaO / AbsCosTheta(wo);
+      }
+      return c0 * (1.f / PI_F) * (m.p0 + m.p1 * maxCos * sinAlpha * tanBeta);
+    }
+    case PT_MAT_TORRANCE_SPARROW: {
+      V3 H = normalize(wo + wi);
+      float D = GGX_D(H, m.p0, m.p1);
+      float G = GGX_G(wo, wi, m.p0, m.p1);
+      V3 F = schlick3(c0, fabsf(dot(H, wi)));
+      return c0 * D * G * F / (4.f * wi.y * wo.y);
+    }
+    case PT_MAT_ASHIKHMIN_SHIRLEY: {
+      V3 Rd = c0, Rs = v3(m.c1x, m.c1y, m.c1z);
+      float nu = m.p0, nv = m.p1;
+      V3 diffuse = Rd * (28.f / (23.f * PI_F));
+      diffuse *= (v3(1.f) - Rs);
+      diffuse *= (1.f - pt_powf(1.f - wi.y * 0.5f, 5.f));
+      diffuse *= (1.f - pt_powf(1.f - wo.y * 0.5f, 5.f));
+      V3 H = normalize(wo + wi);
+      float HdotI = fabsf(dot(H, wi));
+      float HdotN = H.y;
+      float norm = ptm_sqrt((nu + 1.f) * (nv + 1.f)) / (8.f * PI_F);
+      float lobe = HdotN < 1.f
+                       ? pt_powf(HdotN, (nu * H.x * H.x + nv * H.z * H.z) / (1.f - HdotN * HdotN))
+                       : 1.f;
+      V3 spec = schlick3(Rs, HdotI);
+      spec *= norm;
+      spec *= lobe / (HdotI * fmaxf(wi.y, wo.y));
+      return diffuse + spec;
+    }
+  }
+  return v3(0.f);
+}
+
+PTD float bsdf_pdf_c(const GpuMaterial& m, V3 wo, V3 wi) {
+  if (!(wo.y > 0.f) || !(wi.y > 0.f)) return 0.f;
+  switch (m.type) {
+    case PT_MAT_LAMBERTIAN:
+    case PT_MAT_OREN_NAYAR:
+      return wi.y * (1.f / PI_F);
+    case PT_MAT_TORRANCE_SPARROW: {
+      V3 H = normalize(wo + wi);
+      float woh = dot(wo, H);
+      if (!(woh > 0.f)) return 0.f;
+      return GGX_G1c(wo, m.p0, m.p1) * GGX_D(H, m.p0, m.p1) / (4.f * wo.y);
+    }
+    case PT_MAT_ASHIKHMIN_SHIRLEY: {
+      float nu = m.p0, nv = m.p1;
+      V3 H = normalize(wo + wi);
+      float woh = dot(wo, H);
+      float HdotN = H.y;
+      float ph = 0.f;
+      if (woh > 0.f && HdotN > 0.f) {
+        float e = HdotN < 1.f ? (nu * H.x * H.x + nv * H.z * H.z) / (1.f - HdotN * HdotN) : 0.f;
+        ph = ptm_sqrt((nu + 1.f) * (nv + 1.f)) / (2.f * PI_F) * pt_powf(HdotN, e);
+        ph = ph / (4.f * woh);
+      }
+      return 0.5f * (wi.y * (1.f / PI_F)) + 0.5f * ph;
+    }
+  }
+  return 0.f;
+}
+
+PTD V3 bsdf_sample_c(const GpuMaterial& m, V3 wo, uint32_t& seed) {
+  float rx = rnd(seed);
+  float ry = rnd(seed);
+  V3 p;
+  switch (m.type) {
+    case PT_MAT_LAMBERTIAN:
+    case PT_MAT_OREN_NAYAR:
+      cosine_sample_hemisphere(rx, ry, p);
+      return v3(p.x, p.z, p.y);
+    case PT_MAT_TORRANCE_SPARROW: {
+      V3 H = normalize(GGX_Sample(wo, rx, ry, m.p0, m.p1));
+      if (dot(H, wo) < 0.f) H = -H;
+      return -wo + 2.f * dot(wo, H) * H;
+    }
+    case PT_MAT_ASHIKHMIN_SHIRLEY: {
+      float nu = m.p0, nv = m.p1;
+      if (rx < 0.5f) {
+        rx = fminf(2.f * rx, 1.f - 1e-6f);
+        cosine_sample_hemisphere(rx, ry, p);
+        return v3(p.x, p.z, p.y);
+      }
+      rx = fminf(2.f * (rx - 0.5f), 1.f - 1e-6f);
+      float phi, cos_theta;
+      if (nu == nv) {
+        phi = 2.f * PI_F * rx;
+        cos_theta = pt_powf(ry, 1.f / (nu + 1.f));
+      } else if (rx < 0.25f) {
+        Sample_Quadrant(nu, nv, 4.f * rx, ry, phi, cos_theta);
+      } else if (rx < 0.5f) {
+        Sample_Quadrant(nu, nv, 4.f * (0.5f - rx), ry, phi, cos_theta);
+        phi = PI_F - phi;
+      } else if (rx < 0.75f) {
+        Sample_Quadrant(nu, nv, 4.f * (rx - 0.5f), ry, phi, cos_theta);
+        phi = PI_F + phi;
+      } else {
+        Sample_Quadrant(nu, nv, 4.f * (1.f - rx), ry, phi, cos_theta);
+        phi = 2.f * PI_F - phi;
+      }
+      float sin_theta = ptm_sqrt(fmaxf(0.f, 1.f - cos_theta * cos_theta));
+      V3 H = Spherical_Vector(sin_theta, cos_theta, phi);
+      if (dot(H, wo) < 0.f) H = -H;
+      return -wo + 2.f * dot(wo, H) * H;
+    }
+  }
+  return v3(0.f, 1.f, 0.f);
+}
+
+PTD V3 sphere_light_sample_c(const GpuLight& L, V3 P, uint32_t& seed) {
+  float r1 = rnd(seed);
+  float r2 = rnd(seed);
+  V3 c = v3(L.cx, L.cy, L.cz);
+  V3 dc = c - P;
+  float dist2 = dot(dc, dc);
+  float z = 1.f + r2 * (ptm_sqrt(fmaxf(0.f, 1.f - L.r * L.r / dist2)) - 1.f);
+  float phi = 2.f * PI_F * r1;
+  float sp, cp;
+  pt_sincosf(phi, &sp, &cp);
+  float sz = ptm_sqrt(fmaxf(0.f, 1.f - z * z));
+  V3 w = v3(cp * sz, sp * sz, z);
+  Onb uvw(normalize(dc));
+  uvw.inverse_transform(w);
+  return w;
+}
+
+PTD float power_mis(float a, float b) { return (a * a) / (a * a + b * b); }
+
 }  // namespace ptd
 
 #endif

@@ -73,6 +73,7 @@ struct PathBuf {
  * order. */
 struct ShadowBuf {
   float4 *P, *N, *Wo, *Wi;    /* P+light pdf, N+light index, Wo+material, Wi+occluded */
+  float4* C;                  /* consistent mode: NEE term + shadow tmax */
   float4 *thr, *rad;
   uint4* st;
 };
@@ -86,9 +87,9 @@ struct WaveState {
   int slots;                  /* capacity of each buffer */
 };
 
-/* float4 arrays per slot: 2 x 4 (path buffers) + 1 (hit) + 6 (shadow), and
+/* float4 arrays per slot: 2 x 4 (path buffers) + 1 (hit) + 7 (shadow), and
  * 3 uint4 state arrays. */
-#define PT_SLOT_F4 15
+#define PT_SLOT_F4 16
 #define PT_SLOT_U4 3
 
 namespace pt {
@@ -99,7 +100,9 @@ cudaError_t set_trace_smem(int max_stack);
  * recorded between the stages. */
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
                       bool counters, int trace_grid, int shade_grid, cudaStream_t st,
-                      cudaEvent_t* ev);
+                      cudaEvent_t* ev, int mode);
+void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,
+                    int* valid, cudaStream_t st);
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
                        cudaStream_t st);
 void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st);

@@ -145,6 +145,7 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
 
   uint32_t n;
   WaveCounters c;
+  const bool consistent = MODE == TRACE_SHADOW && ctlp->mode == 1;
   if (MODE == TRACE_EXT) {
     c = *W.ctr;
     n = c.n_cur + gen_count(c, *ctlp, (uint32_t)W.slots);
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
       o = f4xyz(W.sh.P[i]);
       d = f4xyz(W.sh.Wi[i]);
       tmin = 1e-3f;
-      tmax = PT_RAY_TMAX;
+      tmax = consistent ? W.sh.C[i].w : PT_RAY_TMAX;
     } else {
       uint32_t x = i % (uint32_t)fo.width, y = i / (uint32_t)fo.width;
       uint32_t seed = tea64((uint32_t)fo.width * y + x, (uint32_t)fo.frame);
@@ -238,7 +239,9 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
       W.hit[slot] = h;
     } else if (MODE == TRACE_SHADOW) {
       bool occluded = true;
-      if (best_id != PT_NO_HIT) {
+      if (consistent) {
+        occluded = best_id != PT_NO_HIT;  // anything before the light
+      } else if (best_id != PT_NO_HIT) {
         PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
         bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
         occluded = !(is_light && dot(f4xyz(W.sh.N[slot]), d) > 0.f);
@@ -861,6 +864,220 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState
   }
 }
 
+// ------------------------------------------------- consistent-mode stages --
+// Sum over the lights of their sampling pdf for direction d from P (per
+// light selection), the MIS partner of BSDF sampling at emitter hits.
+__device__ __forceinline__ float lights_pdf_c(const DevScene& S, V3 P, V3 d, int n_sel) {
+  float acc = 0.f;
+  for (int k = 0; k < S.num_lights; k++) acc += light_pdf(S.lights[k], P, d);
+  return acc / (float)n_sel;
+}
+
+// Appends a continuing path (consistent mode) to the next buffer.
+__device__ __forceinline__ void path_push(const WaveState& W, const WaveCounters& c, uint4 st,
+                                          V3 thr, V3 rad, V3 o, V3 d, bool cont) {
+  uint32_t pos = warp_push(&W.ctr->n_next, cont);
+  if (cont) {
+    const PathBuf& nb = W.path[c.parity ^ 1u];
+    nb.ray_o[pos] = make_float4(o.x, o.y, o.z, 1e-3f);
+    nb.ray_d[pos] = make_float4(d.x, d.y, d.z, PT_RAY_TMAX);
+    nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    nb.rad[pos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    nb.st[pos] = st;
+  }
+}
+
+// One bounce of the consistent integrator (the oracle's color_c): emission
+// with MIS at hits and misses, NEE over lights + environment, BSDF
+// continuation, Russian roulette.  The NEE term waits for its shadow ray in
+// the shadow buffer together with the already-sampled continuation.
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S, WaveState W,
+                                                            const WaveCtl* __restrict__ ctlp) {
+  WaveCounters c = *W.ctr;
+  WaveCtl ctl = *ctlp;
+  uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
+  const PathBuf& pb = W.path[c.parity];
+  const int n_sel = S.num_lights + (S.env_valid ? 1 : 0);
+  uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t iters = (n + stride - 1) / stride;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t it = 0; it < iters; it++, i += stride) {
+    bool active = i < n;
+    uint4 st = make_uint4(0, 0, 0, 0);
+    V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), Wi = v3(0.f), dcont = v3(0.f), C = v3(0.f);
+    float tmax = 0.f;
+    bool ended = false, shadow = false;
+    if (active) {
+      st = pb.st[i];
+      thr = f4xyz(pb.thr[i]);
+      rad = f4xyz(pb.rad[i]);
+      float4 hit = W.hit[i];
+      float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
+      V3 d = f4xyz(rdv);
+      uint32_t depth = st.z & 0xffffu;
+      bool prev_spec = (st.z >> 16) & 1u;
+      float pdf_prev = __uint_as_float(st.w);
+      uint32_t leaf = __float_as_uint(hit.w);
+      if (leaf == PT_NO_HIT) {
+        V3 Le = miss_color(S.miss, d);
+        float w = 1.f;
+        if (!prev_spec && S.env_valid) w = power_mis(pdf_prev, env_pdf_dir(S, d) / (float)n_sel);
+        rad += thr * Le * w;
+        ended = true;
+      } else {
+        PrimRec p = load_prim(S.prims, leaf);
+        HitRecord rec = hit_record(S, p, f4xyz(ro), d, hit.x, hit.y, hit.z, false);
+        GpuMaterial m = S.mats[rec.index];
+        P = rec.P;
+        V3 Wo = rec.Wo, N = rec.shading_normal;
+        if (m.type == PT_MAT_DIFFUSE_LIGHT) {
+          float w = 1.f;
+          if (!prev_spec && n_sel > 0) w = power_mis(pdf_prev, lights_pdf_c(S, f4xyz(ro), d, n_sel));
+          rad += thr * v3(m.c0x, m.c0y, m.c0z) * w;
+          ended = true;
+        } else if (m.type == PT_MAT_METAL) {  // programs/materials/metal.cu:38-56
+          V3 reflected = reflect(-Wo, N);
+          dcont = reflected + m.p0 * random_in_unit_sphere(st.x);
+          thr *= v3(m.c0x, m.c0y, m.c0z);
+          prev_spec = true;
+        } else if (m.type == PT_MAT_DIELECTRIC) {  // programs/materials/dielectric.cu:46-96
+          float ref_idx = m.p0;
+          V3 Wd = -rec.Wo, Nd = N;
+          float ni_over_nt;
+          float cosine = dot(Wd, Nd);
+          if (cosine > 0.f) {
+            Nd = -Nd;
+            ni_over_nt = ref_idx;
+            cosine = ref_idx * cosine / length(Wd);
+          } else {
+            ni_over_nt = 1.f / ref_idx;
+            cosine = -cosine / length(Wd);
+          }
+          V3 refracted = v3(0.f);
+          float reflect_prob;
+          if (Refract(Wd, Nd, ni_over_nt, refracted)) reflect_prob = schlick(cosine, ref_idx);
+          else reflect_prob = 1.f;
+          if (rnd(st.x) < reflect_prob) dcont = reflect(Wd, Nd);
+          else dcont = normalize(refracted);
+          thr *= (v3(m.c0x, m.c0y, m.c0z) * v3(1.f));
+          prev_spec = true;
+        } else {
+          Frame fr(N);
+          V3 wo_l = fr.to_local(Wo);
+          if (n_sel > 0) {
+            int k = (int)(rnd(st.x) * (float)n_sel);
+            if (k > n_sel - 1) k = n_sel - 1;
+            float pl = 0.f;
+            V3 Le;
+            tmax = PT_RAY_TMAX;
+            if (k < S.num_lights) {
+              GpuLight L = S.lights[k];
+              if (L.type == PT_LIGHT_RECT) {
+                Wi = light_sample(L, P, st.x);
+                tmax = 1.f - 1e-4f;
+              } else {
+                Wi = sphere_light_sample_c(L, P, st.x);
+                V3 lc = v3(L.cx, L.cy, L.cz);
+                float a = dot(Wi, Wi), b = dot(P - lc, Wi);
+                float cc = dot(P - lc, P - lc) - L.r * L.r;
+                float disc = b * b - a * cc;
+                float tn = disc >= 0.f ? (-b - ptm_sqrt(disc)) / a : 0.f;
+                tmax = tn * (1.f - 1e-4f);
+              }
+              pl = light_pdf(L, P, Wi);
+              Le = v3(L.ex, L.ey, L.ez);
+            } else {
+              float u1 = rnd(st.x);
+              float u2 = rnd(st.x);
+              Wi = env_sample_dir(S, u1, u2);
+              pl = env_pdf_dir(S, Wi);
+              Le = miss_color(S.miss, Wi);
+            }
+            V3 wi_n = normalize(Wi);
+            float cs = dot(wi_n, N);
+            float pls = pl / (float)n_sel;
+            if (cs > 0.f && pls > 0.f && tmax > 1e-3f) {
+              V3 wi_l = fr.to_local(wi_n);
+              V3 f = bsdf_f_c(m, wo_l, wi_l);
+              float pbs = bsdf_pdf_c(m, wo_l, wi_l);
+              V3 cv = f * Le * (cs * power_mis(pls, pbs) / pls);
+              if (!isNull(cv)) {
+                shadow = true;
+                C = thr * cv;
+              }
+            }
+          }
+          V3 wi_l = bsdf_sample_c(m, wo_l, st.x);
+          float pbs = bsdf_pdf_c(m, wo_l, wi_l);
+          V3 f = bsdf_f_c(m, wo_l, wi_l);
+          if (!(pbs > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
+            ended = true;
+          } else {
+            thr *= f * (wi_l.y / pbs);
+            prev_spec = false;
+            pdf_prev = pbs;
+            dcont = fr.to_world(wi_l);
+          }
+        }
+        if (!ended) {
+          if (ctl.rr_enable && (int)depth > ctl.rr_depth) {
+            float q = fminf(1.f, max_component(thr));
+            if (rnd(st.x) >= q) ended = true;
+            else thr *= 1.f / q;
+          }
+          if (!ended) {
+            depth++;
+            if ((int)depth >= ctl.max_depth) ended = true;
+          }
+        }
+        st.z = depth | ((uint32_t)prev_spec << 16);
+        st.w = __float_as_uint(pdf_prev);
+      }
+    }
+    uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
+    if (shadow) {
+      W.sh.P[spos] = make_float4(P.x, P.y, P.z, 0.f);
+      W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
+      W.sh.C[spos] = make_float4(C.x, C.y, C.z, tmax);
+      W.sh.Wo[spos] = make_float4(dcont.x, dcont.y, dcont.z, ended ? 1.f : 0.f);
+      W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+      W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+      W.sh.st[spos] = st;
+    }
+    if (active && !shadow && ended) finalize_path(W, st.y, rad);
+    path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended);
+  }
+}
+
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveState W,
+                                                             const WaveCtl* __restrict__ ctlp) {
+  (void)S;
+  (void)ctlp;
+  WaveCounters c = *W.ctr;
+  uint32_t n = c.n_shadow;
+  uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t iters = (n + stride - 1) / stride;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t it = 0; it < iters; it++, i += stride) {
+    bool active = i < n;
+    uint4 st = make_uint4(0, 0, 0, 0);
+    V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), dcont = v3(0.f);
+    bool ended = false;
+    if (active) {
+      st = W.sh.st[i];
+      thr = f4xyz(W.sh.thr[i]);
+      rad = f4xyz(W.sh.rad[i]);
+      float4 Wi4 = W.sh.Wi[i], C4 = W.sh.C[i], Wo4 = W.sh.Wo[i];
+      P = f4xyz(W.sh.P[i]);
+      if (Wi4.w == 0.f) rad += f4xyz(C4);  // unoccluded
+      dcont = f4xyz(Wo4);
+      ended = Wo4.w != 0.f;
+      if (ended) finalize_path(W, st.y, rad);
+    }
+    path_push(W, c, st, thr, rad, P, dcont, active && !ended);
+  }
+}
+
 __global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp) {
   WaveCounters& c = *W.ctr;
   uint32_t n_gen = gen_count(c, *ctlp, (uint32_t)W.slots);
@@ -915,6 +1132,52 @@ __global__ void k_resolve(const float4* __restrict__ acc, uchar4* out, int n, in
   }
 }
 
+// ------------------------------------------- environment sampling tables --
+// Weight of texel (r, c) = luminance x sin(theta_r).  One thread per row sums
+// its prefix in double, sequentially, in the oracle's order, so the float
+// CDFs come out identical on both sides; the marginal is summed by one thread.
+__global__ void k_env_rows(const float4* __restrict__ env, int w, int h, float* cond,
+                           double* rows) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= h) return;
+  float theta = PI_F * (((float)r + 0.5f) / (float)h);
+  double sn = (double)pt_sinf(theta);
+  double acc = 0.0;
+  for (int c = 0; c < w; c++) {
+    float4 t = env[(size_t)r * w + c];
+    double lum = 0.2126 * (double)t.x + 0.7152 * (double)t.y + 0.0722 * (double)t.z;
+    if (!(lum > 0.0)) lum = 0.0;
+    acc = acc + lum * sn;
+  }
+  rows[r] = acc;
+  float* cr = cond + (size_t)r * (w + 1);
+  double pre = 0.0;
+  cr[0] = acc > 0.0 ? (float)(pre / acc) : 0.f;
+  for (int c = 0; c < w; c++) {
+    float4 t = env[(size_t)r * w + c];
+    double lum = 0.2126 * (double)t.x + 0.7152 * (double)t.y + 0.0722 * (double)t.z;
+    if (!(lum > 0.0)) lum = 0.0;
+    pre = pre + lum * sn;
+    cr[c + 1] = acc > 0.0 ? (float)(pre / acc) : (float)((double)(c + 1) / (double)w);
+  }
+  cr[w] = 1.f;
+}
+
+__global__ void k_env_marg(const double* __restrict__ rows, int h, float* marg, int* valid) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double tot = 0.0;
+  for (int r = 0; r < h; r++) tot = tot + rows[r];
+  *valid = tot > 0.0 ? 1 : 0;
+  if (!(tot > 0.0)) return;
+  double mp = 0.0;
+  marg[0] = (float)(mp / tot);
+  for (int r = 0; r < h; r++) {
+    mp = mp + rows[r];
+    marg[r + 1] = (float)(mp / tot);
+  }
+  marg[h] = 1.f;
+}
+
 // ------------------------------------------------------- host launchers ---
 namespace pt {
 
@@ -962,7 +1225,7 @@ cudaError_t set_trace_smem(int max_stack) {
 // One wavefront iteration (7 launches).
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
                       bool counters, int trace_grid, int shade_grid, cudaStream_t st,
-                      cudaEvent_t* ev) {
+                      cudaEvent_t* ev, int mode) {
   size_t sm = trace_smem(max_stack);
   FirstHitOut none{};
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
@@ -973,14 +1236,20 @@ void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
   else
     k_trace_t<TRACE_EXT, false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
-  k_shade<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  if (mode == 1)
+    k_shade_c<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  else
+    k_shade<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
   if (counters)
     k_trace_t<TRACE_SHADOW, true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   else
     k_trace_t<TRACE_SHADOW, false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
   if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
-  k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  if (mode == 1)
+    k_finish_c<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
+  else
+    k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
   k_advance<<<1, 1, 0, st>>>(W, ctl);
   if (ev) cudaEventRecordWithFlags(ev[5], st, cudaEventRecordExternal);
 }
@@ -1000,6 +1269,12 @@ void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* pri
   WaveState none{};
   k_trace_t<TRACE_FIRST, false><<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack), st>>>(
       S, none, nullptr, max_stack, fo);
+}
+
+void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,
+                    int* valid, cudaStream_t st) {
+  k_env_rows<<<(h + 127) / 128, 128, 0, st>>>(env, w, h, cond, rows);
+  k_env_marg<<<1, 32, 0, st>>>(rows, h, marg, valid);
 }
 
 void launch_resolve(const float4* acc, uchar4* out, int n, int frame, cudaStream_t st) {

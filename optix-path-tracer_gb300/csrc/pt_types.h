@@ -91,6 +91,9 @@ struct DevScene {
   const float* normals;     /* 3 floats per attribute vertex */
   const float* uvs;         /* 2 floats per attribute vertex */
   const uint32_t* leaf_of_id; /* primitive id -> position in the leaf-ordered records */
+  const float* env_marg;    /* environment sampling: marginal CDF over rows (h+1) */
+  const float* env_cond;    /* conditional CDFs, h rows of w+1 */
+  int env_valid;            /* 1 if the environment can be importance sampled */
   int num_lights;
   int num_prims;
   int root_leaf;            /* 1 if the root is a single leaf (<= 3 prims): node 0 still exists */

@@ -270,7 +270,19 @@ struct BNode {
   int right;
 };
 
+// Piecewise-constant importance sampling of the spherical environment map:
+// weight of texel (r, c) = luminance x sin(theta_r), row (conditional) and
+// row-sum (marginal) prefix sums accumulated sequentially in double, then
+// normalised to float.  The GPU builds it with the same sequential sums.
+struct EnvCdf {
+  std::vector<float> marg;  // h+1
+  std::vector<float> cond;  // h rows of w+1
+  int w = 0, h = 0;
+  bool valid = false;
+};
+
 struct Scene {
+  EnvCdf env_cdf;
   std::vector<Material> mats;
   std::vector<Prim> prims;
   std::vector<Xform> xforms;
@@ -1096,6 +1108,276 @@ V3 brdf_eval(const Material& m, V3 Wo, V3 Wi, V3 N, float& pdf) {
 }
 
 // ------------------------------------------------------------- integrator --
+
+// ========================================================= consistent mode ==
+// Unbiased variant: BRDFs evaluated in the local frame of the shading normal
+// (y up, the reference's trig conventions applied to local vectors), pdfs
+// that match the samplers, no throughput clamps, next-event estimation with
+// MIS (power heuristic) against BSDF sampling for area lights and the
+// importance-sampled environment.  Lights are two-sided emitters.
+
+void build_env_cdf(Scene& s) {
+  EnvCdf& E = s.env_cdf;
+  E = EnvCdf();
+  const Miss& m = s.miss;
+  if (m.type != MISS_ENV || !m.spherical || m.w <= 0 || m.h <= 0) return;
+  int W = m.w, H = m.h;
+  E.w = W;
+  E.h = H;
+  E.cond.assign((size_t)H * (W + 1), 0.f);
+  E.marg.assign(H + 1, 0.f);
+  std::vector<double> rows(H);
+  std::vector<double> pre(W + 1);
+  for (int r = 0; r < H; r++) {
+    float theta = PI_F * (((float)r + 0.5f) / (float)H);
+    double sn = (double)pt_sinf(theta);
+    double acc = 0.0;
+    pre[0] = 0.0;
+    for (int c = 0; c < W; c++) {
+      const float* t = &m.env[((size_t)r * W + c) * 4];
+      double lum = 0.2126 * (double)t[0] + 0.7152 * (double)t[1] + 0.0722 * (double)t[2];
+      if (!(lum > 0.0)) lum = 0.0;
+      acc = acc + lum * sn;
+      pre[c + 1] = acc;
+    }
+    rows[r] = acc;
+    float* cr = &E.cond[(size_t)r * (W + 1)];
+    for (int c = 0; c <= W; c++)
+      cr[c] = acc > 0.0 ? (float)(pre[c] / acc) : (float)((double)c / (double)W);
+    cr[W] = 1.f;
+  }
+  double tot = 0.0;
+  std::vector<double> mp(H + 1);
+  mp[0] = 0.0;
+  for (int r = 0; r < H; r++) {
+    tot = tot + rows[r];
+    mp[r + 1] = tot;
+  }
+  if (!(tot > 0.0)) return;
+  for (int r = 0; r <= H; r++) E.marg[r] = (float)(mp[r] / tot);
+  E.marg[H] = 1.f;
+  E.valid = true;
+}
+
+// largest i in [0, n) with cdf[i] <= u (cdf[0] = 0 <= u < cdf[n] = 1)
+inline int cdf_find(const float* cdf, int n, float u) {
+  int lo = 0, hi = n;  // invariant: cdf[lo] <= u < cdf[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (cdf[mid] <= u) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// direction -> (u, v) of the spherical mapping (programs/miss.cu:66-77)
+inline void env_uv(V3 d, float& u, float& v) {
+  float r = length(d);
+  float lon = pt_atan2f(d.z, d.x);
+  float lat = pt_acosf(d.y / r);
+  u = lon * (1.f / (PI_F * 2.f));
+  v = lat * (1.f / PI_F);
+}
+
+float env_pdf_dir(const EnvCdf& E, V3 d) {
+  if (!E.valid) return 0.f;
+  float u, v;
+  env_uv(d, u, v);
+  if (!(u == u) || !(v == v)) return 0.f;
+  if (u < 0.f) u += 1.f;
+  int r = (int)(v * (float)E.h);
+  if (r < 0) r = 0;
+  if (r >= E.h) r = E.h - 1;
+  int c = (int)(u * (float)E.w);
+  if (c < 0) c = 0;
+  if (c >= E.w) c = E.w - 1;
+  const float* cr = &E.cond[(size_t)r * (E.w + 1)];
+  float pm = E.marg[r + 1] - E.marg[r];
+  float pc = cr[c + 1] - cr[c];
+  float theta = PI_F * (((float)r + 0.5f) / (float)E.h);
+  float st = pt_sinf(theta);
+  if (!(st > 0.f)) return 0.f;
+  return pm * pc * (float)E.w * (float)E.h / (2.f * PI_F * PI_F * st);
+}
+
+V3 env_sample_dir(const EnvCdf& E, float u1, float u2) {
+  int r = cdf_find(E.marg.data(), E.h, u1);
+  float dv = (u1 - E.marg[r]) / (E.marg[r + 1] - E.marg[r]);
+  const float* cr = &E.cond[(size_t)r * (E.w + 1)];
+  int c = cdf_find(cr, E.w, u2);
+  float du = (u2 - cr[c]) / (cr[c + 1] - cr[c]);
+  float v = ((float)r + dv) / (float)E.h;
+  float u = ((float)c + du) / (float)E.w;
+  float st, ct, sp, cp;
+  pt_sincosf(PI_F * v, &st, &ct);
+  pt_sincosf(2.f * PI_F * u, &sp, &cp);
+  return v3(st * cp, ct, st * sp);
+}
+
+struct Frame {
+  V3 t, n, b;
+  explicit Frame(V3 N) {
+    Onb o(N);
+    t = o.t;
+    n = o.n;
+    b = o.b;
+  }
+  V3 to_local(V3 w) const { return v3(dot(w, t), dot(w, n), dot(w, b)); }
+  V3 to_world(V3 l) const { return l.x * t + l.y * n + l.z * b; }
+};
+
+inline float GGX_G1c(V3 V, float nu, float nv) { return 1.f / (1.f + GGX_Lambda(V, nu, nv)); }
+
+// BSDF value f (no cosine) for local y-up directions.
+V3 bsdf_f_c(const Material& m, V3 wo, V3 wi) {
+  if (!(wo.y > 0.f) || !(wi.y > 0.f)) return v3(0.f);
+  switch (m.type) {
+    case MAT_LAMBERTIAN:
+      return m.c0 * (1.f / PI_F);
+    case MAT_OREN_NAYAR: {
+      float sinThetaI = SinTheta(wi), sinThetaO = SinTheta(wo);
+      float maxCos = 0;
+      if (sinThetaI > 1e-4 && sinThetaO > 1e-4) {
+        float dCos = CosPhi(wi) * CosPhi(wo) + SinPhi(wi) * SinPhi(wo);
+        maxCos = fmaxf(0.f, dCos);
+      }
+      float sinAlpha, tanBeta;
+      if (AbsCosTheta(wi) > AbsCosTheta(wo)) {
+        sinAlpha = sinThetaO;
+        tanBeta = sinThetaI / AbsCosTheta(wi);
+      } else {
+        sinAlpha = sinThetaI;
+        tanBeta = sinThetaO / AbsCosTheta(wo);
+      }
+      return m.c0 * (1.f / PI_F) * (m.p0 + m.p1 * maxCos * sinAlpha * tanBeta);
+    }
+    case MAT_TORRANCE_SPARROW: {
+      V3 H = normalize(wo + wi);
+      float D = GGX_D(H, m.p0, m.p1);
+      float G = GGX_G(wo, wi, m.p0, m.p1);
+      V3 F = schlick3(m.c0, fabsf(dot(H, wi)));
+      return m.c0 * D * G * F / (4.f * wi.y * wo.y);
+    }
+    case MAT_ASHIKHMIN_SHIRLEY: {
+      V3 Rd = m.c0, Rs = m.c1;
+      float nu = m.p0, nv = m.p1;
+      V3 diffuse = Rd * (28.f / (23.f * PI_F));
+      diffuse *= (v3(1.f) - Rs);
+      diffuse *= (1.f - pt_powf(1.f - wi.y * 0.5f, 5.f));
+      diffuse *= (1.f - pt_powf(1.f - wo.y * 0.5f, 5.f));
+      V3 H = normalize(wo + wi);
+      float HdotI = fabsf(dot(H, wi));
+      float HdotN = H.y;
+      float norm = ptm_sqrt((nu + 1.f) * (nv + 1.f)) / (8.f * PI_F);
+      float lobe = HdotN < 1.f
+                       ? pt_powf(HdotN, (nu * H.x * H.x + nv * H.z * H.z) / (1.f - HdotN * HdotN))
+                       : 1.f;
+      V3 spec = schlick3(Rs, HdotI);
+      spec *= norm;
+      spec *= lobe / (HdotI * fmaxf(wi.y, wo.y));
+      return diffuse + spec;
+    }
+  }
+  return v3(0.f);
+}
+
+float bsdf_pdf_c(const Material& m, V3 wo, V3 wi) {
+  if (!(wo.y > 0.f) || !(wi.y > 0.f)) return 0.f;
+  switch (m.type) {
+    case MAT_LAMBERTIAN:
+    case MAT_OREN_NAYAR:
+      return wi.y * (1.f / PI_F);
+    case MAT_TORRANCE_SPARROW: {
+      V3 H = normalize(wo + wi);
+      float woh = dot(wo, H);
+      if (!(woh > 0.f)) return 0.f;
+      return GGX_G1c(wo, m.p0, m.p1) * GGX_D(H, m.p0, m.p1) / (4.f * wo.y);
+    }
+    case MAT_ASHIKHMIN_SHIRLEY: {
+      float nu = m.p0, nv = m.p1;
+      V3 H = normalize(wo + wi);
+      float woh = dot(wo, H);
+      float HdotN = H.y;
+      float ph = 0.f;
+      if (woh > 0.f && HdotN > 0.f) {
+        float e = HdotN < 1.f ? (nu * H.x * H.x + nv * H.z * H.z) / (1.f - HdotN * HdotN) : 0.f;
+        ph = ptm_sqrt((nu + 1.f) * (nv + 1.f)) / (2.f * PI_F) * pt_powf(HdotN, e);
+        ph = ph / (4.f * woh);
+      }
+      return 0.5f * (wi.y * (1.f / PI_F)) + 0.5f * ph;
+    }
+  }
+  return 0.f;
+}
+
+// local y-up direction sampled from the BSDF (draws two numbers)
+V3 bsdf_sample_c(const Material& m, V3 wo, uint32_t& seed) {
+  float rx = rnd(seed);
+  float ry = rnd(seed);
+  V3 p;
+  switch (m.type) {
+    case MAT_LAMBERTIAN:
+    case MAT_OREN_NAYAR:
+      cosine_sample_hemisphere(rx, ry, p);
+      return v3(p.x, p.z, p.y);
+    case MAT_TORRANCE_SPARROW: {
+      V3 H = normalize(GGX_Sample(wo, rx, ry, m.p0, m.p1));
+      if (dot(H, wo) < 0.f) H = -H;
+      return -wo + 2.f * dot(wo, H) * H;
+    }
+    case MAT_ASHIKHMIN_SHIRLEY: {
+      float nu = m.p0, nv = m.p1;
+      if (rx < 0.5f) {
+        rx = fminf(2.f * rx, 1.f - 1e-6f);
+        cosine_sample_hemisphere(rx, ry, p);
+        return v3(p.x, p.z, p.y);
+      }
+      rx = fminf(2.f * (rx - 0.5f), 1.f - 1e-6f);
+      float phi, cos_theta;
+      if (nu == nv) {
+        phi = 2.f * PI_F * rx;
+        cos_theta = pt_powf(ry, 1.f / (nu + 1.f));
+      } else if (rx < 0.25f) {
+        Sample_Quadrant(nu, nv, 4.f * rx, ry, phi, cos_theta);
+      } else if (rx < 0.5f) {
+        Sample_Quadrant(nu, nv, 4.f * (0.5f - rx), ry, phi, cos_theta);
+        phi = PI_F - phi;
+      } else if (rx < 0.75f) {
+        Sample_Quadrant(nu, nv, 4.f * (rx - 0.5f), ry, phi, cos_theta);
+        phi = PI_F + phi;
+      } else {
+        Sample_Quadrant(nu, nv, 4.f * (1.f - rx), ry, phi, cos_theta);
+        phi = 2.f * PI_F - phi;
+      }
+      float sin_theta = ptm_sqrt(fmaxf(0.f, 1.f - cos_theta * cos_theta));
+      V3 H = Spherical_Vector(sin_theta, cos_theta, phi);
+      if (dot(H, wo) < 0.f) H = -H;
+      return -wo + 2.f * dot(wo, H) * H;
+    }
+  }
+  return v3(0.f, 1.f, 0.f);
+}
+
+// cone sampling toward a sphere light (consistent mode): direction to the
+// sampled point on the cone (unnormalised) and the distance limit
+inline V3 sphere_light_sample_c(const Light& L, V3 P, uint32_t& seed) {
+  float r1 = rnd(seed);
+  float r2 = rnd(seed);
+  V3 dc = L.c - P;
+  float dist2 = dot(dc, dc);
+  float z = 1.f + r2 * (ptm_sqrt(fmaxf(0.f, 1.f - L.r * L.r / dist2)) - 1.f);
+  float phi = 2.f * PI_F * r1;
+  float sp, cp;
+  pt_sincosf(phi, &sp, &cp);
+  float sz = ptm_sqrt(fmaxf(0.f, 1.f - z * z));
+  V3 w = v3(cp * sz, sp * sz, z);
+  Onb uvw(normalize(dc));
+  uvw.inverse_transform(w);
+  return w;
+}
+
+inline float power_mis(float a, float b) { return (a * a) / (a * a + b * b); }
+
 struct Params {
   int width, height, spp, frame0, max_depth, rr_enable, rr_depth, mode, guide;
 };
@@ -1350,6 +1632,126 @@ struct Tracer {
     return v3(0.f);
   }
 
+
+  // sum over lights of the light-sampling pdf of direction d from P (per
+  // selection), for MIS at emitter hits and misses
+  float lights_pdf_c(V3 P, V3 d, int n_sel) {
+    float acc = 0.f;
+    for (size_t k = 0; k < s.lights.size(); k++) acc += light_pdf(s.lights[k], P, d);
+    return acc / (float)n_sel;
+  }
+
+  V3 color_c(Ray ray, uint32_t seed, const Params& pr) {
+    float tm = s.cam.time0 + rnd(seed) * (s.cam.time1 - s.cam.time0);
+    (void)tm;
+    V3 thr = v3(1.f), rad = v3(0.f);
+    bool prev_spec = true;
+    float pdf_prev = 0.f;
+    const bool env_is = s.env_cdf.valid;
+    const int n_lights = (int)s.lights.size();
+    const int n_sel = n_lights + (env_is ? 1 : 0);
+    for (int depth = 0; depth < pr.max_depth; depth++) {
+      ext++;
+      Hit h = trace(s, ray, cnt);
+      if (h.prim < 0) {
+        PRD prd;
+        prd.throughput = v3(1.f);
+        miss(prd, ray);  // radiance multiplier of the miss programs
+        float w = 1.f;
+        if (!prev_spec && env_is) w = power_mis(pdf_prev, env_pdf_dir(s.env_cdf, ray.d) / (float)n_sel);
+        rad += thr * prd.throughput * w;
+        break;
+      }
+      const Prim& p = s.prims[h.prim];
+      HitRecord rec = hit_record(s, p, ray, h.t, h.u, h.v);
+      const Material& m = s.mats[rec.index];
+      V3 P = rec.P, Wo = rec.Wo, N = rec.shading_normal;
+      if (m.type == MAT_DIFFUSE_LIGHT) {
+        float w = 1.f;
+        if (!prev_spec && n_sel > 0) w = power_mis(pdf_prev, lights_pdf_c(ray.o, ray.d, n_sel));
+        rad += thr * m.c0 * w;
+        break;
+      }
+      if (m.type == MAT_METAL || m.type == MAT_DIELECTRIC) {
+        PRD prd;
+        prd.seed = seed;
+        prd.throughput = thr;
+        prd.radiance = rad;
+        closest_hit(prd, ray, h);
+        seed = prd.seed;
+        thr = prd.throughput;
+        ray = Ray{prd.origin, prd.direction, 1e-3f, RAY_TMAX};
+        prev_spec = true;
+      } else {
+        Frame fr(N);
+        V3 wo_l = fr.to_local(Wo);
+        // next-event estimation
+        if (n_sel > 0) {
+          int k = (int)(rnd(seed) * (float)n_sel);
+          if (k > n_sel - 1) k = n_sel - 1;
+          V3 Wi;
+          float pl = 0.f, tmax = RAY_TMAX;
+          V3 Le;
+          if (k < n_lights) {
+            const Light& L = s.lights[k];
+            if (L.type == LIGHT_RECT) {
+              Wi = light_sample(L, P, seed);
+              tmax = 1.f - 1e-4f;
+            } else {
+              Wi = sphere_light_sample_c(L, P, seed);
+              float a = dot(Wi, Wi), b = dot(P - L.c, Wi);
+              float c = dot(P - L.c, P - L.c) - L.r * L.r;
+              float disc = b * b - a * c;
+              float tn = disc >= 0.f ? (-b - ptm_sqrt(disc)) / a : 0.f;
+              tmax = tn * (1.f - 1e-4f);
+            }
+            pl = light_pdf(L, P, Wi);
+            Le = L.emission;
+          } else {
+            float u1 = rnd(seed);
+            float u2 = rnd(seed);
+            Wi = env_sample_dir(s.env_cdf, u1, u2);
+            pl = env_pdf_dir(s.env_cdf, Wi);
+            PRD q;
+            q.throughput = v3(1.f);
+            miss(q, Ray{P, Wi, 1e-3f, RAY_TMAX});
+            Le = q.throughput;
+          }
+          V3 wi_n = normalize(Wi);
+          float cs = dot(wi_n, N);
+          float pls = pl / (float)n_sel;
+          if (cs > 0.f && pls > 0.f && tmax > 1e-3f) {
+            V3 wi_l = fr.to_local(wi_n);
+            V3 f = bsdf_f_c(m, wo_l, wi_l);
+            float pb = bsdf_pdf_c(m, wo_l, wi_l);
+            V3 c = f * Le * (cs * power_mis(pls, pb) / pls);
+            if (!isNull(c)) {
+              shadow++;
+              Ray sr{P, Wi, 1e-3f, tmax};
+              Hit sh = trace(s, sr, cnt);
+              if (sh.prim < 0) rad += thr * c;
+            }
+          }
+        }
+        // BSDF continuation
+        V3 wi_l = bsdf_sample_c(m, wo_l, seed);
+        float pb = bsdf_pdf_c(m, wo_l, wi_l);
+        V3 f = bsdf_f_c(m, wo_l, wi_l);
+        if (!(pb > 0.f) || isNull(f) || !(wi_l.y > 0.f)) break;
+        thr *= f * (wi_l.y / pb);
+        prev_spec = false;
+        pdf_prev = pb;
+        ray = Ray{P, fr.to_world(wi_l), 1e-3f, RAY_TMAX};
+      }
+      if (pr.rr_enable && depth > pr.rr_depth) {
+        float q = fminf(1.f, max_component(thr));
+        if (rnd(seed) >= q) break;
+        thr *= 1.f / q;
+      }
+    }
+    return rad;
+  }
+
   // programs/raygen.cu:50-64 + 148-165; returns the path's colour
   Ray camera_ray(uint32_t x, uint32_t y, uint32_t W, uint32_t H, uint32_t& seed) {
     float u = float((float)x + rnd(seed)) / (float)W;
@@ -1366,7 +1768,7 @@ struct Tracer {
     uint32_t W = pr.width, H = pr.height;
     uint32_t seed = tea64(W * y + x, (uint32_t)frame);
     Ray ray = camera_ray(x, y, W, H, seed);
-    V3 col = color(ray, seed, pr);
+    V3 col = pr.mode == 1 ? color_c(ray, seed, pr) : color(ray, seed, pr);
     if (!(col.x == col.x)) col.x = 0.f;  // de_nan, programs/raygen.cu:126-134
     if (!(col.y == col.y)) col.y = 0.f;
     if (!(col.z == col.z)) col.z = 0.f;
@@ -1535,6 +1937,7 @@ void or_set_camera(void* sp, const float* from, const float* at, const float* up
 
 int or_commit(void* sp) {
   Scene& s = *(Scene*)sp;
+  build_env_cdf(s);
   s.nodes.clear();
   s.order.resize(s.prims.size());
   for (size_t i = 0; i < s.prims.size(); i++) s.order[i] = (int)i;
@@ -1673,3 +2076,65 @@ int or_hit_record(void* sp, const float* o, const float* d, float* out) {
 }
 
 }  // extern "C"
+
+// Consistent-mode BSDF of one material (user parameters, converted as the
+// material constructors do) for local y-up directions: f (rgb) and pdf.
+extern "C" void or_bsdf_c(int type, const float* c0, const float* c1, float p0, float p1,
+                          const float* wo, const float* wi, float* f, float* pdf) {
+  Scene tmp;
+  int id = or_add_material(&tmp, type, c0, c1, p0, p1);
+  const Material& m = tmp.mats[id];
+  V3 a = v3(wo[0], wo[1], wo[2]), b = v3(wi[0], wi[1], wi[2]);
+  V3 r = bsdf_f_c(m, a, b);
+  f[0] = r.x;
+  f[1] = r.y;
+  f[2] = r.z;
+  *pdf = bsdf_pdf_c(m, a, b);
+}
+
+// n samples of the consistent-mode BSDF sampler from one seed stream.
+extern "C" void or_bsdf_sample_c(int type, const float* c0, const float* c1, float p0, float p1,
+                                 const float* wo, uint32_t seed, int n, float* wi) {
+  Scene tmp;
+  int id = or_add_material(&tmp, type, c0, c1, p0, p1);
+  const Material& m = tmp.mats[id];
+  V3 a = v3(wo[0], wo[1], wo[2]);
+  for (int k = 0; k < n; k++) {
+    V3 r = bsdf_sample_c(m, a, seed);
+    wi[3 * k] = r.x;
+    wi[3 * k + 1] = r.y;
+    wi[3 * k + 2] = r.z;
+  }
+}
+
+// Environment sampling of a committed scene: n directions from n uniform
+// pairs, and the pdf of each returned direction.
+extern "C" int or_env_sample(void* sp, const float* u, int n, float* dirs, float* pdf) {
+  Scene& s = *(Scene*)sp;
+  if (!s.env_cdf.valid) return 0;
+  for (int k = 0; k < n; k++) {
+    V3 d = env_sample_dir(s.env_cdf, u[2 * k], u[2 * k + 1]);
+    dirs[3 * k] = d.x;
+    dirs[3 * k + 1] = d.y;
+    dirs[3 * k + 2] = d.z;
+    pdf[k] = env_pdf_dir(s.env_cdf, d);
+  }
+  return 1;
+}
+
+// Batched form of or_bsdf_c for quadrature checks.
+extern "C" void or_bsdf_c_batch(int type, const float* c0, const float* c1, float p0, float p1,
+                                const float* wo, int n, const float* wi, float* f, float* pdf) {
+  Scene tmp;
+  int id = or_add_material(&tmp, type, c0, c1, p0, p1);
+  const Material& m = tmp.mats[id];
+  V3 a = v3(wo[0], wo[1], wo[2]);
+  for (int k = 0; k < n; k++) {
+    V3 b = v3(wi[3 * k], wi[3 * k + 1], wi[3 * k + 2]);
+    V3 r = bsdf_f_c(m, a, b);
+    f[3 * k] = r.x;
+    f[3 * k + 1] = r.y;
+    f[3 * k + 2] = r.z;
+    pdf[k] = bsdf_pdf_c(m, a, b);
+  }
+}

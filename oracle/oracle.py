@@ -55,6 +55,12 @@ def load():
     L.or_math.argtypes = [ctypes.c_int, _P, _P, _P, ctypes.c_int]
     L.or_trace_ray.argtypes = [_P, _P, _P, ctypes.c_float, _P, _P]
     L.or_hit_record.argtypes = [_P, _P, _P, _P]
+    L.or_bsdf_c.argtypes = [ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P]
+    L.or_bsdf_sample_c.argtypes = [ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float, _P,
+                                   ctypes.c_uint32, ctypes.c_int, _P]
+    L.or_env_sample.argtypes = [_P, _P, ctypes.c_int, _P, _P]
+    L.or_bsdf_c_batch.argtypes = [ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float, _P,
+                                  ctypes.c_int, _P, _P, _P]
     _lib = L
     return L
 
@@ -125,6 +131,14 @@ class Oracle:
         L.or_set_camera(h, _p(_f(cf)), _p(_f(ca)), _p(_f(cu)), vfov, aspect, ap, fd, t0, t1)
         L.or_commit(h)
 
+    def env_sample(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float32)
+        n = len(u)
+        dirs = np.zeros((n, 3), dtype=np.float32)
+        pdf = np.zeros(n, dtype=np.float32)
+        ok = self.L.or_env_sample(self.h, _p(u), n, _p(dirs), _p(pdf))
+        return (dirs, pdf) if ok else (None, None)
+
     def first_hits(self, width, height, frame, threads=0):
         prim = np.zeros(width * height, dtype=np.int32)
         mat = np.zeros(width * height, dtype=np.int32)
@@ -139,21 +153,50 @@ class Oracle:
                         dtype=np.int32)
 
     def render_paths(self, width, height, frame, pixels, max_depth=50, rr_enable=1, rr_depth=10,
-                     threads=0):
+                     threads=0, mode=0):
         pix = np.ascontiguousarray(pixels, dtype=np.uint32)
         out = np.zeros((len(pix), 3), dtype=np.float32)
-        prm = self._params(width, height, 1, frame, max_depth, rr_enable, rr_depth)
+        prm = self._params(width, height, 1, frame, max_depth, rr_enable, rr_depth, mode)
         self.L.or_render_paths(self.h, _p(prm), frame, _p(pix), len(pix), _p(out),
                                threads or os.cpu_count())
         return out
 
     def render(self, width, height, spp, frame0=0, max_depth=50, rr_enable=1, rr_depth=10,
-               acc=None, pixel_stride=1, pixel_offset=0, threads=0):
+               acc=None, pixel_stride=1, pixel_offset=0, threads=0, mode=0):
         if acc is None:
             acc = np.zeros((height, width, 4), dtype=np.float32)
-        prm = self._params(width, height, spp, frame0, max_depth, rr_enable, rr_depth)
+        prm = self._params(width, height, spp, frame0, max_depth, rr_enable, rr_depth, mode)
         stats = np.zeros(3, dtype=np.uint64)
         secs = self.L.or_render(self.h, _p(prm), _p(acc), pixel_stride, pixel_offset,
                                 threads or os.cpu_count(), _p(stats))
         return acc, {"seconds": secs, "ext_rays": int(stats[0]), "shadow_rays": int(stats[1]),
                      "paths": int(stats[2])}
+
+
+def bsdf_c(mtype, c0, c1, p0, p1, wo, wi):
+    """Consistent-mode f (rgb) and pdf for local y-up directions."""
+    L = load()
+    f = np.zeros(3, dtype=np.float32)
+    pdf = np.zeros(1, dtype=np.float32)
+    c1a = None if c1 is None else _f(c1)
+    L.or_bsdf_c(mtype, _p(_f(c0)), _p(c1a), p0, p1, _p(_f(wo)), _p(_f(wi)), _p(f), _p(pdf))
+    return f, float(pdf[0])
+
+
+def bsdf_sample_c(mtype, c0, c1, p0, p1, wo, seed, n):
+    L = load()
+    out = np.zeros((n, 3), dtype=np.float32)
+    c1a = None if c1 is None else _f(c1)
+    L.or_bsdf_sample_c(mtype, _p(_f(c0)), _p(c1a), p0, p1, _p(_f(wo)), seed, n, _p(out))
+    return out
+
+
+def bsdf_c_batch(mtype, c0, c1, p0, p1, wo, wi):
+    L = load()
+    wi = np.ascontiguousarray(wi, dtype=np.float32)
+    n = len(wi)
+    f = np.zeros((n, 3), dtype=np.float32)
+    pdf = np.zeros(n, dtype=np.float32)
+    c1a = None if c1 is None else _f(c1)
+    L.or_bsdf_c_batch(mtype, _p(_f(c0)), _p(c1a), p0, p1, _p(_f(wo)), n, _p(wi), _p(f), _p(pdf))
+    return f, pdf

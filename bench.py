@@ -31,9 +31,10 @@ WORKLOADS = {
     "cornell": ("cornell_c1", 512, 512, 64, dict(max_depth=50, rr_depth=3),
                 "Cornell box: 512x512, 64 spp, 8 primitives (6 quads + 2 rotated boxes), "
                 "one area light, max depth 50, RR after depth 3"),
-    "heightfield": ("heightfield_scene", 1920, 1080, 256, dict(max_depth=50, rr_depth=10),
+    "heightfield": ("heightfield_scene", 1920, 1080, 256, dict(max_depth=50, rr_depth=10, mode=1),
                     "triangle heightfield: 1920x1080, 256 spp, 2,097,152 triangles, "
-                    "TS/AS/ON tiles, 2048x1024 HDR sky"),
+                    "TS/AS/ON tiles, 2048x1024 HDR sky importance-sampled through its 2D CDF "
+                    "(consistent mode: NEE + MIS)"),
 }
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")

@@ -915,7 +915,8 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S, WaveStat
       float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
       V3 d = f4xyz(rdv);
       uint32_t depth = st.z & 0xffffu;
-      bool prev_spec = (st.z >> 16) & 1u;
+      // a camera ray counts as a specular bounce: emission it sees is not MIS-weighted
+      bool prev_spec = ((st.z >> 16) & 1u) || depth == 0;
       float pdf_prev = __uint_as_float(st.w);
       uint32_t leaf = __float_as_uint(hit.w);
       if (leaf == PT_NO_HIT) {

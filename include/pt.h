@@ -67,6 +67,7 @@ typedef struct pt_options {
   int enable_counters; /* count BVH node fetches and primitive tests */
   int enable_timing;   /* per-stage device times (CUDA events in the graph) */
   int bvh_builder;     /* 0 automatic, 1 host (binned SAH), 2 GPU (LBVH + treelets) */
+  int bvh_width;       /* most children per BVH node, 2..8; 0 = 8 */
 } pt_options;
 
 typedef struct pt_render_params {
@@ -96,6 +97,7 @@ typedef struct pt_stats {
   /* device time per stage (enable_timing): generate, trace, shade,
      shadow trace, finish + queue advance */
   double stage_ms[5];
+  uint64_t graph_launches; /* CUDA-graph launches of the last render */
 } pt_stats;
 
 /* ---- context (replaces optix::Context, host_includes/host_common.hpp:21-45) */
@@ -201,7 +203,7 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out);
 /* pt_render for callers that cannot allocate device memory while rendering
  * (a strict memory pool, or an application that allocates only at start-up).
  * No counterpart in the reference.  It calls no cudaMalloc/cudaFree: its
- * wavefront scratch is a fixed 8.5 MiB device array inside libpt.so that
+ * wavefront scratch is a fixed 8.75 MiB device array inside libpt.so that
  * every GPU loading the library holds until exit.  Same results as
  * pt_render.  accum_rgba must be device memory; images of at most 262144
  * pixels (PT_EINVAL beyond); fewer paths in flight, so slower.  All calls
@@ -210,6 +212,50 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out);
  * (cudaGetSymbolAddress); make it before any stream capture. */
 PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params* params, float* accum_rgba,
                              void* stream);
+
+/* ---- batched multi-scene rendering ---------------------------------------
+ * No counterpart in the reference (its main.cpp renders one scene per
+ * process).  Renders many committed scenes in one wavefront: the paths of
+ * all scenes share the path-state buffers, so small scenes and the drained
+ * tail of each render do not leave the GPU idle.  The whole batch is one
+ * CUDA-graph launch whose chunk and iteration loops are device-side
+ * conditional (while) nodes, each bounded on the device.  Each item's
+ * accumulator receives exactly what pt_render gives for the same scene and
+ * parameters.  The batch keeps its own copy of the scenes' geometry
+ * (rebuilt when a scene is re-committed or the node width changes). */
+typedef struct pt_batch pt_batch;
+
+typedef struct pt_batch_item {
+  pt_context* scene;        /* committed context on the batch's device */
+  pt_render_params params;  /* per item; `mode` must be equal for all items, guide 0 */
+  float* accum_rgba;        /* W*H float4, host or device memory (as pt_render) */
+} pt_batch_item;
+
+/* Launch configuration of a batch, chosen by pt_batch_autotune. */
+typedef struct pt_tune {
+  int path_slots;           /* paths in flight */
+  int trace_block;          /* threads per trace block: 64, 128 or 256 */
+  int shade_block;          /* threads per shade block: 64..256, multiple of 32 */
+  int bvh_width;            /* most children per BVH node, 2..8 */
+  int chunk_paths;          /* paths per chunk (per-path result area), 0 = 2^27 */
+  double sample_paths_per_s;/* autotune: throughput of this configuration on its sample */
+} pt_tune;
+
+/* opt: device and builder as for a context (path_slots and bvh_width give
+ * the initial tune). */
+PT_API int pt_batch_create(const pt_options* opt, pt_batch** out);
+PT_API int pt_batch_destroy(pt_batch* b);
+PT_API const char* pt_batch_last_error(pt_batch* b);
+/* Renders n items (1..32767).  Stats (pt_batch_get_stats) sum all items. */
+PT_API int pt_batch_render(pt_batch* b, const pt_batch_item* items, int n, void* stream);
+/* Times short renders of a sample of the items (every item at low spp, into
+ * scratch accumulators; the items' accumulators are not touched) over path
+ * slots, trace and shade block sizes and BVH node width, keeps the fastest
+ * configuration for later pt_batch_render calls and returns it in *best. */
+PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_tune* best);
+PT_API int pt_batch_set_tune(pt_batch* b, const pt_tune* t);
+PT_API int pt_batch_get_tune(pt_batch* b, pt_tune* t);
+PT_API int pt_batch_get_stats(pt_batch* b, pt_stats* out);
 
 #ifdef __cplusplus
 }

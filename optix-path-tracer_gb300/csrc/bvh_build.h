@@ -107,7 +107,8 @@ inline void encode_node(const Box& parent, const WideChild* ch, int nch, uint32_
                         uint32_t prim_base, uint32_t out[20]) {
   encode_node_dev(parent, ch, nch, child_base, prim_base, out);
 }
-int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out);
+/* width: most children per node, 2..8 (the node format holds 8) */
+int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out, int width = 8);
 bool validate_bvh8(const Bvh8Out& b, size_t num_prims);
 
 }  // namespace pt

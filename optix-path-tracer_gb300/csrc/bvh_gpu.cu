@@ -13,8 +13,9 @@
  *                   programming over leaf subsets (Karras & Aila, "Fast
  *                   Parallel Construction of High-Quality BVHs", HPG 2013);
  *                   run twice
- *  6. k_collapse    one launch per level: each binary node becomes an 8-wide
- *                   node by expanding its largest child until 8 children;
+ *  6. k_collapse    one launch per level: each binary node becomes a wide
+ *                   node by expanding its largest child until 8 children
+ *                   (or the requested width);
  *                   subtrees of <= 3 primitives become leaf slots; child
  *                   boxes are quantised to 8 bits (node format: pt_types.h)
  * The result is order independent for rendering (closest hit is the minimum
@@ -57,6 +58,15 @@ __device__ __forceinline__ void box_store(float4* lo, float4* hi, uint32_t i, co
 }
 __device__ __forceinline__ GBox box_load(const float4* lo, const float4* hi, uint32_t i) {
   float4 a = lo[i], b = hi[i];
+  GBox r;
+  r.lo[0] = a.x; r.lo[1] = a.y; r.lo[2] = a.z;
+  r.hi[0] = b.x; r.hi[1] = b.y; r.hi[2] = b.z;
+  return r;
+}
+// Loads of tree data that other threads write during the same kernel
+// (k_bottom_up): L2 only (ld.global.cg), so no stale L1 line is read.
+__device__ __forceinline__ GBox box_load_cg(const float4* lo, const float4* hi, uint32_t i) {
+  float4 a = __ldcg(lo + i), b = __ldcg(hi + i);
   GBox r;
   r.lo[0] = a.x; r.lo[1] = a.y; r.lo[2] = a.z;
   r.hi[0] = b.x; r.hi[1] = b.y; r.hi[2] = b.z;
@@ -228,15 +238,21 @@ struct Tree {
   uint32_t* flags;
 };
 
+// Internal-node data (boxes, costs, counts, links) is written by other
+// threads of k_bottom_up while it runs, so it is read through L2 only; leaf
+// boxes come from an earlier kernel.
 __device__ __forceinline__ GBox ref_box(const Tree& T, uint32_t r) {
-  return (r & LEAF_BIT) ? box_load(T.llo, T.lhi, r & ~LEAF_BIT) : box_load(T.ilo, T.ihi, r);
+  return (r & LEAF_BIT) ? box_load(T.llo, T.lhi, r & ~LEAF_BIT) : box_load_cg(T.ilo, T.ihi, r);
 }
 __device__ __forceinline__ float ref_cost(const Tree& T, uint32_t r) {
-  return (r & LEAF_BIT) ? C_TRI * box_area(box_load(T.llo, T.lhi, r & ~LEAF_BIT)) : T.ilo[r].w;
+  return (r & LEAF_BIT) ? C_TRI * box_area(box_load(T.llo, T.lhi, r & ~LEAF_BIT))
+                        : __ldcg(&T.ilo[r].w);
 }
 __device__ __forceinline__ float ref_count(const Tree& T, uint32_t r) {
-  return (r & LEAF_BIT) ? 1.f : T.ihi[r].w;
+  return (r & LEAF_BIT) ? 1.f : __ldcg(&T.ihi[r].w);
 }
+__device__ __forceinline__ uint32_t left_of(const Tree& T, uint32_t x) { return __ldcg(T.left + x); }
+__device__ __forceinline__ uint32_t right_of(const Tree& T, uint32_t x) { return __ldcg(T.right + x); }
 __device__ __forceinline__ void set_parent(const Tree& T, uint32_t r, uint32_t p) {
   if (r & LEAF_BIT) T.parent_leaf[r & ~LEAF_BIT] = p;
   else T.parent_int[r] = p;
@@ -247,15 +263,15 @@ __device__ __forceinline__ void set_parent(const Tree& T, uint32_t r, uint32_t p
 __device__ void optimize_treelet(const Tree& T, uint32_t root) {
   uint32_t leaves[7], inner[6];
   int nl = 2, ni = 1;
-  leaves[0] = T.left[root];
-  leaves[1] = T.right[root];
+  leaves[0] = left_of(T, root);
+  leaves[1] = right_of(T, root);
   inner[0] = root;
   while (nl < 7) {
     int best = -1;
     float ba = -1.f;
     for (int k = 0; k < nl; k++) {
       if (leaves[k] & LEAF_BIT) continue;
-      float a = box_area(box_load(T.ilo, T.ihi, leaves[k]));
+      float a = box_area(box_load_cg(T.ilo, T.ihi, leaves[k]));
       if (a > ba) {
         ba = a;
         best = k;
@@ -264,8 +280,8 @@ __device__ void optimize_treelet(const Tree& T, uint32_t root) {
     if (best < 0) break;
     uint32_t x = leaves[best];
     inner[ni++] = x;
-    leaves[best] = T.left[x];
-    leaves[nl++] = T.right[x];
+    leaves[best] = left_of(T, x);
+    leaves[nl++] = right_of(T, x);
   }
   if (nl < 3) return;
   const int full = (1 << nl) - 1;
@@ -339,14 +355,14 @@ __global__ void k_bottom_up(Tree T, int n, int optimize) {
     __threadfence();
     if (atomicAdd(&T.flags[node], 1u) == 0) return;
     __threadfence();
-    uint32_t l = T.left[node], r = T.right[node];
+    uint32_t l = left_of(T, node), r = right_of(T, node);
     GBox b = box_union(ref_box(T, l), ref_box(T, r));
     float cnt = ref_count(T, l) + ref_count(T, r);
     float cost = C_INNER * box_area(b) + ref_cost(T, l) + ref_cost(T, r);
     box_store(T.ilo, T.ihi, node, b, cost, cnt);
     if (optimize && cnt >= 7.f) optimize_treelet(T, node);
     __threadfence();
-    node = T.parent_int[node];
+    node = __ldcg(T.parent_int + node);
   }
 }
 
@@ -354,11 +370,13 @@ struct CollapseOut {
   uint4* nodes;           // 5 per node
   float4* rec_out;        // leaf-ordered primitive records
   uint32_t* leaf_of_id;
-  uint32_t* counters;     // [0] nodes, [1] primitives, [2] next-level queue length
+  uint32_t* counters;     // [0] nodes, [1] primitives, [2] next-level queue length, [3] error
+  uint32_t n;             // primitives = capacity of nodes, records and queues
 };
 
 // gathers the primitives of a subtree with <= 3 of them
-__device__ int gather_small(const Tree& T, const uint32_t* sorted_prim, uint32_t r, uint32_t* out) {
+__device__ __forceinline__ int gather_small(const Tree& T, const uint32_t* sorted_prim, uint32_t r,
+                                            uint32_t* out) {
   int cnt = 0;
   uint32_t stk[4];
   int sp = 0;
@@ -378,7 +396,7 @@ __device__ int gather_small(const Tree& T, const uint32_t* sorted_prim, uint32_t
 
 __global__ void k_collapse(Tree T, const uint32_t* __restrict__ sorted_prim,
                            const float4* __restrict__ rec_in, const uint2* __restrict__ qin,
-                           uint32_t nq, uint2* qout, CollapseOut out) {
+                           uint32_t nq, uint2* qout, CollapseOut out, int width) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq) return;
   uint2 it = qin[t];
@@ -389,7 +407,11 @@ __global__ void k_collapse(Tree T, const uint32_t* __restrict__ sorted_prim,
   } else {
     kids[nk++] = T.left[it.x];
     kids[nk++] = T.right[it.x];
-    while (nk < 8) {
+    // at most 6 expansions (2 -> 8 children); a fixed trip count keeps the
+    // per-thread arrays in registers
+#pragma unroll
+    for (int ex = 0; ex < 6; ex++) {
+      if (nk >= width) break;
       int best = -1;
       float ba = -1.f;
       for (int k = 0; k < nk; k++) {
@@ -415,14 +437,22 @@ __global__ void k_collapse(Tree T, const uint32_t* __restrict__ sorted_prim,
     if (!(kids[k] & LEAF_BIT) && c > 3.f) {
       n_int++;
       cnts[k] = 0;
-    } else {
+    } else if (c >= 1.f && c <= 3.f) {
       cnts[k] = (uint32_t)c;
       nprim += cnts[k];
+    } else {  // a count a valid tree cannot have: flag it, write nothing
+      atomicOr(&out.counters[3], 1u);
+      return;
     }
   }
   uint32_t child_base = n_int ? atomicAdd(&out.counters[0], (uint32_t)n_int) : 0;
   uint32_t prim_base = nprim ? atomicAdd(&out.counters[1], nprim) : 0;
   uint32_t qbase = n_int ? atomicAdd(&out.counters[2], (uint32_t)n_int) : 0;
+  if (it.y >= out.n || child_base + (uint32_t)n_int > out.n || prim_base + nprim > out.n ||
+      qbase + (uint32_t)n_int > out.n) {
+    atomicOr(&out.counters[3], 2u);  // would overrun the buffers: the host rejects the tree
+    return;
+  }
   pt::WideChild wc[8];
   GBox parent;
   for (int a = 0; a < 3; a++) {
@@ -448,7 +478,10 @@ __global__ void k_collapse(Tree T, const uint32_t* __restrict__ sorted_prim,
       wc[k].count = cnts[k];
       wc[k].prim_off = off;
       uint32_t pr[3];
-      gather_small(T, sorted_prim, kids[k], pr);
+      if (gather_small(T, sorted_prim, kids[k], pr) != (int)cnts[k]) {
+        atomicOr(&out.counters[3], 4u);
+        return;
+      }
       for (uint32_t q = 0; q < cnts[k]; q++) {
         uint32_t dst = prim_base + off + q;
         out.rec_out[3 * dst] = rec_in[3 * pr[q]];
@@ -492,12 +525,15 @@ namespace pt {
 
 // Builds the BVH8 of n primitive records (call order, on the device) into
 // d_nodes / d_rec_out / d_leaf_of_id (allocated by the caller: n nodes,
-// n records, n ids).  Returns the number of nodes and the depth.
+// n records, n ids).  Returns the number of nodes and the depth (depth < 0:
+// the collapse met an inconsistent tree and stopped before overrunning a
+// buffer; -depth: 1 bad count, 2 capacity, 4 leaf gather mismatch).
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
-                           uint32_t* out_nodes, int* out_depth, int treelet_rounds,
+                           uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
                            cudaStream_t st) {
   cudaError_t e = cudaSuccess;
+  if (width < 2 || width > 8) width = 8;
   float4 *lo = nullptr, *hi = nullptr, *ilo = nullptr, *ihi = nullptr, *slo = nullptr,
          *shi = nullptr;
   uint32_t *keys = nullptr, *vals = nullptr, *keys2 = nullptr, *vals2 = nullptr, *left = nullptr,
@@ -508,7 +544,7 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
   size_t tmp_bytes = 0;
   uint32_t ni = n > 1 ? n - 1 : 1;
   int depth = 0;
-  uint32_t h_cnt[3] = {1, 0, 0};
+  uint32_t h_cnt[4] = {1, 0, 0, 0};
   unsigned int h_cbox[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
 #define BV(x)                         \
   do {                                \
@@ -530,7 +566,7 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
   BV(dalloc(&pint, ni));
   BV(dalloc(&pleaf, n));
   BV(dalloc(&flags, ni));
-  BV(dalloc(&counters, 3));
+  BV(dalloc(&counters, 4));
   BV(dalloc(&cbox, 6));
   BV(dalloc(&qa, n));
   BV(dalloc(&qb, n));
@@ -569,21 +605,21 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
     uint2 root = make_uint2(n > 1 ? 0u : (0u | LEAF_BIT), 0u);
     BV(cudaMemcpyAsync(qa, &root, sizeof(root), cudaMemcpyHostToDevice, st));
     uint32_t nq = 1;
-    CollapseOut co{d_nodes, d_rec_out, d_leaf_of_id, counters};
+    CollapseOut co{d_nodes, d_rec_out, d_leaf_of_id, counters, n};
     while (nq) {
       depth++;
       BV(cudaMemsetAsync(counters + 2, 0, 4, st));
-      k_collapse<<<(nq + 127) / 128, 128, 0, st>>>(T, vals2, d_rec, qa, nq, qb, co);
+      k_collapse<<<(nq + 127) / 128, 128, 0, st>>>(T, vals2, d_rec, qa, nq, qb, co, width);
       BV(cudaMemcpyAsync(h_cnt, counters, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
       BV(cudaStreamSynchronize(st));
-      nq = h_cnt[2];
+      nq = h_cnt[3] ? 0u : h_cnt[2];
       uint2* tq = qa;
       qa = qb;
       qb = tq;
     }
     BV(cudaGetLastError());
-    *out_nodes = h_cnt[0];
-    *out_depth = depth;
+    *out_nodes = h_cnt[3] ? 0u : h_cnt[0];
+    *out_depth = h_cnt[3] ? -(int)h_cnt[3] : depth;  // < 0: the collapse found an inconsistent tree
   }
 done:
 #undef BV

@@ -151,7 +151,8 @@ struct Bvh2 {
 // The quantisation grid of encode_node extends the parent box upward by up
 // to 255 steps; the parent itself must cover the children, which the caller
 // guarantees (parent = union of children).
-int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out) {
+int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out, int width) {
+  if (width < 2 || width > 8) width = 8;
   size_t n = boxes.size();
   out.nodes.clear();
   out.leaf_order.clear();
@@ -179,7 +180,7 @@ int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out) {
     uint32_t self = (uint32_t)head;
     head++;
     out.depth = std::max(out.depth, pd.depth);
-    // gather up to 8 children by expanding the largest internal child
+    // gather up to `width` children by expanding the largest internal child
     std::vector<int> kids;
     const BNode& bn = B[pd.bnode];
     if (bn.left < 0) {
@@ -187,7 +188,7 @@ int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out) {
     } else {
       kids.push_back(bn.left);
       kids.push_back(bn.right);
-      while (kids.size() < 8) {
+      while ((int)kids.size() < width) {
         int best = -1;
         float best_area = -1.f;
         for (size_t k = 0; k < kids.size(); k++) {

@@ -20,108 +20,22 @@
 
 #include "../../include/pt.h"
 #include "bvh_build.h"
+#include "pt_context.h"
 #include "pt_internal.h"
 #include "ptmath.h"
 
 namespace pt {
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
-                           uint32_t* out_nodes, int* out_depth, int treelet_rounds,
+                           uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
                            cudaStream_t st);
 }
 
 namespace {
-
 const float PI_F = 3.141592654f;
-
-struct HostPrim {
-  int type, axis, flip, xform;
-  uint32_t material;
-  float f[9];
-};
-
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  cudaError_t ensure(size_t count) {
-    if (count <= n && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    cudaError_t e = cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
-    if (e == cudaSuccess) n = count;
-    return e;
-  }
-  cudaError_t upload(const T* h, size_t count, cudaStream_t st) {
-    cudaError_t e = ensure(count);
-    if (e != cudaSuccess || count == 0) return e;
-    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st);
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-};
-
 }  // namespace
 
-struct pt_context {
-  int device = 0;
-  std::string err;
-  pt_options opt{};
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // ---- host scene
-  std::vector<GpuMaterial> mats;
-  std::vector<HostPrim> prims;
-  std::vector<float> xforms;  // 24 floats each: m rows, inv rows (float4-padded 3x4)
-  std::vector<uint4> tri_attr;
-  std::vector<float> normals, uvs;
-  std::vector<GpuLight> lights;
-  GpuMiss miss{};
-  std::vector<float4> env;
-  GpuCamera cam{};
-  bool committed = false;
-  // ---- device scene
-  DevBuf<uint4> d_nodes;
-  DevBuf<float4> d_prims, d_xforms, d_env;
-  DevBuf<GpuMaterial> d_mats;
-  DevBuf<GpuLight> d_lights;
-  DevBuf<uint4> d_tri_attr;
-  DevBuf<float> d_normals, d_uvs;
-  DevBuf<uint32_t> d_leaf_of_id;
-  DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
-  DevBuf<float> d_env_marg, d_env_cond;  // environment sampling CDFs
-  DevBuf<double> d_env_rows;
-  DevBuf<int> d_env_valid;
-  int env_valid = 0;
-  DevScene scene{};
-  int bvh_depth = 0;
-  size_t bvh_nodes = 0;
-  // ---- wavefront state
-  int slots = 0;
-  WaveState W{};
-  DevBuf<float4> d_slot_f4;   // PT_SLOT_F4 float4 arrays of `slots` entries
-  DevBuf<uint4> d_slot_u4;    // PT_SLOT_U4 uint4 arrays
-  DevBuf<WaveCounters> d_ctr;
-  DevBuf<WaveCtl> d_ctl;
-  DevBuf<float4> d_results;
-  DevBuf<float4> d_acc;
-  DevBuf<float> d_tmp;
-  DevBuf<uint32_t> d_tmpu;
-  WaveCounters* h_ctr = nullptr;  // pinned
-  WaveCtl* h_ctl = nullptr;       // pinned
-  cudaGraphExec_t graph = nullptr;
-  bool graph_counters = false;
-  bool graph_timing = false;
-  int graph_mode = 0;
-  std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
-  int max_stack = 0;
-  int trace_grid = 0, shade_grid = 0;
-  pt_stats stats{};
-};
+using namespace pth;
 
 static int fail(pt_context* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -186,7 +100,7 @@ static bool finite3(const float* v) {
   return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
 }
 
-static bool is_device_ptr(const void* p) {
+bool pth::is_device_ptr(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
@@ -263,6 +177,8 @@ PT_API const char* pt_last_error(pt_context* ctx) {
 PT_API int pt_context_create(const pt_options* opt, pt_context** out) {
   if (!out) return PT_EINVAL;
   *out = nullptr;
+  if (opt && (opt->bvh_width != 0 && (opt->bvh_width < 2 || opt->bvh_width > 8)))
+    return PT_EINVAL;
   pt_context* ctx = new (std::nothrow) pt_context();
   if (!ctx) return PT_ENOMEM;
   if (opt) ctx->opt = *opt;
@@ -647,6 +563,75 @@ static void prim_record(const HostPrim& p, uint32_t id, float4* out) {
   out[2] = make_float4(p.f[6], p.f[7], p.f[8], matf);
 }
 
+}  // extern "C"
+
+// Builds the BVH8 of the scene's primitives (transforms already on the
+// device) into nodes / leaf-ordered records / leaf_of_id, with at most
+// `width` children per node, and checks its structure on the host.
+int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<float4>& d_prims,
+                   DevBuf<uint32_t>& d_leaf_of_id, size_t* out_nodes, int* out_depth) {
+  cudaStream_t st = ctx->stream;
+  size_t n = ctx->prims.size();
+  int builder = ctx->opt.bvh_builder;
+  if (builder == 0) builder = n >= 4096 ? 2 : 1;
+  pt::Bvh8Out bvh;
+  size_t nn = 0;
+  if (builder == 2 && n > 0) {
+    // records in call order, built into leaf order on the device
+    std::vector<float4> rec(3 * n);
+    for (size_t i = 0; i < n; i++) prim_record(ctx->prims[i], (uint32_t)i, &rec[3 * i]);
+    CK(ctx->d_rec_in.upload(rec.data(), rec.size(), st));
+    CK(d_nodes.ensure(5 * std::max<size_t>(1, n)));
+    CK(d_prims.ensure(3 * n));
+    CK(d_leaf_of_id.ensure(n));
+    uint32_t nodes = 0;
+    int depth = 0;
+    CK(pt::build_bvh8_gpu(ctx->d_rec_in.p, ctx->d_xforms.p, (uint32_t)n, d_nodes.p,
+                          d_prims.p, d_leaf_of_id.p, &nodes, &depth, 2, width, st));
+    if (depth < 0)
+      return fail(ctx, PT_EINVAL,
+                  "GPU BVH8 failed validation (collapse check " + std::to_string(-depth) + ")");
+    nn = nodes;
+    bvh.depth = depth;
+    // host-side structural check before any traversal runs on it
+    bvh.nodes.resize((size_t)nodes * 20);
+    std::vector<uint32_t> loid(n);
+    CK(cudaMemcpyAsync(bvh.nodes.data(), d_nodes.p, bvh.nodes.size() * 4,
+                       cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(loid.data(), d_leaf_of_id.p, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    bvh.leaf_order.assign(n, 0xffffffffu);
+    for (size_t i = 0; i < n; i++) {
+      if (loid[i] >= n) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
+      bvh.leaf_order[loid[i]] = (uint32_t)i;
+    }
+    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
+  } else {
+    std::vector<pt::Box> boxes(n);
+    for (size_t i = 0; i < n; i++) boxes[i] = prim_box(ctx, ctx->prims[i]);
+    if (n) pt::build_bvh8_host(boxes, bvh, width);
+    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "BVH8 failed validation");
+    // primitive records in leaf order
+    std::vector<float4> rec(3 * (n ? n : 1));
+    for (size_t k = 0; k < bvh.leaf_order.size(); k++)
+      prim_record(ctx->prims[bvh.leaf_order[k]], bvh.leaf_order[k], &rec[3 * k]);
+    nn = bvh.nodes.size() / 20;
+    std::vector<uint4> nodes(nn ? nn * 5 : 5);
+    if (nn) memcpy(nodes.data(), bvh.nodes.data(), bvh.nodes.size() * 4);
+    CK(d_nodes.upload(nodes.data(), nodes.size(), st));
+    CK(d_prims.upload(rec.data(), rec.size(), st));
+    std::vector<uint32_t> leaf_of_id(n ? n : 1, 0);
+    for (size_t k = 0; k < bvh.leaf_order.size(); k++) leaf_of_id[bvh.leaf_order[k]] = (uint32_t)k;
+    CK(d_leaf_of_id.upload(leaf_of_id.data(), leaf_of_id.size(), st));
+  }
+  CK(cudaStreamSynchronize(st));
+  *out_nodes = nn;
+  *out_depth = bvh.depth;
+  return PT_OK;
+}
+
+extern "C" {
+
 PT_API int pt_commit(pt_context* ctx) {
   if (!ctx) return PT_EINVAL;
   CK(cudaSetDevice(ctx->device));
@@ -660,55 +645,11 @@ PT_API int pt_commit(pt_context* ctx) {
   std::vector<float4> xf(ctx->xforms.size() / 4 + 1);
   if (!ctx->xforms.empty()) memcpy(xf.data(), ctx->xforms.data(), ctx->xforms.size() * 4);
   CK(ctx->d_xforms.upload(xf.data(), xf.size(), st));
-  int builder = ctx->opt.bvh_builder;
-  if (builder == 0) builder = n >= 4096 ? 2 : 1;
-  pt::Bvh8Out bvh;
   size_t nn = 0;
-  if (builder == 2 && n > 0) {
-    // records in call order, built into leaf order on the device
-    std::vector<float4> rec(3 * n);
-    for (size_t i = 0; i < n; i++) prim_record(ctx->prims[i], (uint32_t)i, &rec[3 * i]);
-    CK(ctx->d_rec_in.upload(rec.data(), rec.size(), st));
-    CK(ctx->d_nodes.ensure(5 * std::max<size_t>(1, n)));
-    CK(ctx->d_prims.ensure(3 * n));
-    CK(ctx->d_leaf_of_id.ensure(n));
-    uint32_t nodes = 0;
-    int depth = 0;
-    CK(pt::build_bvh8_gpu(ctx->d_rec_in.p, ctx->d_xforms.p, (uint32_t)n, ctx->d_nodes.p,
-                          ctx->d_prims.p, ctx->d_leaf_of_id.p, &nodes, &depth, 2, st));
-    nn = nodes;
-    bvh.depth = depth;
-    // host-side structural check before any traversal runs on it
-    bvh.nodes.resize((size_t)nodes * 20);
-    std::vector<uint32_t> loid(n);
-    CK(cudaMemcpyAsync(bvh.nodes.data(), ctx->d_nodes.p, bvh.nodes.size() * 4,
-                       cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(loid.data(), ctx->d_leaf_of_id.p, n * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    bvh.leaf_order.assign(n, 0xffffffffu);
-    for (size_t i = 0; i < n; i++) {
-      if (loid[i] >= n) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
-      bvh.leaf_order[loid[i]] = (uint32_t)i;
-    }
-    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
-  } else {
-    std::vector<pt::Box> boxes(n);
-    for (size_t i = 0; i < n; i++) boxes[i] = prim_box(ctx, ctx->prims[i]);
-    if (n) pt::build_bvh8_host(boxes, bvh);
-    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "BVH8 failed validation");
-    // primitive records in leaf order
-    std::vector<float4> rec(3 * (n ? n : 1));
-    for (size_t k = 0; k < bvh.leaf_order.size(); k++)
-      prim_record(ctx->prims[bvh.leaf_order[k]], bvh.leaf_order[k], &rec[3 * k]);
-    nn = bvh.nodes.size() / 20;
-    std::vector<uint4> nodes(nn ? nn * 5 : 5);
-    if (nn) memcpy(nodes.data(), bvh.nodes.data(), bvh.nodes.size() * 4);
-    CK(ctx->d_nodes.upload(nodes.data(), nodes.size(), st));
-    CK(ctx->d_prims.upload(rec.data(), rec.size(), st));
-    std::vector<uint32_t> leaf_of_id(n ? n : 1, 0);
-    for (size_t k = 0; k < bvh.leaf_order.size(); k++) leaf_of_id[bvh.leaf_order[k]] = (uint32_t)k;
-    CK(ctx->d_leaf_of_id.upload(leaf_of_id.data(), leaf_of_id.size(), st));
-  }
+  int depth = 0;
+  int width = ctx->opt.bvh_width ? ctx->opt.bvh_width : 8;
+  int rc = build_bvh(ctx, width, ctx->d_nodes, ctx->d_prims, ctx->d_leaf_of_id, &nn, &depth);
+  if (rc) return rc;
   std::vector<GpuMaterial> mats = ctx->mats;
   if (mats.empty()) mats.resize(1);
   CK(ctx->d_mats.upload(mats.data(), mats.size(), st));
@@ -760,26 +701,29 @@ PT_API int pt_commit(pt_context* ctx) {
   S.env_marg = ctx->d_env_marg.p;
   S.env_cond = ctx->d_env_cond.p;
   S.env_valid = ctx->env_valid;
-  ctx->bvh_depth = bvh.depth;
+  ctx->bvh_depth = depth;
   ctx->bvh_nodes = nn;
-  ctx->max_stack = std::max(1, bvh.depth + 1);
-  if (pt::trace_smem(ctx->max_stack) > 200 * 1024)
+  ctx->bvh_width = width;
+  ctx->max_stack = std::max(1, depth + 1);
+  if (pt::trace_smem(ctx->max_stack, PT_TRACE_BLOCK) > 200 * 1024)
     return fail(ctx, PT_EINVAL, "BVH too deep for the traversal stack");
-  CK(pt::set_trace_smem(ctx->max_stack));
-  ctx->trace_grid = pt::wave_grid(0, ctx->max_stack);
-  ctx->shade_grid = pt::wave_grid(1, ctx->max_stack);
+  CK(pt::set_trace_smem());
+  ctx->lc = pt::default_launch(ctx->max_stack);
   auto t1 = std::chrono::steady_clock::now();
   ctx->stats.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   ctx->stats.bvh_nodes = nn;
   ctx->stats.bvh_bytes = nn * 80 + n * 48;
-  ctx->stats.bvh_depth = bvh.depth;
+  ctx->stats.bvh_depth = depth;
+  ctx->commit_gen++;
   ctx->committed = true;
   return PT_OK;
 }
 
+}  // extern "C"
+
 // ------------------------------------------------------------------- render
 // Carves the wavefront arrays out of one float4 block and one uint4 block.
-static void carve_wave(WaveState& W, float4* f, uint4* u, size_t s) {
+void pth::carve_wave(WaveState& W, float4* f, uint4* u, size_t s) {
   for (int k = 0; k < 2; k++) {
     PathBuf& b = W.path[k];
     b.ray_o = f + (4 * k + 0) * s;
@@ -799,6 +743,8 @@ static void carve_wave(WaveState& W, float4* f, uint4* u, size_t s) {
   W.sh.st = u + 2 * s;
   W.slots = (int)s;
 }
+
+extern "C" {
 
 static int ensure_wave(pt_context* ctx, size_t results_needed) {
   int slots = ctx->opt.path_slots > 0 ? ctx->opt.path_slots : (1 << 21);
@@ -861,9 +807,8 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < kItersPerGraph; i++)
-      pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters,
-                           ctx->trace_grid, ctx->shade_grid, st,
-                           timing ? &ctx->tev[6 * i] : nullptr, p->mode);
+      pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters, ctx->lc,
+                           st, timing ? &ctx->tev[6 * i] : nullptr, p->mode, nullptr, false, 0);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
     cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
@@ -880,6 +825,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   unsigned long long iters = 0;
   while (true) {
     CK(cudaGraphLaunch(ctx->graph, st));
+    ctx->stats.graph_launches++;
     iters += kItersPerGraph;
     CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr.p, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -911,12 +857,14 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
 static void reset_render_stats(pt_context* ctx) {
   pt_stats& s = ctx->stats;
   s.paths = s.ext_rays = s.shadow_rays = s.node_fetches = s.prim_tests = 0;
-  s.iterations = s.kernel_launches = 0;
+  s.iterations = s.kernel_launches = s.graph_launches = 0;
   for (double& x : s.stage_ms) x = 0.0;
   s.render_ms = 0.0;
 }
 
-static int check_params(pt_context* ctx, const pt_render_params* p) {
+}  // extern "C"
+
+int pth::check_params(pt_context* ctx, const pt_render_params* p) {
   if (!p) return fail(ctx, PT_EINVAL, "null params");
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->frame0 < 0 || p->max_depth <= 0 ||
       p->max_depth > 65535)
@@ -929,6 +877,8 @@ static int check_params(pt_context* ctx, const pt_render_params* p) {
   if (!ctx->committed) return fail(ctx, PT_ESTATE, "scene not committed (call pt_commit)");
   return PT_OK;
 }
+
+extern "C" {
 
 // Render into a device accumulator.
 static int render_device(pt_context* ctx, const pt_render_params* p, float4* d_acc) {
@@ -1185,8 +1135,8 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
     unsigned long long iters = 0;
     while (true) {
       for (int i = 0; i < kItersPerGraph; i++)
-        pt::launch_iteration(ctx->scene, W, d_ctl, ctx->max_stack, false, ctx->trace_grid,
-                             ctx->shade_grid, st, nullptr, p->mode);
+        pt::launch_iteration(ctx->scene, W, d_ctl, ctx->max_stack, false, ctx->lc, st, nullptr,
+                             p->mode, nullptr, false, 0);
       CK(cudaGetLastError());
       iters += kItersPerGraph;
       ctx->stats.iterations += kItersPerGraph;

@@ -1,0 +1,125 @@
+/*
+ * pt_context.h - host-side state of a scene context, shared by the single
+ * scene API (pt_api.cu) and batched rendering (pt_batch.cu).
+ */
+#ifndef PT_CONTEXT_H
+#define PT_CONTEXT_H
+
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "../../include/pt.h"
+#include "pt_internal.h"
+
+namespace pth {
+
+struct HostPrim {
+  int type, axis, flip, xform;
+  uint32_t material;
+  float f[9];
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const T* h, size_t count, cudaStream_t st) {
+    cudaError_t e = ensure(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace pth
+
+using pth::DevBuf;
+using pth::HostPrim;
+
+struct pt_context {
+  int device = 0;
+  std::string err;
+  pt_options opt{};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // ---- host scene
+  std::vector<GpuMaterial> mats;
+  std::vector<HostPrim> prims;
+  std::vector<float> xforms;  // 24 floats each: m rows, inv rows (float4-padded 3x4)
+  std::vector<uint4> tri_attr;
+  std::vector<float> normals, uvs;
+  std::vector<GpuLight> lights;
+  GpuMiss miss{};
+  std::vector<float4> env;
+  GpuCamera cam{};
+  bool committed = false;
+  // ---- device scene
+  DevBuf<uint4> d_nodes;
+  DevBuf<float4> d_prims, d_xforms, d_env;
+  DevBuf<GpuMaterial> d_mats;
+  DevBuf<GpuLight> d_lights;
+  DevBuf<uint4> d_tri_attr;
+  DevBuf<float> d_normals, d_uvs;
+  DevBuf<uint32_t> d_leaf_of_id;
+  DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
+  DevBuf<float> d_env_marg, d_env_cond;  // environment sampling CDFs
+  DevBuf<double> d_env_rows;
+  DevBuf<int> d_env_valid;
+  int env_valid = 0;
+  DevScene scene{};
+  int bvh_depth = 0;
+  size_t bvh_nodes = 0;
+  int bvh_width = 8;          // node width the committed BVH was built with
+  uint64_t commit_gen = 0;    // increases with every pt_commit
+  // ---- wavefront state
+  int slots = 0;
+  WaveState W{};
+  DevBuf<float4> d_slot_f4;   // PT_SLOT_F4 float4 arrays of `slots` entries
+  DevBuf<uint4> d_slot_u4;    // PT_SLOT_U4 uint4 arrays
+  DevBuf<WaveCounters> d_ctr;
+  DevBuf<WaveCtl> d_ctl;
+  DevBuf<float4> d_results;
+  DevBuf<float4> d_acc;
+  DevBuf<float> d_tmp;
+  DevBuf<uint32_t> d_tmpu;
+  WaveCounters* h_ctr = nullptr;  // pinned
+  WaveCtl* h_ctl = nullptr;       // pinned
+  cudaGraphExec_t graph = nullptr;
+  bool graph_counters = false;
+  bool graph_timing = false;
+  int graph_mode = 0;
+  std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
+  int max_stack = 0;
+  LaunchCfg lc{};
+  pt_stats stats{};
+};
+
+
+namespace pth {
+/* Builds the scene's BVH (at most `width` children per node) into the given
+ * buffers; returns a PT_ status. */
+int build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<float4>& d_prims,
+              DevBuf<uint32_t>& d_leaf_of_id, size_t* out_nodes, int* out_depth);
+/* Carves the wavefront arrays of `slots` paths out of one float4 block
+ * (PT_SLOT_F4 per slot) and one uint4 block (PT_SLOT_U4 per slot). */
+void carve_wave(WaveState& W, float4* f, uint4* u, size_t slots);
+bool is_device_ptr(const void* p);
+/* Render parameters valid for the context (sets ctx->err otherwise). */
+int check_params(pt_context* ctx, const pt_render_params* p);
+}  // namespace pth
+
+#endif

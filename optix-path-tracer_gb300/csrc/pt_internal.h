@@ -9,11 +9,26 @@
 #include <stdint.h>
 #include "pt_types.h"
 
-#define PT_TRACE_BLOCK 128
+#define PT_TRACE_BLOCK 128       /* default threads per trace block */
+#define PT_TRACE_MAXTHREADS 256  /* largest trace block the kernels are compiled for */
 #ifndef PT_TRACE_MINBLOCKS
-#define PT_TRACE_MINBLOCKS 6  /* <= 80 registers per thread, no spills */
+#define PT_TRACE_MINBLOCKS 3     /* of 256 threads: <= 80 registers per thread, no spills */
 #endif
-#define PT_SHADE_BLOCK 256
+#define PT_SHADE_BLOCK 256       /* default and largest shade block */
+
+/* Path state word st.z: depth (bits 0-15), previous bounce specular (bit 16),
+ * scene of a batch (bits 17-31). */
+#define PT_ST_DEPTH_MASK 0xffffu
+#define PT_ST_SPEC_BIT 16
+#define PT_ST_SCENE_SHIFT 17
+#define PT_ST_KEEP_MASK 0xfffe0000u
+#define PT_MAX_BATCH_SCENES 32767
+
+/* Launch shape of the stage kernels. */
+struct LaunchCfg {
+  int trace_block, trace_grid;
+  int shade_block, shade_grid;
+};
 
 struct Ray3 {
   float3 o, d;
@@ -25,11 +40,14 @@ struct WaveCounters {
   uint32_t n_next;       /* paths written to the next buffer */
   uint32_t n_shadow;     /* paths parked at a shadow ray this iteration */
   uint32_t parity;       /* which path buffer is current */
-  uint32_t error;        /* bit 0: traversal stack overflow */
-  uint32_t iter;
+  uint32_t error;        /* bit 0: traversal stack overflow, bit 1: iteration bound reached */
+  uint32_t iter;         /* iterations of the current chunk */
   unsigned long long next_path;   /* next path id of the chunk to generate */
   unsigned long long ext_rays, shadow_rays;
   unsigned long long node_fetches, prim_tests;
+  unsigned long long iters_total; /* iterations over all chunks (batch) */
+  uint32_t chunk;        /* current chunk of a batch */
+  uint32_t n_chunks;     /* chunks of the batch (set by the host) */
 };
 
 /* Per-chunk render controls, in device memory (kernels read them, so one
@@ -40,6 +58,41 @@ struct WaveCtl {
   int max_depth, rr_enable, rr_depth, mode, guide;
   unsigned long long chunk_paths; /* paths in this chunk */
   uint32_t wh_m, wh_l, w_m, w_l;  /* invariant-divisor constants for W*H and W */
+  /* batch: segments [seg_begin, seg_end) make up this chunk, `pixels` pixels */
+  uint32_t seg_begin, seg_end, pixels, pad;
+  unsigned long long max_iter;    /* device-side iteration bound of this chunk */
+};
+
+/* ---- batched multi-scene rendering ---------------------------------------
+ * Every scene of a batch is copied into one set of geometry arrays (nodes,
+ * records, transforms, materials, attributes) with its indices shifted, so
+ * traversal needs only a per-ray root node.  Camera, miss program, lights
+ * and environment tables stay per scene. */
+struct BatchScene {
+  DevScene S;          /* geometry pointers: the batch arrays; the rest: this scene's */
+  int width, height, max_depth, rr_enable, rr_depth, pad;
+  uint32_t wh_m, wh_l, w_m, w_l;
+};
+
+/* Consecutive frames of one scene inside a chunk. */
+struct BatchSeg {
+  uint32_t path_off;   /* first path of the segment, chunk-relative */
+  uint32_t pix_off;    /* first pixel of the segment among the chunk's pixels */
+  uint32_t scene;      /* index into the BatchScene table */
+  uint32_t frame0, frames, pad;
+  float4* acc;         /* device accumulator of the scene */
+};
+
+struct BatchChunk {
+  unsigned long long paths, max_iter;
+  uint32_t seg_begin, seg_end, pixels, pad;
+};
+
+/* Kernel-parameter view of a batch (null pointers for a single scene). */
+struct BatchRefs {
+  const BatchScene* scenes;
+  const BatchSeg* segs;
+  const uint32_t* roots;     /* root node per scene */
 };
 
 /* Unsigned division by an invariant 32-bit divisor d >= 1 (Granlund &
@@ -93,14 +146,36 @@ struct WaveState {
 #define PT_SLOT_U4 3
 
 namespace pt {
-size_t trace_smem(int max_stack);
-int wave_grid(int kind, int max_stack);
-cudaError_t set_trace_smem(int max_stack);
+size_t trace_smem(int max_stack, int block);
+/* Resident blocks per SM x SMs for a trace (kind 0) or shade (kind 1)
+ * kernel of `block` threads. */
+int wave_grid(int kind, int max_stack, int block);
+/* Raises the dynamic shared memory limit of the trace kernels to the
+ * device maximum (once per device). */
+cudaError_t set_trace_smem();
+/* Default launch shape for a BVH of the given stack depth. */
+LaunchCfg default_launch(int max_stack);
 /* One wavefront iteration (7 kernels).  ev, if not null, holds 6 events
- * recorded between the stages. */
+ * recorded between the stages.  br: batch tables, or null for one scene.
+ * use_cond: the queue-advance kernel sets graph conditional `cond` to
+ * whether the chunk has work left (device-side iteration loop). */
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
-                      bool counters, int trace_grid, int shade_grid, cudaStream_t st,
-                      cudaEvent_t* ev, int mode);
+                      bool counters, const LaunchCfg& lc, cudaStream_t st, cudaEvent_t* ev,
+                      int mode, const BatchRefs* br, bool use_cond,
+                      unsigned long long cond);
+/* Batch chunk boundaries: begin loads chunk c.chunk into *ctl and resets the
+ * queues (and sets conditional `inner` to 1); end accumulates the chunk's
+ * results into the scenes' accumulators, moves to the next chunk and sets
+ * conditional `outer` to whether one is left. */
+void launch_batch_begin(const WaveState& W, WaveCtl* ctl, const BatchChunk* chunks,
+                        bool use_cond, unsigned long long inner, cudaStream_t st);
+void launch_batch_end(const WaveState& W, const WaveCtl* ctl, const BatchRefs& br,
+                      bool use_cond, unsigned long long outer, cudaStream_t st);
+/* Adds offsets to the indices of one scene copied into the batch arrays. */
+void launch_relocate(uint4* nodes, size_t n_nodes, uint32_t node_off, uint32_t prim_off,
+                     float4* prims, size_t n_prims, uint32_t xform_off, uint32_t id_off,
+                     uint32_t mat_off, uint32_t* leaf_of_id, uint4* tri_attr, uint32_t attr_off,
+                     cudaStream_t st);
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,
                     int* valid, cudaStream_t st);
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,

@@ -126,21 +126,23 @@ struct FirstHitOut {
 
 enum { TRACE_EXT = 0, TRACE_SHADOW = 1, TRACE_FIRST = 2 };
 
-size_t trace_smem_bytes(int max_stack) {
-  return (size_t)(PT_TRACE_BLOCK / 32) * sizeof(WarpShared) +
-         (size_t)PT_TRACE_BLOCK * max_stack * (sizeof(uint2) + sizeof(float));
+size_t trace_smem_bytes(int max_stack, int block) {
+  return (size_t)(block / 32) * sizeof(WarpShared) +
+         (size_t)block * max_stack * (sizeof(uint2) + sizeof(float));
 }
 
-template <int MODE, bool COUNT>
-__global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
+// BATCH: rays of several scenes; each starts at its scene's root node (the
+// scene index is in the path state word st.z).
+template <int MODE, bool COUNT, bool BATCH>
+__global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     k_trace_t(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp, int max_stack,
-              FirstHitOut fo) {
+              FirstHitOut fo, BatchRefs br) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   WarpShared& ws = ((WarpShared*)smem)[threadIdx.x >> 5];
-  uint2* stk = (uint2*)(smem + (PT_TRACE_BLOCK / 32) * sizeof(WarpShared)) + threadIdx.x;
-  float* stkt = (float*)((uint2*)(smem + (PT_TRACE_BLOCK / 32) * sizeof(WarpShared)) +
-                         (size_t)max_stack * blockDim.x) + threadIdx.x;
+  unsigned char* stk_base = smem + (blockDim.x >> 5) * sizeof(WarpShared);
+  uint2* stk = (uint2*)stk_base + threadIdx.x;
+  float* stkt = (float*)((uint2*)stk_base + (size_t)max_stack * blockDim.x) + threadIdx.x;
   const int bd = blockDim.x;
 
   uint32_t n;
@@ -222,7 +224,11 @@ __global__ void __launch_bounds__(PT_TRACE_BLOCK, PT_TRACE_MINBLOCKS)
     tbest = tmax;
     best_id = PT_NO_HIT;
     ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
-    cur = 0;
+    cur = S.root;
+    if (BATCH) {
+      uint32_t z = MODE == TRACE_EXT ? W.path[c.parity].st[i].z : W.sh.st[i].z;
+      cur = __ldg(br.roots + (z >> PT_ST_SCENE_SHIFT));
+    }
     sp = 0;
   };
 
@@ -484,7 +490,14 @@ __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool active) {
 }
 
 // ---------------------------------------------------------- path state ----
-// st.x = seed, st.y = path id in the chunk, st.z = depth | prevSpecular<<16
+// st.x = seed, st.y = path id in the chunk, st.z = depth | prevSpecular<<16 |
+// scene<<17 (batch), st.w = pdf of the last BSDF sample (consistent mode)
+
+// Depth limit and Russian roulette of a path (per render, or per scene of a
+// batch).
+struct PathCtl {
+  int max_depth, rr_enable, rr_depth;
+};
 __device__ __forceinline__ void finalize_path(const WaveState& W, uint32_t pid, V3 col) {
   // de_nan, programs/raygen.cu:126-134
   if (!(col.x == col.x)) col.x = 0.f;
@@ -504,12 +517,12 @@ struct Tail {
 // Ends the path or appends it, compacted, to the next path buffer.  All
 // lanes of the warp call it (the append is a warp-aggregated atomic).
 __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters& c,
-                                          const WaveCtl& ctl, uint4 st, V3 thr, V3 rad,
+                                          const PathCtl& ctl, uint4 st, V3 thr, V3 rad,
                                           const Tail& tl, bool active) {
   bool cont = false;
   if (active) {
-    uint32_t depth = st.z & 0xffffu;
-    bool prevSpec = (st.z >> 16) & 1u;
+    uint32_t depth = st.z & PT_ST_DEPTH_MASK;
+    bool prevSpec = (st.z >> PT_ST_SPEC_BIT) & 1u;
     bool done = false;
     V3 col = v3(0.f);
     if (tl.event == 2) {
@@ -539,7 +552,7 @@ __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters
           done = true;
         } else {
           cont = true;
-          st.z = depth | ((uint32_t)prevSpec << 16);
+          st.z = (st.z & PT_ST_KEEP_MASK) | depth | ((uint32_t)prevSpec << PT_ST_SPEC_BIT);
         }
       }
     }
@@ -557,22 +570,57 @@ __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters
 }
 
 // ------------------------------------------------------------- kernels ----
-__global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp) {
+// Segment of a batch chunk that holds path `pid` (binary search over the
+// segments' first paths).
+__device__ __forceinline__ uint32_t find_seg(const BatchSeg* __restrict__ segs, uint32_t lo,
+                                             uint32_t hi, uint32_t pid, bool by_pixel) {
+  // invariant: segs[lo].off <= pid, answer in [lo, hi)
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    uint32_t off = by_pixel ? segs[mid].pix_off : segs[mid].path_off;
+    if (off <= pid) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <bool BATCH>
+__global__ void k_generate(DevScene S0, WaveState W, const WaveCtl* __restrict__ ctlp,
+                           BatchRefs br) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = gen_count(c, ctl, (uint32_t)W.slots);
-  uint32_t WH = (uint32_t)ctl.width * (uint32_t)ctl.height;
   const PathBuf& pb = W.path[c.parity];
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     uint32_t pos = c.n_cur + j;
     uint32_t pid = (uint32_t)(c.next_path + j);
-    uint32_t fr = fastdiv(pid, ctl.wh_m, ctl.wh_l);
-    uint32_t frame = (uint32_t)ctl.frame0 + fr;
-    uint32_t pix = pid - fr * WH;
-    uint32_t y = fastdiv(pix, ctl.w_m, ctl.w_l);
-    uint32_t x = pix - y * (uint32_t)ctl.width;
-    uint32_t seed = tea64((uint32_t)ctl.width * y + x, frame);
-    Ray3 r = camera_ray(S.cam, x, y, ctl.width, ctl.height, seed);
+    uint32_t width = (uint32_t)ctl.width, height = (uint32_t)ctl.height;
+    uint32_t wh_m = ctl.wh_m, wh_l = ctl.wh_l, w_m = ctl.w_m, w_l = ctl.w_l;
+    uint32_t frame0 = (uint32_t)ctl.frame0, local = pid, scene = 0;
+    const DevScene* Sp = &S0;
+    if (BATCH) {
+      const BatchSeg& sg = br.segs[find_seg(br.segs, ctl.seg_begin, ctl.seg_end, pid, false)];
+      scene = sg.scene;
+      const BatchScene& B = br.scenes[scene];
+      Sp = &B.S;
+      width = (uint32_t)B.width;
+      height = (uint32_t)B.height;
+      wh_m = B.wh_m;
+      wh_l = B.wh_l;
+      w_m = B.w_m;
+      w_l = B.w_l;
+      frame0 = sg.frame0;
+      local = pid - sg.path_off;
+    }
+    const DevScene& S = *Sp;
+    uint32_t WH = width * height;
+    uint32_t fr = fastdiv(local, wh_m, wh_l);
+    uint32_t frame = frame0 + fr;
+    uint32_t pix = local - fr * WH;
+    uint32_t y = fastdiv(pix, w_m, w_l);
+    uint32_t x = pix - y * width;
+    uint32_t seed = tea64(width * y + x, frame);
+    Ray3 r = camera_ray(S.cam, x, y, width, height, seed);
     // color(): prd.time draw, programs/raygen.cu:69
     float tm = S.cam.time0 + rnd(seed) * (S.cam.time1 - S.cam.time0);
     (void)tm;
@@ -580,8 +628,31 @@ __global__ void k_generate(DevScene S, WaveState W, const WaveCtl* __restrict__ 
     pb.ray_d[pos] = make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX);
     pb.thr[pos] = make_float4(1.f, 1.f, 1.f, 0.f);
     pb.rad[pos] = make_float4(0.f, 0.f, 0.f, 0.f);
-    pb.st[pos] = make_uint4(seed, pid, 0u, 0u);
+    pb.st[pos] = make_uint4(seed, pid, scene << PT_ST_SCENE_SHIFT, 0u);
   }
+}
+
+// Scene and path controls of a path: the render's, or its batch scene's.
+template <bool BATCH>
+__device__ __forceinline__ const DevScene& path_scene(const DevScene& S0, const BatchRefs& br,
+                                                      uint32_t stz) {
+  return BATCH ? br.scenes[stz >> PT_ST_SCENE_SHIFT].S : S0;
+}
+template <bool BATCH>
+__device__ __forceinline__ PathCtl path_ctl(const WaveCtl& ctl, const BatchRefs& br,
+                                            uint32_t stz) {
+  PathCtl pc;
+  if (BATCH) {
+    const BatchScene& B = br.scenes[stz >> PT_ST_SCENE_SHIFT];
+    pc.max_depth = B.max_depth;
+    pc.rr_enable = B.rr_enable;
+    pc.rr_depth = B.rr_depth;
+  } else {
+    pc.max_depth = ctl.max_depth;
+    pc.rr_enable = ctl.rr_enable;
+    pc.rr_depth = ctl.rr_depth;
+  }
+  return pc;
 }
 
 // Direct_Light (programs/materials/light_sample.cuh:36-73) up to the shadow
@@ -698,8 +769,10 @@ __device__ __forceinline__ V3 miss_color(const GpuMiss& ms, V3 d) {
   return 2.f * env_lookup(ms, u, v);
 }
 
-__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState W,
-                                                          const WaveCtl* __restrict__ ctlp) {
+template <bool BATCH>
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S0, WaveState W,
+                                                          const WaveCtl* __restrict__ ctlp,
+                                                          BatchRefs br) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
@@ -721,8 +794,9 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
     float lightPDF = 0.f;
     int lindex = 0;
     uint32_t mid = 0;
+    if (active) st = pb.st[i];
+    const DevScene& S = path_scene<BATCH>(S0, br, st.z);
     if (active) {
-      st = pb.st[i];
       float4 t4 = pb.thr[i], r4 = pb.rad[i];
       thr = f4xyz(t4);
       rad = f4xyz(r4);
@@ -830,12 +904,14 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S, WaveState 
       W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
     }
     if (missed) finalize_path(W, st.y, col);  // misses end here
-    path_tail(W, c, ctl, st, thr, rad, tl, tail);
+    path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, tail);
   }
 }
 
-__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState W,
-                                                           const WaveCtl* __restrict__ ctlp) {
+template <bool BATCH>
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S0, WaveState W,
+                                                           const WaveCtl* __restrict__ ctlp,
+                                                           BatchRefs br) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_shadow;
@@ -849,8 +925,9 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState
     Tail tl;
     tl.event = 1;
     tl.isSpecular = false;
+    if (active) st = W.sh.st[i];
+    const DevScene& S = path_scene<BATCH>(S0, br, st.z);
     if (active) {
-      st = W.sh.st[i];
       thr = f4xyz(W.sh.thr[i]);
       rad = f4xyz(W.sh.rad[i]);
       float4 P4 = W.sh.P[i], N4 = W.sh.N[i], Wo4 = W.sh.Wo[i], Wi4 = W.sh.Wi[i];
@@ -860,7 +937,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S, WaveState
                           Wi4.w != 0.f);
       after_nee(m, st.x, P, Wo, N, direct, thr, rad, tl);
     }
-    path_tail(W, c, ctl, st, thr, rad, tl, active);
+    path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, active);
   }
 }
 
@@ -891,13 +968,14 @@ __device__ __forceinline__ void path_push(const WaveState& W, const WaveCounters
 // with MIS at hits and misses, NEE over lights + environment, BSDF
 // continuation, Russian roulette.  The NEE term waits for its shadow ray in
 // the shadow buffer together with the already-sampled continuation.
-__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S, WaveState W,
-                                                            const WaveCtl* __restrict__ ctlp) {
+template <bool BATCH>
+__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S0, WaveState W,
+                                                            const WaveCtl* __restrict__ ctlp,
+                                                            BatchRefs br) {
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
   const PathBuf& pb = W.path[c.parity];
-  const int n_sel = S.num_lights + (S.env_valid ? 1 : 0);
   uint32_t stride = gridDim.x * blockDim.x;
   uint32_t iters = (n + stride - 1) / stride;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -907,16 +985,19 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S, WaveStat
     V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), Wi = v3(0.f), dcont = v3(0.f), C = v3(0.f);
     float tmax = 0.f;
     bool ended = false, shadow = false;
+    if (active) st = pb.st[i];
+    const DevScene& S = path_scene<BATCH>(S0, br, st.z);
+    const int n_sel = S.num_lights + (S.env_valid ? 1 : 0);
     if (active) {
-      st = pb.st[i];
+      const PathCtl pc = path_ctl<BATCH>(ctl, br, st.z);
       thr = f4xyz(pb.thr[i]);
       rad = f4xyz(pb.rad[i]);
       float4 hit = W.hit[i];
       float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
       V3 d = f4xyz(rdv);
-      uint32_t depth = st.z & 0xffffu;
+      uint32_t depth = st.z & PT_ST_DEPTH_MASK;
       // a camera ray counts as a specular bounce: emission it sees is not MIS-weighted
-      bool prev_spec = ((st.z >> 16) & 1u) || depth == 0;
+      bool prev_spec = ((st.z >> PT_ST_SPEC_BIT) & 1u) || depth == 0;
       float pdf_prev = __uint_as_float(st.w);
       uint32_t leaf = __float_as_uint(hit.w);
       if (leaf == PT_NO_HIT) {
@@ -1021,17 +1102,17 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S, WaveStat
           }
         }
         if (!ended) {
-          if (ctl.rr_enable && (int)depth > ctl.rr_depth) {
+          if (pc.rr_enable && (int)depth > pc.rr_depth) {
             float q = fminf(1.f, max_component(thr));
             if (rnd(st.x) >= q) ended = true;
             else thr *= 1.f / q;
           }
           if (!ended) {
             depth++;
-            if ((int)depth >= ctl.max_depth) ended = true;
+            if ((int)depth >= pc.max_depth) ended = true;
           }
         }
-        st.z = depth | ((uint32_t)prev_spec << 16);
+        st.z = (st.z & PT_ST_KEEP_MASK) | depth | ((uint32_t)prev_spec << PT_ST_SPEC_BIT);
         st.w = __float_as_uint(pdf_prev);
       }
     }
@@ -1079,9 +1160,16 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveSta
   }
 }
 
-__global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp) {
+// Queue bookkeeping after an iteration.  With use_cond (the iteration loop
+// is a graph conditional node) it also decides whether the loop goes on:
+// not once the chunk has drained, an error was flagged, or the chunk's
+// iteration bound is reached (then error bit 1 is set, so the loop always
+// ends).
+__global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp, int use_cond,
+                          cudaGraphConditionalHandle cond) {
   WaveCounters& c = *W.ctr;
-  uint32_t n_gen = gen_count(c, *ctlp, (uint32_t)W.slots);
+  const WaveCtl& ctl = *ctlp;
+  uint32_t n_gen = gen_count(c, ctl, (uint32_t)W.slots);
   c.ext_rays += c.n_cur + n_gen;
   c.shadow_rays += c.n_shadow;
   c.next_path += n_gen;
@@ -1090,6 +1178,106 @@ __global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp) {
   c.n_shadow = 0;
   c.parity ^= 1u;
   c.iter++;
+  c.iters_total++;
+  if (use_cond) {
+    bool more = c.n_cur != 0 || c.next_path < ctl.chunk_paths;
+    if (more && (unsigned long long)c.iter >= ctl.max_iter) c.error |= 2u;
+    if (c.error) more = false;
+    cudaGraphSetConditional(cond, more ? 1u : 0u);
+  }
+}
+
+// ------------------------------------------------------ batch chunk steps --
+__global__ void k_batch_begin(WaveState W, WaveCtl* ctl, const BatchChunk* __restrict__ chunks,
+                              int use_cond, cudaGraphConditionalHandle inner) {
+  WaveCounters& c = *W.ctr;
+  BatchChunk ch{};
+  if (c.chunk < c.n_chunks) ch = chunks[c.chunk];
+  else c.error |= 2u;  // no chunk left: run nothing
+  ctl->chunk_paths = ch.paths;
+  ctl->max_iter = ch.max_iter;
+  ctl->seg_begin = ch.seg_begin;
+  ctl->seg_end = ch.seg_end;
+  ctl->pixels = ch.pixels;
+  c.n_cur = 0;
+  c.n_next = 0;
+  c.n_shadow = 0;
+  c.parity = 0;
+  c.iter = 0;
+  c.next_path = 0;
+  if (use_cond) cudaGraphSetConditional(inner, c.error ? 0u : 1u);
+}
+
+// acc[x, H-1-y] += (col, 1) in frame order for every pixel of every segment
+// of the chunk (the batch form of k_accumulate).
+__global__ void k_accumulate_batch(const float4* __restrict__ results, const WaveCtl* __restrict__ ctlp,
+                                   BatchRefs br) {
+  const WaveCtl ctl = *ctlp;
+  if (ctl.seg_end <= ctl.seg_begin) return;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ctl.pixels;
+       g += gridDim.x * blockDim.x) {
+    const BatchSeg& sg = br.segs[find_seg(br.segs, ctl.seg_begin, ctl.seg_end, g, true)];
+    const BatchScene& B = br.scenes[sg.scene];
+    uint32_t w = (uint32_t)B.width, h = (uint32_t)B.height, WH = w * h;
+    uint32_t p = g - sg.pix_off;
+    uint32_t y = fastdiv(p, B.w_m, B.w_l), x = p - y * w;
+    size_t o = (size_t)(h - 1 - y) * w + x;
+    float4 a = sg.acc[o];
+    for (uint32_t f = 0; f < sg.frames; f++) {
+      float4 r = results[(size_t)sg.path_off + (size_t)f * WH + p];
+      a.x += r.x;
+      a.y += r.y;
+      a.z += r.z;
+      a.w += 1.f;
+    }
+    sg.acc[o] = a;
+  }
+}
+
+__global__ void k_batch_end(WaveState W, int use_cond, cudaGraphConditionalHandle outer) {
+  WaveCounters& c = *W.ctr;
+  c.chunk++;
+  if (use_cond) cudaGraphSetConditional(outer, (c.chunk < c.n_chunks && !c.error) ? 1u : 0u);
+}
+
+// ------------------------------------------------ batch scene relocation --
+__global__ void k_relocate_nodes(uint4* nodes, size_t n, uint32_t node_off, uint32_t prim_off) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    uint4 w = nodes[5 * i + 1];
+    w.x += node_off;
+    w.y += prim_off;
+    nodes[5 * i + 1] = w;
+  }
+}
+
+__global__ void k_relocate_prims(float4* prims, size_t n, uint32_t xform_off, uint32_t id_off,
+                                 uint32_t mat_off) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float4 r0 = prims[3 * i], r1 = prims[3 * i + 1], r2 = prims[3 * i + 2];
+    uint32_t tag = __float_as_uint(r0.w);
+    if (tag >> 8) tag += xform_off << 8;  // transform index + 1 (0: world space)
+    r0.w = __uint_as_float(tag);
+    r1.w = __uint_as_float(__float_as_uint(r1.w) + id_off);
+    r2.w = __uint_as_float(__float_as_uint(r2.w) + mat_off);
+    prims[3 * i] = r0;
+    prims[3 * i + 1] = r1;
+    prims[3 * i + 2] = r2;
+  }
+}
+
+__global__ void k_relocate_ids(uint32_t* leaf_of_id, uint4* tri_attr, size_t n, uint32_t prim_off,
+                               uint32_t attr_off) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    leaf_of_id[i] += prim_off;
+    uint4 a = tri_attr[i];
+    a.x += attr_off;
+    a.y += attr_off;
+    a.z += attr_off;
+    tri_attr[i] = a;
+  }
 }
 
 // acc[x, H-1-y] += (col, 1) in frame order (programs/raygen.cu:153-166)
@@ -1194,65 +1382,135 @@ static int num_sms() {
   return g_num_sms;
 }
 
-size_t trace_smem(int max_stack) { return trace_smem_bytes(max_stack); }
+size_t trace_smem(int max_stack, int block) { return trace_smem_bytes(max_stack, block); }
 
-int wave_grid(int kind, int max_stack) {
+int wave_grid(int kind, int max_stack, int block) {
   int blocks = 0;
   cudaError_t e = cudaSuccess;
   if (kind == 0)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace_t<TRACE_EXT, false>,
-                                                      PT_TRACE_BLOCK, trace_smem(max_stack));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace_t<TRACE_EXT, false, false>,
+                                                      block, trace_smem(max_stack, block));
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade, PT_SHADE_BLOCK, 0);
-  if (e != cudaSuccess || blocks < 1) blocks = 1;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false>, block, 0);
+  if (e != cudaSuccess || blocks < 1) {
+    cudaGetLastError();
+    blocks = 1;
+  }
   return blocks * num_sms();
 }
 
-template <typename K>
-static cudaError_t smem_attr(K k, size_t sm) {
-  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+LaunchCfg default_launch(int max_stack) {
+  LaunchCfg lc;
+  lc.trace_block = PT_TRACE_BLOCK;
+  lc.shade_block = PT_SHADE_BLOCK;
+  lc.trace_grid = wave_grid(0, max_stack, lc.trace_block);
+  lc.shade_grid = wave_grid(1, max_stack, lc.shade_block);
+  return lc;
 }
 
-cudaError_t set_trace_smem(int max_stack) {
-  size_t sm = trace_smem(max_stack);
-  cudaError_t e;
-  if ((e = smem_attr(k_trace_t<TRACE_EXT, false>, sm)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_EXT, true>, sm)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false>, sm)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true>, sm)) != cudaSuccess) return e;
-  return smem_attr(k_trace_t<TRACE_FIRST, false>, sm);
+// Dynamic shared memory limit of kernel k: the per-block opt-in maximum
+// minus its static shared memory.
+template <typename K>
+static cudaError_t smem_attr(K k, int optin) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, k);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fa.sharedSizeBytes);
+}
+
+static const int kMaxDev = 64;
+static bool g_smem_set[kMaxDev];
+
+cudaError_t set_trace_smem() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxDev && g_smem_set[dev]) return cudaSuccess;
+  int optin = 0;
+  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
+      cudaSuccess)
+    return e;
+  if ((e = smem_attr(k_trace_t<TRACE_EXT, false, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_EXT, true, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_EXT, false, true>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_EXT, true, true>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false, true>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true, true>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_FIRST, false, false>, optin)) != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxDev) g_smem_set[dev] = true;
+  return cudaSuccess;
+}
+
+template <bool BATCH>
+static void launch_iteration_t(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
+                               int max_stack, bool counters, const LaunchCfg& lc, cudaStream_t st,
+                               cudaEvent_t* ev, int mode, const BatchRefs& br, bool use_cond,
+                               unsigned long long cond) {
+  size_t sm = trace_smem(max_stack, lc.trace_block);
+  FirstHitOut none{};
+  const int tb = lc.trace_block, tg = lc.trace_grid, sb = lc.shade_block, sg = lc.shade_grid;
+  if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
+  k_generate<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
+  if (counters)
+    k_trace_t<TRACE_EXT, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+  else
+    k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+  if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
+  if (mode == 1)
+    k_shade_c<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  else
+    k_shade<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
+  if (counters)
+    k_trace_t<TRACE_SHADOW, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+  else
+    k_trace_t<TRACE_SHADOW, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+  if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
+  if (mode == 1)
+    k_finish_c<<<sg, sb, 0, st>>>(S, W, ctl);
+  else
+    k_finish<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  k_advance<<<1, 1, 0, st>>>(W, ctl, use_cond ? 1 : 0, (cudaGraphConditionalHandle)cond);
+  if (ev) cudaEventRecordWithFlags(ev[5], st, cudaEventRecordExternal);
 }
 
 // One wavefront iteration (7 launches).
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
-                      bool counters, int trace_grid, int shade_grid, cudaStream_t st,
-                      cudaEvent_t* ev, int mode) {
-  size_t sm = trace_smem(max_stack);
-  FirstHitOut none{};
-  if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
-  k_generate<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
-  if (counters)
-    k_trace_t<TRACE_EXT, true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
+                      bool counters, const LaunchCfg& lc, cudaStream_t st, cudaEvent_t* ev,
+                      int mode, const BatchRefs* br, bool use_cond, unsigned long long cond) {
+  if (br)
+    launch_iteration_t<true>(S, W, ctl, max_stack, counters, lc, st, ev, mode, *br, use_cond, cond);
   else
-    k_trace_t<TRACE_EXT, false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
-  if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
-  if (mode == 1)
-    k_shade_c<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  else
-    k_shade<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
-  if (counters)
-    k_trace_t<TRACE_SHADOW, true><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
-  else
-    k_trace_t<TRACE_SHADOW, false><<<trace_grid, PT_TRACE_BLOCK, sm, st>>>(S, W, ctl, max_stack, none);
-  if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
-  if (mode == 1)
-    k_finish_c<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  else
-    k_finish<<<shade_grid, PT_SHADE_BLOCK, 0, st>>>(S, W, ctl);
-  k_advance<<<1, 1, 0, st>>>(W, ctl);
-  if (ev) cudaEventRecordWithFlags(ev[5], st, cudaEventRecordExternal);
+    launch_iteration_t<false>(S, W, ctl, max_stack, counters, lc, st, ev, mode, BatchRefs{},
+                              use_cond, cond);
+}
+
+void launch_batch_begin(const WaveState& W, WaveCtl* ctl, const BatchChunk* chunks,
+                        bool use_cond, unsigned long long inner, cudaStream_t st) {
+  k_batch_begin<<<1, 1, 0, st>>>(W, ctl, chunks, use_cond ? 1 : 0,
+                                 (cudaGraphConditionalHandle)inner);
+}
+
+void launch_batch_end(const WaveState& W, const WaveCtl* ctl, const BatchRefs& br,
+                      bool use_cond, unsigned long long outer, cudaStream_t st) {
+  k_accumulate_batch<<<num_sms() * 8, 256, 0, st>>>(W.results, ctl, br);
+  k_batch_end<<<1, 1, 0, st>>>(W, use_cond ? 1 : 0, (cudaGraphConditionalHandle)outer);
+}
+
+void launch_relocate(uint4* nodes, size_t n_nodes, uint32_t node_off, uint32_t prim_off,
+                     float4* prims, size_t n_prims, uint32_t xform_off, uint32_t id_off,
+                     uint32_t mat_off, uint32_t* leaf_of_id, uint4* tri_attr, uint32_t attr_off,
+                     cudaStream_t st) {
+  int g = num_sms() * 4;
+  if (n_nodes) k_relocate_nodes<<<g, 256, 0, st>>>(nodes, n_nodes, node_off, prim_off);
+  if (n_prims) {
+    k_relocate_prims<<<g, 256, 0, st>>>(prims, n_prims, xform_off, id_off, mat_off);
+    k_relocate_ids<<<g, 256, 0, st>>>(leaf_of_id, tri_attr, n_prims, prim_off, attr_off);
+  }
 }
 
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
@@ -1268,8 +1526,9 @@ void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* pri
                        float* t, int max_stack, uint32_t* err, cudaStream_t st) {
   FirstHitOut fo{prim, mat, t, w, h, frame, err};
   WaveState none{};
-  k_trace_t<TRACE_FIRST, false><<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack), st>>>(
-      S, none, nullptr, max_stack, fo);
+  k_trace_t<TRACE_FIRST, false, false>
+      <<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack, PT_TRACE_BLOCK), st>>>(
+          S, none, nullptr, max_stack, fo, BatchRefs{});
 }
 
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,

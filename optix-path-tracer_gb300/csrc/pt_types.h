@@ -96,7 +96,7 @@ struct DevScene {
   int env_valid;            /* 1 if the environment can be importance sampled */
   int num_lights;
   int num_prims;
-  int root_leaf;            /* 1 if the root is a single leaf (<= 3 prims): node 0 still exists */
+  uint32_t root;            /* BVH8 node where traversal starts (0 for one scene) */
   int pad;
   GpuMiss miss;
   GpuCamera cam;

@@ -39,7 +39,7 @@ class PtError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("path_slots", ctypes.c_int),
                 ("enable_counters", ctypes.c_int), ("enable_timing", ctypes.c_int),
-                ("bvh_builder", ctypes.c_int)]
+                ("bvh_builder", ctypes.c_int), ("bvh_width", ctypes.c_int)]
 
 
 class RenderParams(ctypes.Structure):
@@ -55,7 +55,18 @@ class Stats(ctypes.Structure):
                 ("bvh_bytes", ctypes.c_uint64), ("bvh_depth", ctypes.c_int),
                 ("build_ms", ctypes.c_double), ("render_ms", ctypes.c_double),
                 ("iterations", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
-                ("stage_ms", ctypes.c_double * 5)]
+                ("stage_ms", ctypes.c_double * 5), ("graph_launches", ctypes.c_uint64)]
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("params", RenderParams),
+                ("accum_rgba", ctypes.c_void_p)]
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("path_slots", ctypes.c_int), ("trace_block", ctypes.c_int),
+                ("shade_block", ctypes.c_int), ("bvh_width", ctypes.c_int),
+                ("chunk_paths", ctypes.c_int), ("sample_paths_per_s", ctypes.c_double)]
 
 
 _F3 = ctypes.c_float * 3
@@ -95,6 +106,13 @@ SIGNATURES = {
     "pt_resolve_display": [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P],
     "pt_get_stats": [_P, ctypes.POINTER(Stats)],
     "pt_render_noalloc": [_P, ctypes.POINTER(RenderParams), _P, _P],
+    "pt_batch_create": [ctypes.POINTER(Options), ctypes.POINTER(_P)],
+    "pt_batch_destroy": [_P],
+    "pt_batch_render": [_P, ctypes.POINTER(BatchItem), ctypes.c_int, _P],
+    "pt_batch_autotune": [_P, ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.POINTER(Tune)],
+    "pt_batch_set_tune": [_P, ctypes.POINTER(Tune)],
+    "pt_batch_get_tune": [_P, ctypes.POINTER(Tune)],
+    "pt_batch_get_stats": [_P, ctypes.POINTER(Stats)],
 }
 
 _lib = None
@@ -117,6 +135,8 @@ def load_library(path=LIB_PATH):
     lib.pt_last_error.restype = ctypes.c_char_p
     lib.pt_version.argtypes = []
     lib.pt_version.restype = ctypes.c_char_p
+    lib.pt_batch_last_error.argtypes = [_P]
+    lib.pt_batch_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 
@@ -279,9 +299,11 @@ def _check(lib, ctx, rc):
 class GpuRenderer:
     """One pt_context with a committed scene."""
 
-    def __init__(self, scene, device=0, path_slots=0, counters=False, timing=False, builder=0):
+    def __init__(self, scene, device=0, path_slots=0, counters=False, timing=False, builder=0,
+                 bvh_width=0):
         self.lib = load_library()
-        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, builder)
+        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, builder,
+                      bvh_width)
         ctx = _P()
         rc = self.lib.pt_context_create(ctypes.byref(opt), ctypes.byref(ctx))
         if rc != 0:
@@ -400,9 +422,78 @@ class GpuRenderer:
     def stats(self):
         s = Stats()
         self._c(self.lib.pt_get_stats(self.ctx, ctypes.byref(s)))
-        d = {k: getattr(s, k) for k, _ in Stats._fields_}
-        d["stage_ms"] = list(s.stage_ms)
-        return d
+        return _stats_dict(s)
+
+
+def _stats_dict(s):
+    d = {k: getattr(s, k) for k, _ in Stats._fields_}
+    d["stage_ms"] = list(s.stage_ms)
+    return d
+
+
+class Batch:
+    """A pt_batch: many committed scenes (GpuRenderer contexts) rendered in
+    one wavefront."""
+
+    def __init__(self, device=0, path_slots=0, counters=False, timing=False, bvh_width=0):
+        self.lib = load_library()
+        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, 0, bvh_width)
+        b = _P()
+        rc = self.lib.pt_batch_create(ctypes.byref(opt), ctypes.byref(b))
+        if rc != 0:
+            raise PtError(rc, "pt_batch_create failed")
+        self.b = b
+
+    def close(self):
+        if self.b:
+            self.lib.pt_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc):
+        if rc != 0:
+            raise PtError(rc, self.lib.pt_batch_last_error(self.b).decode())
+
+    @staticmethod
+    def _items(jobs):
+        """jobs: list of (GpuRenderer, RenderParams, acc) with acc a numpy
+        float32 HxWx4 array or a device pointer int."""
+        arr = (BatchItem * len(jobs))()
+        for k, (r, p, acc) in enumerate(jobs):
+            arr[k].scene = r.ctx.value
+            arr[k].params = p
+            arr[k].accum_rgba = acc if isinstance(acc, int) else acc.ctypes.data
+        return arr
+
+    def render(self, jobs, stream=None):
+        arr = self._items(jobs)
+        self._c(self.lib.pt_batch_render(self.b, arr, len(jobs), stream))
+        return [acc for _, _, acc in jobs]
+
+    def autotune(self, jobs):
+        arr = self._items(jobs)
+        t = Tune()
+        self._c(self.lib.pt_batch_autotune(self.b, arr, len(jobs), ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tune._fields_}
+
+    def set_tune(self, path_slots, trace_block, shade_block, bvh_width, chunk_paths=0):
+        t = Tune(path_slots, trace_block, shade_block, bvh_width, chunk_paths, 0.0)
+        self._c(self.lib.pt_batch_set_tune(self.b, ctypes.byref(t)))
+
+    def tune(self):
+        t = Tune()
+        self._c(self.lib.pt_batch_get_tune(self.b, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tune._fields_}
+
+    def stats(self):
+        s = Stats()
+        self._c(self.lib.pt_batch_get_stats(self.b, ctypes.byref(s)))
+        return _stats_dict(s)
 
 
 # ------------------------------------------------------------ scene content
@@ -561,8 +652,7 @@ def heightfield_mesh(cells=1024, amplitude=0.1, seed=0, extent=1.0):
     idx = np.empty((2 * cells * cells, 3), dtype=np.uint32)
     idx[0::2] = np.stack([v0, v2, v1], axis=-1)
     idx[1::2] = np.stack([v1, v2, v3], axis=-1)
-    tile_of_tri = np.repeat(((j // max(1, cells // 16)) * 16 + (i // max(1, cells // 16))
-                             ).reshape(-1), 2)
+    tile_of_tri = np.repeat(((j * 16 // cells) * 16 + (i * 16 // cells)).reshape(-1), 2)
     return verts, idx, nrm.reshape(-1, 3).astype(np.float32), uvs, tile_of_tri
 
 

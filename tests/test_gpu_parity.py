@@ -148,6 +148,23 @@ def test_builders_match_oracle(ptgb_mod, oracle_mod, builder, name):
     g.close()
 
 
+@pytest.mark.parametrize("builder", [1, 2])
+@pytest.mark.parametrize("width", [2, 4, 6])
+def test_node_width_keeps_results(ptgb_mod, builder, width):
+    """Narrower BVH nodes (2..8 children) change traversal, never results:
+    first hits and paths equal the 8-wide tree's bit for bit."""
+    s, w, h = ptgb_mod.heightfield_scene(64, 36, cells=80, env_w=128, env_h=64), 64, 36
+    ref = ptgb_mod.GpuRenderer(s, builder=builder)
+    g = ptgb_mod.GpuRenderer(s, builder=builder, bvh_width=width)
+    for a, b in zip(g.first_hits(w, h, 3), ref.first_hits(w, h, 3)):
+        assert np.array_equal(a, b)
+    prm = ptgb_mod.GpuRenderer.params(w, h, 2, mode=1)
+    assert np.array_equal(g.render(prm), ref.render(prm))
+    assert g.stats()["bvh_depth"] >= ref.stats()["bvh_depth"]
+    g.close()
+    ref.close()
+
+
 def test_gpu_builder_large_mesh(ptgb_mod):
     """GPU builder on 2M triangles: valid tree (checked at commit), sane
     depth and node count, and a render that completes."""

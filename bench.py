@@ -8,6 +8,10 @@ ABI.  Prints one JSON line (rank 0).  `--impl reference` times the CPU
 restatement of the reference's device programs (the reference itself needs
 the OptiX 6 SDK and an OpenGL window, neither of which exists here) on a
 bounded sample of the same workload with all host threads.
+
+`--workload batch` is the batched multi-scene configuration: 64 seeded
+heightfield scenes (1e3..1e6 triangles, 256^2..1024^2, 16..256 spp) in one
+pt_batch_render per step, after pt_batch_autotune.
 """
 import argparse
 import json
@@ -36,6 +40,13 @@ WORKLOADS = {
                     "TS/AS/ON tiles, 2048x1024 HDR sky importance-sampled through its 2D CDF "
                     "(consistent mode: NEE + MIS)"),
 }
+
+BATCH_DESC = ("batched multi-scene render: 64 seeded heightfield scenes, triangles log-uniform "
+              "over 1e3..1e6 (8.96 M in all), square images of 256/512/1024 px, spp U{16..256} "
+              "(4.78 G paths in all), 1024x512 HDR sky importance-sampled (consistent mode), "
+              "max depth 50, RR after depth 10; one pt_batch_render (one CUDA-graph launch) "
+              "per step")
+BATCH_KW = dict(max_depth=50, rr_depth=10, mode=1)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
@@ -134,13 +145,26 @@ def cpu_sample(scene, w, h, spp, kw, target_s, threads, max_stride=None):
     return st, stride, frames
 
 
+def batch_cpu_scene(ptgb, items):
+    """The scene of the batch whose triangle count is the median: the CPU
+    sample of the batched workload."""
+    k = sorted(range(len(items)), key=lambda i: items[i][3])[len(items) // 2]
+    scene, res, spp, tris = items[k]
+    return scene, res, spp, tris, k
+
+
 def run_reference(args, wl):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import ptgb
     gen, w, h, spp, kw, desc = wl
-    scene = getattr(ptgb, gen)(w, h)
+    if gen == "batch_workload":
+        scene, w, spp, tris, k = batch_cpu_scene(ptgb, ptgb.batch_workload())
+        h = w
+        desc = desc + f" (CPU sample: scene {k}, {tris} triangles, {w}x{h})"
+    else:
+        scene = getattr(ptgb, gen)(w, h)
     threads = os.cpu_count()
     sys.path.insert(0, ORACLE)
     import oracle
@@ -322,17 +346,196 @@ def run_ours(args, wl):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    import numpy as np
+    import torch
+    import ptgb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    items = ptgb.batch_workload()
+    kw = BATCH_KW
+    rends = [ptgb.GpuRenderer(sc, device=local) for sc, *_ in items]
+    # replicas: rank r renders frames [r*spp, (r+1)*spp) of every scene
+    params = [ptgb.GpuRenderer.params(res, res, spp, frame0=rank * spp, **kw)
+              for _, res, spp, _ in items]
+    npix = [res * res for _, res, _, _ in items]
+    acc = torch.zeros((sum(npix), 4), dtype=torch.float32, device=f"cuda:{local}")
+    offs = np.concatenate([[0], np.cumsum(npix)[:-1]]).astype(np.int64)
+    jobs = [(r, p, acc.data_ptr() + 16 * int(o)) for r, p, o in zip(rends, params, offs)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    b = ptgb.Batch(device=local)
+    t_tune = time.perf_counter()
+    tune = b.autotune(jobs)
+    t_tune = time.perf_counter() - t_tune
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        b.render(jobs)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    dev_ms, paths, rays, launches, graphs = 0.0, 0, 0, 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()                      # evict L2 between steps
+        torch.cuda.synchronize()
+        b.render(jobs)                     # synchronous; device-timed inside
+        st = b.stats()
+        dev_ms += st["render_ms"]
+        paths += st["paths"]
+        rays += st["ext_rays"] + st["shadow_rays"]
+        launches += st["kernel_launches"]
+        graphs += st["graph_launches"]
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_s = dev_ms / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s, wall, float(paths), float(rays)], device=f"cuda:{local}")
+        mx = t.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = t.clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        dev_s, wall = float(mx[0]), float(mx[1])
+        tot_paths, tot_rays = float(sm[2]), float(sm[3])
+    else:
+        tot_paths, tot_rays = float(paths), float(rays)
+    value = tot_paths / dev_s
+
+    # ---- the same scenes one at a time (same batch object and tune)
+    single_ms = 0.0
+    for j in jobs:
+        b.render([j])
+        single_ms += b.stats()["render_ms"]
+    single_value = (paths / args.steps) / (single_ms / 1e3)
+
+    # ---- stage split (host loop with events) and bytes per ray (counters),
+    # each on a 1/8-spp copy of the batch
+    small = [(r, ptgb.GpuRenderer.params(p.width, p.height, max(1, p.spp // 8),
+                                         frame0=p.frame0, **kw), a) for r, p, a in jobs]
+    bt = ptgb.Batch(device=local, timing=True)
+    bt.set_tune(tune["path_slots"], tune["trace_block"], tune["shade_block"], tune["bvh_width"])
+    bt.render(small)
+    sst = bt.stats()
+    bt.close()
+    bc = ptgb.Batch(device=local, counters=True)
+    bc.set_tune(tune["path_slots"], tune["trace_block"], tune["shade_block"], tune["bvh_width"])
+    bc.render(small)
+    cs = bc.stats()
+    bc.close()
+    rays_c = cs["ext_rays"] + cs["shadow_rays"]
+    n_node = cs["node_fetches"] / rays_c
+    n_prim = cs["prim_tests"] / rays_c
+    b_ray = 32 + 16 + 80 * n_node + 48 * n_prim
+    trace_ms = sst["stage_ms"][1] + sst["stage_ms"][3]
+    trace_launches = 2 * sst["iterations"]
+    rays_t = sst["ext_rays"] + sst["shadow_rays"]
+    achieved = rays_t * b_ray / (trace_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+
+    # ---- end to end: commit every scene (upload + BVH build) and render the
+    # batch into pinned host accumulators
+    host = [torch.zeros((p.height, p.width, 4), dtype=torch.float32).pin_memory().numpy()
+            for p in params]
+    hjobs = [(r, p, a) for r, p, a in zip(rends, params, host)]
+    e2e_t, e2e_paths = 0.0, 0
+    for _ in range(max(1, args.steps // 2)):
+        barrier()
+        t1 = time.perf_counter()
+        for r in rends:
+            r._c(r.lib.pt_commit(r.ctx))
+        b.render(hjobs)
+        e2e_t += time.perf_counter() - t1
+        e2e_paths += b.stats()["paths"]
+    h2d = sum(int(r.stats()["bvh_bytes"]) for r in rends)
+    d2h = 16 * sum(npix)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        scene, res, spp, tris, k = batch_cpu_scene(ptgb, items)
+        cst, stride, frames = cpu_sample(scene, res, res, spp, kw, args.cpu_seconds,
+                                         os.cpu_count())
+        cpu = {"value": cst["paths"] / cst["seconds"], "unit": "paths/s",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": f"scene {k} of the batch (median size: {tris} triangles, {res}x{res}): "
+                         f"every {stride}th pixel x {frames} spp ({cst['paths']} paths, "
+                         f"{cst['seconds']:.1f} s)",
+               "mrays_per_s": (cst["ext_rays"] + cst["shadow_rays"]) / cst["seconds"] / 1e6}
+
+    if rank == 0:
+        line = {
+            "metric": "paths/s", "value": value, "unit": "paths/s",
+            "mrays_per_s": tot_rays / dev_s / 1e6,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": BATCH_DESC, "scenes": len(items),
+                       "paths_per_rank_step": paths // args.steps,
+                       "l2": "flushed between steps (256 MiB write); per-step working set "
+                             "(8.96 M triangles of geometry, path state, results) exceeds L2",
+                       "tune": tune, "autotune_s": t_tune,
+                       "parallelism": f"replicas{world}" if world > 1 else "single"},
+            "unbatched": {"value": single_value, "unit": "paths/s",
+                          "note": "the same 64 scenes rendered one at a time (one graph launch "
+                                  "each), device time"},
+            "e2e": {"value": e2e_paths / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "includes": "pt_commit of all 64 scenes (upload + BVH8 build) + "
+                                "pt_batch_render into pinned host accumulators"},
+            "gpu_launches": launches,
+            "graph_launches": graphs,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_trace + k_trace_shadow (BVH8 closest hit, batch)",
+                         "peak_source": peak_kind, "bytes_per_ray": b_ray,
+                         "nodes_per_ray": n_node, "prims_per_ray": n_prim,
+                         "avg_launch_ms": trace_ms / trace_launches,
+                         "rays_per_launch": rays_t / trace_launches,
+                         "measured_on": "1/8-spp copy of the batch (host loop with events)"},
+            "stage_ms_share": {k: v / max(sum(sst["stage_ms"]), 1e-9) for k, v in
+                               zip(["generate", "trace", "shade", "shadow_trace", "finish"],
+                                   sst["stage_ms"])},
+            "wall_s": wall,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
+    for r in rends:
+        r.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 5; 2 for the batch workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS) + ["batch"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spp", type=int, default=0, help="override spp (small profiling cases)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 2 if args.workload == "batch" else 5
+    if args.workload == "batch":
+        if args.impl == "reference":
+            run_reference(args, ("batch_workload", 0, 0, 0, BATCH_KW, BATCH_DESC))
+        else:
+            run_batch(args)
+        return
     wl = WORKLOADS[args.workload]
     if args.spp:
         wl = wl[:3] + (args.spp,) + wl[4:5] + (wl[5].replace(f"{wl[3]} spp", f"{args.spp} spp"),)

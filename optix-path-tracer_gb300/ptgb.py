@@ -678,11 +678,13 @@ def sky_env(width=2048, height=1024, sun_peak=5e4, sun_dir=(0.4, 0.6, -0.69), si
     return np.ascontiguousarray(rgba, dtype=np.float32)
 
 
-def heightfield_scene(width=1920, height=1080, cells=1024, seed=0, env_w=2048, env_h=1024):
+def heightfield_scene(width=1920, height=1080, cells=1024, seed=0, env_w=2048, env_h=1024,
+                      env=None):
     """Triangle heightfield of the third benchmark configuration: fBm terrain
     with one material per tile (16x16 tiles) drawn from Torrance-Sparrow
     (roughness U[0.05,0.5]), Ashikhmin-Shirley (nu,nv U[10,1000]) and
-    Oren-Nayar (sigma U[0,0.5]); HDR sky with a sun lobe."""
+    Oren-Nayar (sigma U[0,0.5]); HDR sky with a sun lobe (`env`, if given,
+    is a ready sky_env array)."""
     rng = SplitMix64(seed ^ 0xC3)
     U = rng.uniform
     s = Scene()
@@ -701,9 +703,28 @@ def heightfield_scene(width=1920, height=1080, cells=1024, seed=0, env_w=2048, e
     verts, idx, nrm, uvs, tile = heightfield_mesh(cells, 0.1, seed)
     mpt = np.asarray(mats, dtype=np.uint32)[tile]
     s.mesh(verts, idx, mats[0], mat_per_tri=mpt, normals=nrm, uvs=uvs)
-    s.miss_env(sky_env(env_w, env_h), spherical=True)
+    s.miss_env(sky_env(env_w, env_h) if env is None else env, spherical=True)
     s.set_camera((0.0, 0.9, 1.9), (0.0, 0.0, 0.0), (0, 1, 0), 45.0, width / height, 0.0, 2.0)
     return s
+
+
+def batch_workload(n=64, seed=4, env_w=1024, env_h=512):
+    """The batched multi-scene workload: n seeded heightfield scenes with
+    triangle counts log-uniform over [1e3, 1e6], square images of 256, 512 or
+    1024 pixels a side and spp uniform over 16..256.  Returns a list of
+    (scene, size, spp, triangles)."""
+    rng = SplitMix64(seed)
+    U = rng.uniform
+    env = sky_env(env_w, env_h)
+    out = []
+    for k in range(n):
+        tris = 1e3 * 1000.0 ** U()
+        cells = max(16, int(round((tris / 2) ** 0.5)))
+        res = (256, 512, 1024)[min(2, int(U() * 3))]
+        spp = 16 + min(240, int(U() * 241))
+        out.append((heightfield_scene(res, res, cells=cells, seed=100 + k, env=env), res, spp,
+                    2 * cells * cells))
+    return out
 
 
 def material_zoo(width=128, height=96, cells=12):

@@ -68,6 +68,9 @@ typedef struct pt_options {
   int enable_timing;   /* per-stage device times (CUDA events in the graph) */
   int bvh_builder;     /* 0 automatic, 1 host (binned SAH), 2 GPU (LBVH + treelets) */
   int bvh_width;       /* most children per BVH node, 2..8; 0 = 8 */
+  int shade_order;     /* 0 automatic (material-sorted tiles when the scene uses
+                          Oren-Nayar, Torrance-Sparrow or Ashikhmin-Shirley), 1 sorted,
+                          2 path order */
 } pt_options;
 
 typedef struct pt_render_params {
@@ -238,6 +241,7 @@ typedef struct pt_tune {
   int shade_block;          /* threads per shade block: 64..256, multiple of 32 */
   int bvh_width;            /* most children per BVH node, 2..8 */
   int chunk_paths;          /* paths per chunk (per-path result area), 0 = 2^27 */
+  int shade_order;          /* as pt_options.shade_order */
   double sample_paths_per_s;/* autotune: throughput of this configuration on its sample */
 } pt_tune;
 
@@ -250,7 +254,8 @@ PT_API const char* pt_batch_last_error(pt_batch* b);
 PT_API int pt_batch_render(pt_batch* b, const pt_batch_item* items, int n, void* stream);
 /* Times short renders of a sample of the items (every item at low spp, into
  * scratch accumulators; the items' accumulators are not touched) over path
- * slots, trace and shade block sizes and BVH node width, keeps the fastest
+ * slots, trace and shade block sizes, BVH node width and shade order (material-
+ * sorted tiles or path order), keeps the fastest
  * configuration for later pt_batch_render calls and returns it in *best. */
 PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_tune* best);
 PT_API int pt_batch_set_tune(pt_batch* b, const pt_tune* t);

@@ -177,7 +177,8 @@ PT_API const char* pt_last_error(pt_context* ctx) {
 PT_API int pt_context_create(const pt_options* opt, pt_context** out) {
   if (!out) return PT_EINVAL;
   *out = nullptr;
-  if (opt && (opt->bvh_width != 0 && (opt->bvh_width < 2 || opt->bvh_width > 8)))
+  if (opt && ((opt->bvh_width != 0 && (opt->bvh_width < 2 || opt->bvh_width > 8)) ||
+              opt->shade_order < 0 || opt->shade_order > 2))
     return PT_EINVAL;
   pt_context* ctx = new (std::nothrow) pt_context();
   if (!ctx) return PT_ENOMEM;
@@ -709,6 +710,7 @@ PT_API int pt_commit(pt_context* ctx) {
     return fail(ctx, PT_EINVAL, "BVH too deep for the traversal stack");
   CK(pt::set_trace_smem());
   ctx->lc = pt::default_launch(ctx->max_stack);
+  ctx->lc.sort = ctx->opt.shade_order == 1 || (ctx->opt.shade_order == 0 && pth::sort_pays(ctx));
   auto t1 = std::chrono::steady_clock::now();
   ctx->stats.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   ctx->stats.bvh_nodes = nn;
@@ -863,6 +865,14 @@ static void reset_render_stats(pt_context* ctx) {
 }
 
 }  // extern "C"
+
+bool pth::sort_pays(const pt_context* ctx) {
+  for (const GpuMaterial& m : ctx->mats)
+    if (m.type == PT_MAT_OREN_NAYAR || m.type == PT_MAT_TORRANCE_SPARROW ||
+        m.type == PT_MAT_ASHIKHMIN_SHIRLEY)
+      return true;
+  return false;
+}
 
 int pth::check_params(pt_context* ctx, const pt_render_params* p) {
   if (!p) return fail(ctx, PT_EINVAL, "null params");

@@ -127,7 +127,8 @@ static bool tune_valid(const pt_tune& t) {
   return t.path_slots >= 1024 && t.path_slots <= (1 << 24) &&
          (t.trace_block == 64 || t.trace_block == 128 || t.trace_block == 256) &&
          t.shade_block >= 64 && t.shade_block <= PT_SHADE_BLOCK && t.shade_block % 32 == 0 &&
-         t.bvh_width >= 2 && t.bvh_width <= 8 && t.chunk_paths >= 0;
+         t.bvh_width >= 2 && t.bvh_width <= 8 && t.chunk_paths >= 0 &&
+         t.shade_order >= 0 && t.shade_order <= 2;
 }
 
 static void drop_graph(pt_batch* b) {
@@ -410,6 +411,9 @@ static int batch_render(pt_batch* b, const pt_batch_item* items, int n, float4* 
   lc.shade_block = b->tune.shade_block;
   lc.trace_grid = pt::wave_grid(0, b->max_stack, lc.trace_block);
   lc.shade_grid = pt::wave_grid(1, b->max_stack, lc.shade_block);
+  lc.sort = b->tune.shade_order == 1;
+  if (b->tune.shade_order == 0)
+    for (const ScenePart& p : b->parts) lc.sort = lc.sort || sort_pays(p.ctx);
   b->lc = lc;
   // accumulators: the items' device buffers, or device copies of host ones
   std::vector<float4*> acc(n);
@@ -643,6 +647,7 @@ PT_API int pt_batch_create(const pt_options* opt, pt_batch** out) {
   b->tune.trace_block = PT_TRACE_BLOCK;
   b->tune.shade_block = PT_SHADE_BLOCK;
   b->tune.bvh_width = (opt && opt->bvh_width) ? opt->bvh_width : 8;
+  b->tune.shade_order = opt ? opt->shade_order : 0;
   if (!tune_valid(b->tune)) {
     delete b;
     return PT_EINVAL;
@@ -781,6 +786,7 @@ PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_
   const int tb_opts[] = {64, 128, 256};
   const int sb_opts[] = {128, 256};
   const int w_opts[] = {8, 4};
+  const int order_opts[] = {1, 2};
   for (int v : slot_opts) {
     pt_tune t = best;
     t.path_slots = v;
@@ -799,6 +805,11 @@ PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_
   for (int v : w_opts) {
     pt_tune t = best;
     t.bvh_width = v;
+    if ((rc = consider(t))) return rc;
+  }
+  for (int v : order_opts) {
+    pt_tune t = best;
+    t.shade_order = v;
     if ((rc = consider(t))) return rc;
   }
   best.sample_paths_per_s = best_pps;

@@ -118,6 +118,10 @@ int build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<float4>
  * (PT_SLOT_F4 per slot) and one uint4 block (PT_SLOT_U4 per slot). */
 void carve_wave(WaveState& W, float4* f, uint4* u, size_t slots);
 bool is_device_ptr(const void* p);
+/* Whether shading in material-sorted tiles pays for this scene: it does when
+ * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
+ * is present, whose code paths diverge most in a mixed warp. */
+bool sort_pays(const pt_context* ctx);
 /* Render parameters valid for the context (sets ctx->err otherwise). */
 int check_params(pt_context* ctx, const pt_render_params* p);
 }  // namespace pth

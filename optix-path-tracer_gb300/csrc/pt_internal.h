@@ -28,6 +28,7 @@
 struct LaunchCfg {
   int trace_block, trace_grid;
   int shade_block, shade_grid;
+  int sort;            /* shade in material-sorted tiles */
 };
 
 struct Ray3 {

@@ -168,21 +168,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
   int sp = 0;
   bool active = false;
 
-  auto fetch = [&]() {
-    for (; i < n && S.num_prims == 0; i += stride) {
-      // empty scene: every ray misses
-      if (MODE == TRACE_EXT) {
-        W.hit[i] = make_float4(W.path[c.parity].ray_d[i].w, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
-      } else if (MODE == TRACE_SHADOW) {
-        W.sh.Wi[i].w = 1.f;
-      } else {
-        fo.prim[i] = PT_NO_HIT;
-        fo.mat[i] = PT_NO_HIT;
-        fo.t[i] = 0.f;
-      }
-    }
-    active = i < n;
-    if (!active) return;
+  auto load_ray = [&]() {
     if (MODE == TRACE_EXT) {
       slot = i;
       float4 ro = W.path[c.parity].ray_o[i], rdv = W.path[c.parity].ray_d[i];
@@ -205,31 +191,6 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       tmin = 1e-6f;
       tmax = PT_RAY_TMAX;
     }
-    const float eps = 1e-18f;
-    float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
-    float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
-    float dz = fabsf(d.z) < eps ? copysignf(eps, d.z) : d.z;
-    ix = 1.0f / dx;
-    iy = 1.0f / dy;
-    iz = 1.0f / dz;
-    negx = ix < 0.f;
-    negy = iy < 0.f;
-    negz = iz < 0.f;
-    WtRay w = wt_setup(d);
-    ws.ro[lane] = make_float4(o.x, o.y, o.z, tmin);
-    ws.rd[lane] = make_float4(d.x, d.y, d.z, tmax);
-    ws.wt[lane] = make_float4(w.Sx, w.Sy, w.Sz,
-                              __uint_as_float((uint32_t)w.kx | ((uint32_t)w.ky << 2) |
-                                              ((uint32_t)w.kz << 4)));
-    tbest = tmax;
-    best_id = PT_NO_HIT;
-    ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
-    cur = S.root;
-    if (BATCH) {
-      uint32_t z = MODE == TRACE_EXT ? W.path[c.parity].st[i].z : W.sh.st[i].z;
-      cur = __ldg(br.roots + (z >> PT_ST_SCENE_SHIFT));
-    }
-    sp = 0;
   };
 
   auto finish = [&]() {
@@ -265,6 +226,50 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         fo.t[i] = tbest;
       }
     }
+  };
+
+  auto fetch = [&]() {
+    // a ray with a NaN in its origin or direction hits nothing (every
+    // primitive test fails or yields a NaN distance, which never wins the
+    // closest-hit minimum), and neither does any ray of an empty scene: both
+    // end here, without a traversal (a NaN ray would pass every box test)
+    while (i < n) {
+      load_ray();
+      bool nan = !(o.x == o.x && o.y == o.y && o.z == o.z && d.x == d.x && d.y == d.y &&
+                   d.z == d.z);
+      if (!nan && S.num_prims != 0) break;
+      best_id = PT_NO_HIT;
+      tbest = tmax;
+      finish();
+      i += stride;
+    }
+    active = i < n;
+    if (!active) return;
+    const float eps = 1e-18f;
+    float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
+    float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
+    float dz = fabsf(d.z) < eps ? copysignf(eps, d.z) : d.z;
+    ix = 1.0f / dx;
+    iy = 1.0f / dy;
+    iz = 1.0f / dz;
+    negx = ix < 0.f;
+    negy = iy < 0.f;
+    negz = iz < 0.f;
+    WtRay w = wt_setup(d);
+    ws.ro[lane] = make_float4(o.x, o.y, o.z, tmin);
+    ws.rd[lane] = make_float4(d.x, d.y, d.z, tmax);
+    ws.wt[lane] = make_float4(w.Sx, w.Sy, w.Sz,
+                              __uint_as_float((uint32_t)w.kx | ((uint32_t)w.ky << 2) |
+                                              ((uint32_t)w.kz << 4)));
+    tbest = tmax;
+    best_id = PT_NO_HIT;
+    ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
+    cur = S.root;
+    if (BATCH) {
+      uint32_t z = MODE == TRACE_EXT ? W.path[c.parity].st[i].z : W.sh.st[i].z;
+      cur = __ldg(br.roots + (z >> PT_ST_SCENE_SHIFT));
+    }
+    sp = 0;
   };
 
   fetch();
@@ -769,143 +774,222 @@ __device__ __forceinline__ V3 miss_color(const GpuMiss& ms, V3 d) {
   return 2.f * env_lookup(ms, u, v);
 }
 
+// ------------------------------------------------ material-sorted tiles --
+// The shade kernels take the live paths in tiles of blockDim x
+// PT_SORT_ITEMS consecutive positions and shade each tile in the order of
+// its material key (0 miss, 1 + material type, PT_SORT_KEYS - 1 past the
+// end): a counting sort in shared memory (shared atomics give the ranks, one
+// thread the key offsets).  Warps then run one material's code instead of a
+// mix, which is what bounds these kernels (SIMT efficiency and instruction
+// fetch).  The order does not change any path's result.
+#define PT_SORT_ITEMS 4
+#define PT_SORT_KEYS (PT_NUM_MAT_TYPES + 2)
+
+struct SortTile {
+  uint16_t perm[PT_SHADE_BLOCK * PT_SORT_ITEMS];  // tile position in sorted order
+  uint32_t cnt[PT_SORT_KEYS];
+  uint32_t start[PT_SORT_KEYS];
+};
+
+__device__ __forceinline__ uint32_t shade_key(const DevScene& S0, const float4* __restrict__ hit,
+                                              uint32_t i, uint32_t n) {
+  if (i >= n) return PT_SORT_KEYS - 1;
+  uint32_t leaf = __float_as_uint(hit[i].w);
+  if (leaf == PT_NO_HIT) return 0;
+  uint32_t mid = __float_as_uint(__ldg(&S0.prims[3 * (size_t)leaf + 2].w));
+  return 1u + (uint32_t)__ldg(&S0.mats[mid].type);
+}
+
+__device__ __forceinline__ void sort_tile(SortTile& t, const DevScene& S0,
+                                          const float4* __restrict__ hit, uint32_t base,
+                                          uint32_t n) {
+  const uint32_t bd = blockDim.x;
+  if (threadIdx.x < PT_SORT_KEYS) t.cnt[threadIdx.x] = 0;
+  __syncthreads();
+  uint32_t key[PT_SORT_ITEMS], rank[PT_SORT_ITEMS];
+#pragma unroll
+  for (int it = 0; it < PT_SORT_ITEMS; it++) {
+    key[it] = shade_key(S0, hit, base + it * bd + threadIdx.x, n);
+    rank[it] = atomicAdd(&t.cnt[key[it]], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t sum = 0;
+    for (int k = 0; k < PT_SORT_KEYS; k++) {
+      t.start[k] = sum;
+      sum += t.cnt[k];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < PT_SORT_ITEMS; it++)
+    t.perm[t.start[key[it]] + rank[it]] = (uint16_t)(it * bd + threadIdx.x);
+  __syncthreads();
+}
+
+// Loop of a shade kernel over its paths: material-sorted tiles (SORT) or a
+// plain grid-stride loop.  Every lane of a warp runs every step (the queue
+// appends inside are warp-aggregated).
+#define SHADE_LOOP(CALL)                                                           \
+  if (SORT) {                                                                      \
+    const uint32_t tile_n = blockDim.x * PT_SORT_ITEMS;                            \
+    for (uint32_t base = blockIdx.x * tile_n; base < n; base += gridDim.x * tile_n) { \
+      sort_tile(tile, S0, W.hit, base, n);                                         \
+      for (int it = 0; it < PT_SORT_ITEMS; it++) {                                 \
+        uint32_t i = base + tile.perm[it * blockDim.x + threadIdx.x];              \
+        CALL;                                                                      \
+      }                                                                            \
+      __syncthreads();                                                             \
+    }                                                                              \
+  } else {                                                                         \
+    uint32_t stride = gridDim.x * blockDim.x;                                      \
+    uint32_t iters = (n + stride - 1) / stride;                                    \
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;                            \
+    for (uint32_t it = 0; it < iters; it++, i += stride) {                         \
+      CALL;                                                                        \
+    }                                                                              \
+  }
+
+// One path of k_shade (position i of the current buffer; all lanes of the
+// warp call it together: the queue appends are warp-aggregated).
 template <bool BATCH>
+__device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& W,
+                                         const WaveCounters& c, const WaveCtl& ctl,
+                                         const BatchRefs& br, uint32_t i, bool active) {
+  const PathBuf& pb = W.path[c.parity];
+  uint4 st = make_uint4(0, 0, 0, 0);
+  V3 thr = v3(0.f), rad = v3(0.f);
+  Tail tl;
+  tl.event = 1;
+  tl.isSpecular = false;
+  bool tail = false, shadow = false, missed = false;
+  V3 col = v3(0.f);
+  V3 P, N, Wo, Wi;
+  float lightPDF = 0.f;
+  int lindex = 0;
+  uint32_t mid = 0;
+  if (active) st = pb.st[i];
+  const DevScene& S = path_scene<BATCH>(S0, br, st.z);
+  if (active) {
+    float4 t4 = pb.thr[i], r4 = pb.rad[i];
+    thr = f4xyz(t4);
+    rad = f4xyz(r4);
+    float4 hit = W.hit[i];
+    float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
+    uint32_t leaf = __float_as_uint(hit.w);
+    if (leaf == PT_NO_HIT) {
+      thr *= miss_color(S.miss, f4xyz(rdv));
+      col = rad + clamp3(thr, 0.f, 1.f);  // raygen.cu:81-82
+      missed = true;
+    } else {
+      PrimRec p = load_prim(S.prims, leaf);
+      HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, false);
+      mid = rec.index;
+      GpuMaterial m = S.mats[mid];
+      P = rec.P;
+      Wo = rec.Wo;
+      N = rec.shading_normal;
+      switch (m.type) {
+        case PT_MAT_LAMBERTIAN:
+        case PT_MAT_OREN_NAYAR:
+        case PT_MAT_DIFFUSE_LIGHT: {
+          bool isLight = m.type == PT_MAT_DIFFUSE_LIGHT;
+          if (nee_begin(S, st.x, P, N, isLight, Wi, lightPDF, lindex)) {
+            shadow = true;
+          } else {
+            after_nee(m, st.x, P, Wo, N, v3(0.f), thr, rad, tl);
+            tail = true;
+          }
+          break;
+        }
+        case PT_MAT_METAL: {  // programs/materials/metal.cu:38-56
+          V3 reflected = reflect(-Wo, N);
+          tl.direction = reflected + m.p0 * random_in_unit_sphere(st.x);
+          tl.event = 0;
+          tl.origin = P;
+          thr *= v3(m.c0x, m.c0y, m.c0z);
+          tl.isSpecular = true;
+          tail = true;
+          break;
+        }
+        case PT_MAT_DIELECTRIC: {  // programs/materials/dielectric.cu:46-96
+          float ref_idx = m.p0;
+          V3 Wd = -rec.Wo;
+          V3 Nd = N;
+          V3 absorption = v3(1.f);
+          float ni_over_nt;
+          float cosine = dot(Wd, Nd);
+          if (cosine > 0.f) {
+            Nd = -Nd;
+            ni_over_nt = ref_idx;
+            cosine = ref_idx * cosine / length(Wd);
+          } else {
+            ni_over_nt = 1.f / ref_idx;
+            cosine = -cosine / length(Wd);
+          }
+          V3 refracted = v3(0.f);
+          float reflect_prob;
+          if (Refract(Wd, Nd, ni_over_nt, refracted))
+            reflect_prob = schlick(cosine, ref_idx);
+          else
+            reflect_prob = 1.f;
+          if (rnd(st.x) < reflect_prob)
+            tl.direction = reflect(Wd, Nd);
+          else
+            tl.direction = normalize(refracted);
+          tl.event = 0;
+          tl.origin = P;
+          thr *= (v3(m.c0x, m.c0y, m.c0z) * absorption);
+          tl.isSpecular = true;
+          tail = true;
+          break;
+        }
+        case PT_MAT_TORRANCE_SPARROW:
+        case PT_MAT_ASHIKHMIN_SHIRLEY: {
+          V3 Wn = brdf_sample(m, Wo, N, st.x);
+          float pdf = 0.f;
+          V3 attenuation = brdf_eval(m, Wo, Wn, N, pdf);
+          tl.event = 0;
+          tl.origin = P;
+          tl.direction = Wn;
+          if (m.type == PT_MAT_TORRANCE_SPARROW)
+            thr *= clamp3(attenuation / pdf, 0.f, 1.f);
+          else
+            thr *= clamp3(attenuation, 0.f, 1.f);
+          tl.isSpecular = true;
+          tail = true;
+          break;
+        }
+        default:
+          tl.event = 1;
+          tail = true;
+      }
+    }
+  }
+  // shadow rays: park the Direct_Light context and the path state
+  uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
+  if (shadow) {
+    W.sh.P[spos] = make_float4(P.x, P.y, P.z, lightPDF);
+    W.sh.N[spos] = make_float4(N.x, N.y, N.z, __int_as_float(lindex));
+    W.sh.Wo[spos] = make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid));
+    W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
+    W.sh.st[spos] = st;
+    W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+  }
+  if (missed) finalize_path(W, st.y, col);  // misses end here
+  path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, tail);
+}
+
+template <bool BATCH, bool SORT>
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S0, WaveState W,
                                                           const WaveCtl* __restrict__ ctlp,
                                                           BatchRefs br) {
+  __shared__ SortTile tile;
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
-  const PathBuf& pb = W.path[c.parity];
-  uint32_t stride = gridDim.x * blockDim.x;
-  // all lanes of a warp iterate together (ballots inside)
-  uint32_t iters = (n + stride - 1) / stride;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (uint32_t it = 0; it < iters; it++, i += stride) {
-    bool active = i < n;
-    uint4 st = make_uint4(0, 0, 0, 0);
-    V3 thr = v3(0.f), rad = v3(0.f);
-    Tail tl;
-    tl.event = 1;
-    tl.isSpecular = false;
-    bool tail = false, shadow = false, missed = false;
-    V3 col = v3(0.f);
-    V3 P, N, Wo, Wi;
-    float lightPDF = 0.f;
-    int lindex = 0;
-    uint32_t mid = 0;
-    if (active) st = pb.st[i];
-    const DevScene& S = path_scene<BATCH>(S0, br, st.z);
-    if (active) {
-      float4 t4 = pb.thr[i], r4 = pb.rad[i];
-      thr = f4xyz(t4);
-      rad = f4xyz(r4);
-      float4 hit = W.hit[i];
-      float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
-      uint32_t leaf = __float_as_uint(hit.w);
-      if (leaf == PT_NO_HIT) {
-        thr *= miss_color(S.miss, f4xyz(rdv));
-        col = rad + clamp3(thr, 0.f, 1.f);  // raygen.cu:81-82
-        missed = true;
-      } else {
-        PrimRec p = load_prim(S.prims, leaf);
-        HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, false);
-        mid = rec.index;
-        GpuMaterial m = S.mats[mid];
-        P = rec.P;
-        Wo = rec.Wo;
-        N = rec.shading_normal;
-        switch (m.type) {
-          case PT_MAT_LAMBERTIAN:
-          case PT_MAT_OREN_NAYAR:
-          case PT_MAT_DIFFUSE_LIGHT: {
-            bool isLight = m.type == PT_MAT_DIFFUSE_LIGHT;
-            if (nee_begin(S, st.x, P, N, isLight, Wi, lightPDF, lindex)) {
-              shadow = true;
-            } else {
-              after_nee(m, st.x, P, Wo, N, v3(0.f), thr, rad, tl);
-              tail = true;
-            }
-            break;
-          }
-          case PT_MAT_METAL: {  // programs/materials/metal.cu:38-56
-            V3 reflected = reflect(-Wo, N);
-            tl.direction = reflected + m.p0 * random_in_unit_sphere(st.x);
-            tl.event = 0;
-            tl.origin = P;
-            thr *= v3(m.c0x, m.c0y, m.c0z);
-            tl.isSpecular = true;
-            tail = true;
-            break;
-          }
-          case PT_MAT_DIELECTRIC: {  // programs/materials/dielectric.cu:46-96
-            float ref_idx = m.p0;
-            V3 Wd = -rec.Wo;
-            V3 Nd = N;
-            V3 absorption = v3(1.f);
-            float ni_over_nt;
-            float cosine = dot(Wd, Nd);
-            if (cosine > 0.f) {
-              Nd = -Nd;
-              ni_over_nt = ref_idx;
-              cosine = ref_idx * cosine / length(Wd);
-            } else {
-              ni_over_nt = 1.f / ref_idx;
-              cosine = -cosine / length(Wd);
-            }
-            V3 refracted = v3(0.f);
-            float reflect_prob;
-            if (Refract(Wd, Nd, ni_over_nt, refracted))
-              reflect_prob = schlick(cosine, ref_idx);
-            else
-              reflect_prob = 1.f;
-            if (rnd(st.x) < reflect_prob)
-              tl.direction = reflect(Wd, Nd);
-            else
-              tl.direction = normalize(refracted);
-            tl.event = 0;
-            tl.origin = P;
-            thr *= (v3(m.c0x, m.c0y, m.c0z) * absorption);
-            tl.isSpecular = true;
-            tail = true;
-            break;
-          }
-          case PT_MAT_TORRANCE_SPARROW:
-          case PT_MAT_ASHIKHMIN_SHIRLEY: {
-            V3 Wn = brdf_sample(m, Wo, N, st.x);
-            float pdf = 0.f;
-            V3 attenuation = brdf_eval(m, Wo, Wn, N, pdf);
-            tl.event = 0;
-            tl.origin = P;
-            tl.direction = Wn;
-            if (m.type == PT_MAT_TORRANCE_SPARROW)
-              thr *= clamp3(attenuation / pdf, 0.f, 1.f);
-            else
-              thr *= clamp3(attenuation, 0.f, 1.f);
-            tl.isSpecular = true;
-            tail = true;
-            break;
-          }
-          default:
-            tl.event = 1;
-            tail = true;
-        }
-      }
-    }
-    // shadow rays: park the Direct_Light context and the path state
-    uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
-    if (shadow) {
-      W.sh.P[spos] = make_float4(P.x, P.y, P.z, lightPDF);
-      W.sh.N[spos] = make_float4(N.x, N.y, N.z, __int_as_float(lindex));
-      W.sh.Wo[spos] = make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid));
-      W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
-      W.sh.st[spos] = st;
-      W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
-      W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
-    }
-    if (missed) finalize_path(W, st.y, col);  // misses end here
-    path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, tail);
-  }
+  SHADE_LOOP(shade_path<BATCH>(S0, W, c, ctl, br, i, i < n))
 }
 
 template <bool BATCH>
@@ -968,167 +1052,170 @@ __device__ __forceinline__ void path_push(const WaveState& W, const WaveCounters
 // with MIS at hits and misses, NEE over lights + environment, BSDF
 // continuation, Russian roulette.  The NEE term waits for its shadow ray in
 // the shadow buffer together with the already-sampled continuation.
+// One path of k_shade_c (see shade_path).
 template <bool BATCH>
+__device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState& W,
+                                           const WaveCounters& c, const WaveCtl& ctl,
+                                           const BatchRefs& br, uint32_t i, bool active) {
+  const PathBuf& pb = W.path[c.parity];
+  uint4 st = make_uint4(0, 0, 0, 0);
+  V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), Wi = v3(0.f), dcont = v3(0.f), C = v3(0.f);
+  float tmax = 0.f;
+  bool ended = false, shadow = false;
+  if (active) st = pb.st[i];
+  const DevScene& S = path_scene<BATCH>(S0, br, st.z);
+  const int n_sel = S.num_lights + (S.env_valid ? 1 : 0);
+  if (active) {
+    const PathCtl pc = path_ctl<BATCH>(ctl, br, st.z);
+    thr = f4xyz(pb.thr[i]);
+    rad = f4xyz(pb.rad[i]);
+    float4 hit = W.hit[i];
+    float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
+    V3 d = f4xyz(rdv);
+    uint32_t depth = st.z & PT_ST_DEPTH_MASK;
+    // a camera ray counts as a specular bounce: emission it sees is not MIS-weighted
+    bool prev_spec = ((st.z >> PT_ST_SPEC_BIT) & 1u) || depth == 0;
+    float pdf_prev = __uint_as_float(st.w);
+    uint32_t leaf = __float_as_uint(hit.w);
+    if (leaf == PT_NO_HIT) {
+      V3 Le = miss_color(S.miss, d);
+      float w = 1.f;
+      if (!prev_spec && S.env_valid) w = power_mis(pdf_prev, env_pdf_dir(S, d) / (float)n_sel);
+      rad += thr * Le * w;
+      ended = true;
+    } else {
+      PrimRec p = load_prim(S.prims, leaf);
+      HitRecord rec = hit_record(S, p, f4xyz(ro), d, hit.x, hit.y, hit.z, false);
+      GpuMaterial m = S.mats[rec.index];
+      P = rec.P;
+      V3 Wo = rec.Wo, N = rec.shading_normal;
+      if (m.type == PT_MAT_DIFFUSE_LIGHT) {
+        float w = 1.f;
+        if (!prev_spec && n_sel > 0) w = power_mis(pdf_prev, lights_pdf_c(S, f4xyz(ro), d, n_sel));
+        rad += thr * v3(m.c0x, m.c0y, m.c0z) * w;
+        ended = true;
+      } else if (m.type == PT_MAT_METAL) {  // programs/materials/metal.cu:38-56
+        V3 reflected = reflect(-Wo, N);
+        dcont = reflected + m.p0 * random_in_unit_sphere(st.x);
+        thr *= v3(m.c0x, m.c0y, m.c0z);
+        prev_spec = true;
+      } else if (m.type == PT_MAT_DIELECTRIC) {  // programs/materials/dielectric.cu:46-96
+        float ref_idx = m.p0;
+        V3 Wd = -rec.Wo, Nd = N;
+        float ni_over_nt;
+        float cosine = dot(Wd, Nd);
+        if (cosine > 0.f) {
+          Nd = -Nd;
+          ni_over_nt = ref_idx;
+          cosine = ref_idx * cosine / length(Wd);
+        } else {
+          ni_over_nt = 1.f / ref_idx;
+          cosine = -cosine / length(Wd);
+        }
+        V3 refracted = v3(0.f);
+        float reflect_prob;
+        if (Refract(Wd, Nd, ni_over_nt, refracted)) reflect_prob = schlick(cosine, ref_idx);
+        else reflect_prob = 1.f;
+        if (rnd(st.x) < reflect_prob) dcont = reflect(Wd, Nd);
+        else dcont = normalize(refracted);
+        thr *= (v3(m.c0x, m.c0y, m.c0z) * v3(1.f));
+        prev_spec = true;
+      } else {
+        Frame fr(N);
+        V3 wo_l = fr.to_local(Wo);
+        if (n_sel > 0) {
+          int k = (int)(rnd(st.x) * (float)n_sel);
+          if (k > n_sel - 1) k = n_sel - 1;
+          float pl = 0.f;
+          V3 Le;
+          tmax = PT_RAY_TMAX;
+          if (k < S.num_lights) {
+            GpuLight L = S.lights[k];
+            if (L.type == PT_LIGHT_RECT) {
+              Wi = light_sample(L, P, st.x);
+              tmax = 1.f - 1e-4f;
+            } else {
+              Wi = sphere_light_sample_c(L, P, st.x);
+              V3 lc = v3(L.cx, L.cy, L.cz);
+              float a = dot(Wi, Wi), b = dot(P - lc, Wi);
+              float cc = dot(P - lc, P - lc) - L.r * L.r;
+              float disc = b * b - a * cc;
+              float tn = disc >= 0.f ? (-b - ptm_sqrt(disc)) / a : 0.f;
+              tmax = tn * (1.f - 1e-4f);
+            }
+            pl = light_pdf(L, P, Wi);
+            Le = v3(L.ex, L.ey, L.ez);
+          } else {
+            float u1 = rnd(st.x);
+            float u2 = rnd(st.x);
+            Wi = env_sample_dir(S, u1, u2);
+            pl = env_pdf_dir(S, Wi);
+            Le = miss_color(S.miss, Wi);
+          }
+          V3 wi_n = normalize(Wi);
+          float cs = dot(wi_n, N);
+          float pls = pl / (float)n_sel;
+          if (cs > 0.f && pls > 0.f && tmax > 1e-3f) {
+            V3 wi_l = fr.to_local(wi_n);
+            V3 f = bsdf_f_c(m, wo_l, wi_l);
+            float pbs = bsdf_pdf_c(m, wo_l, wi_l);
+            V3 cv = f * Le * (cs * power_mis(pls, pbs) / pls);
+            if (!isNull(cv)) {
+              shadow = true;
+              C = thr * cv;
+            }
+          }
+        }
+        V3 wi_l = bsdf_sample_c(m, wo_l, st.x);
+        float pbs = bsdf_pdf_c(m, wo_l, wi_l);
+        V3 f = bsdf_f_c(m, wo_l, wi_l);
+        if (!(pbs > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
+          ended = true;
+        } else {
+          thr *= f * (wi_l.y / pbs);
+          prev_spec = false;
+          pdf_prev = pbs;
+          dcont = fr.to_world(wi_l);
+        }
+      }
+      if (!ended) {
+        if (pc.rr_enable && (int)depth > pc.rr_depth) {
+          float q = fminf(1.f, max_component(thr));
+          if (rnd(st.x) >= q) ended = true;
+          else thr *= 1.f / q;
+        }
+        if (!ended) {
+          depth++;
+          if ((int)depth >= pc.max_depth) ended = true;
+        }
+      }
+      st.z = (st.z & PT_ST_KEEP_MASK) | depth | ((uint32_t)prev_spec << PT_ST_SPEC_BIT);
+      st.w = __float_as_uint(pdf_prev);
+    }
+  }
+  uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
+  if (shadow) {
+    W.sh.P[spos] = make_float4(P.x, P.y, P.z, 0.f);
+    W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
+    W.sh.C[spos] = make_float4(C.x, C.y, C.z, tmax);
+    W.sh.Wo[spos] = make_float4(dcont.x, dcont.y, dcont.z, ended ? 1.f : 0.f);
+    W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    W.sh.st[spos] = st;
+  }
+  if (active && !shadow && ended) finalize_path(W, st.y, rad);
+  path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended);
+}
+
+template <bool BATCH, bool SORT>
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S0, WaveState W,
                                                             const WaveCtl* __restrict__ ctlp,
                                                             BatchRefs br) {
+  __shared__ SortTile tile;
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
-  const PathBuf& pb = W.path[c.parity];
-  uint32_t stride = gridDim.x * blockDim.x;
-  uint32_t iters = (n + stride - 1) / stride;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (uint32_t it = 0; it < iters; it++, i += stride) {
-    bool active = i < n;
-    uint4 st = make_uint4(0, 0, 0, 0);
-    V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), Wi = v3(0.f), dcont = v3(0.f), C = v3(0.f);
-    float tmax = 0.f;
-    bool ended = false, shadow = false;
-    if (active) st = pb.st[i];
-    const DevScene& S = path_scene<BATCH>(S0, br, st.z);
-    const int n_sel = S.num_lights + (S.env_valid ? 1 : 0);
-    if (active) {
-      const PathCtl pc = path_ctl<BATCH>(ctl, br, st.z);
-      thr = f4xyz(pb.thr[i]);
-      rad = f4xyz(pb.rad[i]);
-      float4 hit = W.hit[i];
-      float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
-      V3 d = f4xyz(rdv);
-      uint32_t depth = st.z & PT_ST_DEPTH_MASK;
-      // a camera ray counts as a specular bounce: emission it sees is not MIS-weighted
-      bool prev_spec = ((st.z >> PT_ST_SPEC_BIT) & 1u) || depth == 0;
-      float pdf_prev = __uint_as_float(st.w);
-      uint32_t leaf = __float_as_uint(hit.w);
-      if (leaf == PT_NO_HIT) {
-        V3 Le = miss_color(S.miss, d);
-        float w = 1.f;
-        if (!prev_spec && S.env_valid) w = power_mis(pdf_prev, env_pdf_dir(S, d) / (float)n_sel);
-        rad += thr * Le * w;
-        ended = true;
-      } else {
-        PrimRec p = load_prim(S.prims, leaf);
-        HitRecord rec = hit_record(S, p, f4xyz(ro), d, hit.x, hit.y, hit.z, false);
-        GpuMaterial m = S.mats[rec.index];
-        P = rec.P;
-        V3 Wo = rec.Wo, N = rec.shading_normal;
-        if (m.type == PT_MAT_DIFFUSE_LIGHT) {
-          float w = 1.f;
-          if (!prev_spec && n_sel > 0) w = power_mis(pdf_prev, lights_pdf_c(S, f4xyz(ro), d, n_sel));
-          rad += thr * v3(m.c0x, m.c0y, m.c0z) * w;
-          ended = true;
-        } else if (m.type == PT_MAT_METAL) {  // programs/materials/metal.cu:38-56
-          V3 reflected = reflect(-Wo, N);
-          dcont = reflected + m.p0 * random_in_unit_sphere(st.x);
-          thr *= v3(m.c0x, m.c0y, m.c0z);
-          prev_spec = true;
-        } else if (m.type == PT_MAT_DIELECTRIC) {  // programs/materials/dielectric.cu:46-96
-          float ref_idx = m.p0;
-          V3 Wd = -rec.Wo, Nd = N;
-          float ni_over_nt;
-          float cosine = dot(Wd, Nd);
-          if (cosine > 0.f) {
-            Nd = -Nd;
-            ni_over_nt = ref_idx;
-            cosine = ref_idx * cosine / length(Wd);
-          } else {
-            ni_over_nt = 1.f / ref_idx;
-            cosine = -cosine / length(Wd);
-          }
-          V3 refracted = v3(0.f);
-          float reflect_prob;
-          if (Refract(Wd, Nd, ni_over_nt, refracted)) reflect_prob = schlick(cosine, ref_idx);
-          else reflect_prob = 1.f;
-          if (rnd(st.x) < reflect_prob) dcont = reflect(Wd, Nd);
-          else dcont = normalize(refracted);
-          thr *= (v3(m.c0x, m.c0y, m.c0z) * v3(1.f));
-          prev_spec = true;
-        } else {
-          Frame fr(N);
-          V3 wo_l = fr.to_local(Wo);
-          if (n_sel > 0) {
-            int k = (int)(rnd(st.x) * (float)n_sel);
-            if (k > n_sel - 1) k = n_sel - 1;
-            float pl = 0.f;
-            V3 Le;
-            tmax = PT_RAY_TMAX;
-            if (k < S.num_lights) {
-              GpuLight L = S.lights[k];
-              if (L.type == PT_LIGHT_RECT) {
-                Wi = light_sample(L, P, st.x);
-                tmax = 1.f - 1e-4f;
-              } else {
-                Wi = sphere_light_sample_c(L, P, st.x);
-                V3 lc = v3(L.cx, L.cy, L.cz);
-                float a = dot(Wi, Wi), b = dot(P - lc, Wi);
-                float cc = dot(P - lc, P - lc) - L.r * L.r;
-                float disc = b * b - a * cc;
-                float tn = disc >= 0.f ? (-b - ptm_sqrt(disc)) / a : 0.f;
-                tmax = tn * (1.f - 1e-4f);
-              }
-              pl = light_pdf(L, P, Wi);
-              Le = v3(L.ex, L.ey, L.ez);
-            } else {
-              float u1 = rnd(st.x);
-              float u2 = rnd(st.x);
-              Wi = env_sample_dir(S, u1, u2);
-              pl = env_pdf_dir(S, Wi);
-              Le = miss_color(S.miss, Wi);
-            }
-            V3 wi_n = normalize(Wi);
-            float cs = dot(wi_n, N);
-            float pls = pl / (float)n_sel;
-            if (cs > 0.f && pls > 0.f && tmax > 1e-3f) {
-              V3 wi_l = fr.to_local(wi_n);
-              V3 f = bsdf_f_c(m, wo_l, wi_l);
-              float pbs = bsdf_pdf_c(m, wo_l, wi_l);
-              V3 cv = f * Le * (cs * power_mis(pls, pbs) / pls);
-              if (!isNull(cv)) {
-                shadow = true;
-                C = thr * cv;
-              }
-            }
-          }
-          V3 wi_l = bsdf_sample_c(m, wo_l, st.x);
-          float pbs = bsdf_pdf_c(m, wo_l, wi_l);
-          V3 f = bsdf_f_c(m, wo_l, wi_l);
-          if (!(pbs > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
-            ended = true;
-          } else {
-            thr *= f * (wi_l.y / pbs);
-            prev_spec = false;
-            pdf_prev = pbs;
-            dcont = fr.to_world(wi_l);
-          }
-        }
-        if (!ended) {
-          if (pc.rr_enable && (int)depth > pc.rr_depth) {
-            float q = fminf(1.f, max_component(thr));
-            if (rnd(st.x) >= q) ended = true;
-            else thr *= 1.f / q;
-          }
-          if (!ended) {
-            depth++;
-            if ((int)depth >= pc.max_depth) ended = true;
-          }
-        }
-        st.z = (st.z & PT_ST_KEEP_MASK) | depth | ((uint32_t)prev_spec << PT_ST_SPEC_BIT);
-        st.w = __float_as_uint(pdf_prev);
-      }
-    }
-    uint32_t spos = warp_push(&W.ctr->n_shadow, shadow);
-    if (shadow) {
-      W.sh.P[spos] = make_float4(P.x, P.y, P.z, 0.f);
-      W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
-      W.sh.C[spos] = make_float4(C.x, C.y, C.z, tmax);
-      W.sh.Wo[spos] = make_float4(dcont.x, dcont.y, dcont.z, ended ? 1.f : 0.f);
-      W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
-      W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
-      W.sh.st[spos] = st;
-    }
-    if (active && !shadow && ended) finalize_path(W, st.y, rad);
-    path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended);
-  }
+  SHADE_LOOP(shade_c_path<BATCH>(S0, W, c, ctl, br, i, i < n))
 }
 
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveState W,
@@ -1391,7 +1478,7 @@ int wave_grid(int kind, int max_stack, int block) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace_t<TRACE_EXT, false, false>,
                                                       block, trace_smem(max_stack, block));
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false>, block, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false, true>, block, 0);
   if (e != cudaSuccess || blocks < 1) {
     cudaGetLastError();
     blocks = 1;
@@ -1403,6 +1490,7 @@ LaunchCfg default_launch(int max_stack) {
   LaunchCfg lc;
   lc.trace_block = PT_TRACE_BLOCK;
   lc.shade_block = PT_SHADE_BLOCK;
+  lc.sort = 1;
   lc.trace_grid = wave_grid(0, max_stack, lc.trace_block);
   lc.shade_grid = wave_grid(1, max_stack, lc.shade_block);
   return lc;
@@ -1460,10 +1548,13 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
   else
     k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
-  if (mode == 1)
-    k_shade_c<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
-  else
-    k_shade<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  if (mode == 1) {
+    if (lc.sort) k_shade_c<BATCH, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade_c<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  } else {
+    if (lc.sort) k_shade<BATCH, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  }
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
   if (counters)
     k_trace_t<TRACE_SHADOW, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);

@@ -39,7 +39,8 @@ class PtError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("path_slots", ctypes.c_int),
                 ("enable_counters", ctypes.c_int), ("enable_timing", ctypes.c_int),
-                ("bvh_builder", ctypes.c_int), ("bvh_width", ctypes.c_int)]
+                ("bvh_builder", ctypes.c_int), ("bvh_width", ctypes.c_int),
+                ("shade_order", ctypes.c_int)]
 
 
 class RenderParams(ctypes.Structure):
@@ -66,7 +67,8 @@ class BatchItem(ctypes.Structure):
 class Tune(ctypes.Structure):
     _fields_ = [("path_slots", ctypes.c_int), ("trace_block", ctypes.c_int),
                 ("shade_block", ctypes.c_int), ("bvh_width", ctypes.c_int),
-                ("chunk_paths", ctypes.c_int), ("sample_paths_per_s", ctypes.c_double)]
+                ("chunk_paths", ctypes.c_int), ("shade_order", ctypes.c_int),
+                ("sample_paths_per_s", ctypes.c_double)]
 
 
 _F3 = ctypes.c_float * 3
@@ -300,10 +302,10 @@ class GpuRenderer:
     """One pt_context with a committed scene."""
 
     def __init__(self, scene, device=0, path_slots=0, counters=False, timing=False, builder=0,
-                 bvh_width=0):
+                 bvh_width=0, shade_order=0):
         self.lib = load_library()
         opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, builder,
-                      bvh_width)
+                      bvh_width, shade_order)
         ctx = _P()
         rc = self.lib.pt_context_create(ctypes.byref(opt), ctypes.byref(ctx))
         if rc != 0:
@@ -435,9 +437,11 @@ class Batch:
     """A pt_batch: many committed scenes (GpuRenderer contexts) rendered in
     one wavefront."""
 
-    def __init__(self, device=0, path_slots=0, counters=False, timing=False, bvh_width=0):
+    def __init__(self, device=0, path_slots=0, counters=False, timing=False, bvh_width=0,
+                 shade_order=0):
         self.lib = load_library()
-        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, 0, bvh_width)
+        opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, 0, bvh_width,
+                      shade_order)
         b = _P()
         rc = self.lib.pt_batch_create(ctypes.byref(opt), ctypes.byref(b))
         if rc != 0:
@@ -481,8 +485,9 @@ class Batch:
         self._c(self.lib.pt_batch_autotune(self.b, arr, len(jobs), ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in Tune._fields_}
 
-    def set_tune(self, path_slots, trace_block, shade_block, bvh_width, chunk_paths=0):
-        t = Tune(path_slots, trace_block, shade_block, bvh_width, chunk_paths, 0.0)
+    def set_tune(self, path_slots, trace_block, shade_block, bvh_width, chunk_paths=0,
+                 shade_order=0):
+        t = Tune(path_slots, trace_block, shade_block, bvh_width, chunk_paths, shade_order, 0.0)
         self._c(self.lib.pt_batch_set_tune(self.b, ctypes.byref(t)))
 
     def tune(self):

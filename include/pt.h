@@ -186,6 +186,16 @@ PT_API int pt_commit(pt_context* ctx);
 PT_API int pt_render(pt_context* ctx, const pt_render_params* params, float* accum_rgba,
                      void* stream);
 
+/* pt_render with per-pixel sums in double precision: accum_rgba holds 4
+ * doubles per pixel (W*H*4, host or device memory, 16-byte aligned), the same
+ * layout and frame order as pt_render's float4 accumulator; each path's
+ * float colour is widened and added in frame order.  For long progressive
+ * renders (beyond about 4096 frames float sums drop the low bits of each new
+ * frame).  No counterpart in the reference (its acc_buffer is float4,
+ * host_includes/buffers.hpp:13-18). */
+PT_API int pt_render_accum64(pt_context* ctx, const pt_render_params* params,
+                             double* accum_rgba, void* stream);
+
 /* Per-path colour of one frame (W*H*3 floats, row y*W+x, not flipped): the
  * value renderPixel adds to the accumulator, for parity checks. */
 PT_API int pt_render_paths(pt_context* ctx, const pt_render_params* params, float* out_rgb,
@@ -215,6 +225,38 @@ PT_API int pt_get_stats(pt_context* ctx, pt_stats* out);
  * (cudaGetSymbolAddress); make it before any stream capture. */
 PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params* params, float* accum_rgba,
                              void* stream);
+
+/* ---- learned sampling guide ----------------------------------------------
+ * No counterpart in the reference.  A small MLP (BF16 tensor-core kernels,
+ * FP32 accumulation) maps the encoded shading point (position in the scene
+ * box, normal, outgoing direction: 76 features) through 4 hidden layers of 64
+ * to a mixture of 8 von Mises-Fisher lobes and the probability of sampling it
+ * instead of the BSDF; consistent-mode renders with params.guide = 1 sample
+ * their bounces from alpha * guide + (1 - alpha) * BSDF (one-sample MIS, so
+ * the estimate stays unbiased) and train the network online on the radiance
+ * they carry back.  Parameters: PT_GUIDE_PARAMS floats, five row-major
+ * [rows x 80] matrices (W1..W4: 64 rows, W5: 48 rows) whose column 76 (W1)
+ * or 64 (W2..W5) is the bias; padding entries are kept 0.
+ * Samples: PT_GUIDE_SAMPLE_FLOATS floats each: position, normal, outgoing
+ * direction, sampled direction (3 each), BSDF pdf of that direction, weight
+ * (F / q: the integrand over the density it was drawn from), 2 unused. */
+#define PT_GUIDE_PARAMS 24320
+#define PT_GUIDE_OUTPUTS 48
+#define PT_GUIDE_SAMPLE_FLOATS 16
+/* Seeded He-uniform initialisation; resets the Adam state. */
+PT_API int pt_guide_init(pt_context* ctx, uint64_t seed);
+PT_API int pt_guide_get_params(pt_context* ctx, float* params);
+PT_API int pt_guide_set_params(pt_context* ctx, const float* params);
+/* Scene box of the position encoding: x01 = (p - bmin) * binv. */
+PT_API int pt_guide_bounds(pt_context* ctx, float bmin[3], float binv[3]);
+/* Raw network outputs (PT_GUIDE_OUTPUTS per sample) of n samples. */
+PT_API int pt_guide_eval(pt_context* ctx, const float* samples, int n, float* outputs);
+/* Loss sum(-w log q(wi)) / sum(w) of n samples and its gradient
+ * (PT_GUIDE_PARAMS floats); no update. */
+PT_API int pt_guide_gradient(pt_context* ctx, const float* samples, int n, float* grad,
+                             float* loss);
+/* One Adam step (beta 0.9/0.99) with learning rate lr on n samples. */
+PT_API int pt_guide_train(pt_context* ctx, const float* samples, int n, float lr, float* loss);
 
 /* ---- batched multi-scene rendering ---------------------------------------
  * No counterpart in the reference (its main.cpp renders one scene per

@@ -165,6 +165,8 @@ static pt::Box prim_box(const pt_context* ctx, const HostPrim& p) {
   return b;
 }
 
+pt::Box pth::prim_bounds(const pt_context* ctx, const HostPrim& p) { return prim_box(ctx, p); }
+
 // ====================================================================== ABI ==
 extern "C" {
 
@@ -226,6 +228,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_ctl.release();
   ctx->d_results.release();
   ctx->d_acc.release();
+  ctx->d_acc64.release();
   ctx->d_tmp.release();
   ctx->d_tmpu.release();
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
@@ -890,20 +893,25 @@ int pth::check_params(pt_context* ctx, const pt_render_params* p) {
 
 extern "C" {
 
-// Render into a device accumulator.
-static int render_device(pt_context* ctx, const pt_render_params* p, float4* d_acc) {
+// Render into a device accumulator: float4 per pixel, or 4 doubles per
+// pixel when acc64.
+static int render_device(pt_context* ctx, const pt_render_params* p, void* d_acc,
+                         bool acc64 = false) {
   cudaStream_t st = ctx->stream;
   size_t WH = (size_t)p->width * p->height;
   const size_t results_cap = (size_t)1 << 27;  // 128 M paths = 2 GiB of results
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)p->spp, results_cap / WH));
   int rc = ensure_wave(ctx, (size_t)chunk * WH);
   if (rc) return rc;
-  if (p->frame0 == 0) CK(cudaMemsetAsync(d_acc, 0, WH * sizeof(float4), st));
+  if (p->frame0 == 0) CK(cudaMemsetAsync(d_acc, 0, WH * (acc64 ? 32 : 16), st));
   for (int f = 0; f < p->spp; f += chunk) {
     int frames = std::min(chunk, p->spp - f);
     rc = run_chunk(ctx, p, p->frame0 + f, frames);
     if (rc) return rc;
-    pt::launch_accumulate(ctx->d_results.p, d_acc, p->width, p->height, frames, st);
+    if (acc64)
+      pt::launch_accumulate64(ctx->d_results.p, (double*)d_acc, p->width, p->height, frames, st);
+    else
+      pt::launch_accumulate(ctx->d_results.p, (float4*)d_acc, p->width, p->height, frames, st);
     ctx->stats.kernel_launches += 1;
   }
   return PT_OK;
@@ -936,6 +944,40 @@ PT_API int pt_render(pt_context* ctx, const pt_render_params* params, float* acc
   if (rc) return rc;
   CK(cudaEventRecord(ctx->ev1, st));
   if (!dev) CK(cudaMemcpyAsync(accum_rgba, d_acc, WH * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->stats.render_ms = ms;
+  return PT_OK;
+}
+
+PT_API int pt_render_accum64(pt_context* ctx, const pt_render_params* params,
+                             double* accum_rgba, void* stream) {
+  if (!ctx) return PT_EINVAL;
+  int rc = check_params(ctx, params);
+  if (rc) return rc;
+  if (!accum_rgba) return fail(ctx, PT_EINVAL, "null accumulator");
+  if (((uintptr_t)accum_rgba & 15u) != 0)
+    return fail(ctx, PT_EINVAL, "the double accumulator must be 16-byte aligned");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
+  CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  reset_render_stats(ctx);
+  size_t WH = (size_t)params->width * params->height;
+  bool dev = is_device_ptr(accum_rgba);
+  double* d_acc = accum_rgba;
+  if (!dev) {
+    CK(ctx->d_acc64.ensure(4 * WH));
+    d_acc = ctx->d_acc64.p;
+    if (params->frame0 != 0)
+      CK(cudaMemcpyAsync(d_acc, accum_rgba, WH * 32, cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaEventRecord(ctx->ev0, st));
+  rc = render_device(ctx, params, d_acc, true);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->ev1, st));
+  if (!dev) CK(cudaMemcpyAsync(accum_rgba, d_acc, WH * 32, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));

@@ -10,6 +10,8 @@
 #include <vector>
 
 #include "../../include/pt.h"
+#include "bvh_build.h"
+#include "pt_guide.cuh"
 #include "pt_internal.h"
 
 namespace pth {
@@ -49,6 +51,24 @@ struct DevBuf {
 
 using pth::DevBuf;
 using pth::HostPrim;
+
+/* State of the learned sampling guide of a context. */
+struct GuideState {
+  bool ready = false;        // weights initialised
+  bool bounds = false;       // scene box known
+  DevBuf<float> w32, m, v;   // FP32 master weights, Adam moments (PTG_PARAMS each)
+  DevBuf<uint16_t> wbf;      // BF16 copy read by the MMAs
+  DevBuf<float> partial;     // per-CTA gradients
+  DevBuf<float> grad;        // summed gradient (tests)
+  DevBuf<float> scalars;     // [0] loss, [1] sum of sample weights
+  DevBuf<uint32_t> counters; // [0] samples in the training array, [1] failure flag
+  DevBuf<GuideSample> samples;
+  DevBuf<float> eval_out;
+  DevBuf<GuideParams> out;   // per path slot: decoded guide
+  float bmin[3] = {0, 0, 0}, binv[3] = {1, 1, 1};
+  int step = 0;
+  int grid = 0;
+};
 
 struct pt_context {
   int device = 0;
@@ -94,6 +114,7 @@ struct pt_context {
   DevBuf<WaveCtl> d_ctl;
   DevBuf<float4> d_results;
   DevBuf<float4> d_acc;
+  DevBuf<double> d_acc64;     // staging for host double accumulators
   DevBuf<float> d_tmp;
   DevBuf<uint32_t> d_tmpu;
   WaveCounters* h_ctr = nullptr;  // pinned
@@ -105,6 +126,7 @@ struct pt_context {
   std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
   int max_stack = 0;
   LaunchCfg lc{};
+  GuideState guide;
   pt_stats stats{};
 };
 
@@ -122,6 +144,11 @@ bool is_device_ptr(const void* p);
  * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
  * is present, whose code paths diverge most in a mixed warp. */
 bool sort_pays(const pt_context* ctx);
+/* Padded world box of one primitive (the BVH builders' leaf box). */
+pt::Box prim_bounds(const pt_context* ctx, const HostPrim& p);
+/* Allocates the guide's buffers and finds the scene box of its position
+ * encoding; returns a PT_ status. */
+int guide_prepare(pt_context* ctx);
 /* Render parameters valid for the context (sets ctx->err otherwise). */
 int check_params(pt_context* ctx, const pt_render_params* p);
 }  // namespace pth

@@ -1,0 +1,532 @@
+/*
+ * pt_guide.cu - tensor-core kernels of the learned sampling guide
+ * (pt_guide.cuh describes the network).  sm_103a tcgen05: operands in
+ * shared memory as 8x8 core-matrix tiles without swizzle, read through
+ * matrix descriptors; the FP32 accumulators live in tensor memory; one thread
+ * issues the MMAs and a bounded mbarrier wait hands the result to the CTA.
+ *
+ *   k_guide_infer  per wavefront iteration: hit record -> 76 features ->
+ *                  5 layers (BF16 x BF16 -> FP32) -> decoded guide per path
+ *   k_guide_grad   training: forward, loss gradient, backward over tiles of
+ *                  128 samples; each persistent CTA keeps the five weight
+ *                  gradients in tensor memory across its tiles (bias
+ *                  gradients come out of the ones column) and writes one
+ *                  partial gradient
+ *   k_guide_adam   deterministic sum of the partials, Adam on the FP32
+ *                  masters, BF16 copies for the next MMAs
+ *
+ * Layout rules (measured on GB300 by a layout probe): K-major operand, core
+ * matrices 8 rows x 16 B; descriptor LBO = byte stride between cores along K,
+ * SBO = along M/N.  MN-major operand (the transpose bit set): cores are 8
+ * K-rows x 8 contiguous M/N elements; LBO again along K, SBO along M/N.  So
+ * one activation tile serves as the K-major A of the forward MMA and as the
+ * MN-major operand of the weight-gradient MMA.
+ */
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "pt_device.cuh"
+#include "pt_guide.cuh"
+#include "pt_internal.h"
+
+using namespace ptd;
+
+namespace {
+
+// ------------------------------------------------------------ tcgen05 ------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor, no swizzle (descriptor version 1).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: BF16 A and B, FP32 D, M = 128.
+__device__ __forceinline__ uint32_t idesc(int n, int ta, int tb) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)ta << 15) | ((uint32_t)tb << 16) |
+         ((uint32_t)(n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(mbar))
+               : "memory");
+}
+
+// Bounded wait for an mbarrier phase; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 24) && !done; it++) {
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+  }
+  return done != 0;
+}
+
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// Byte offset of element (r, c) in a tile of C columns stored as 8x8 core
+// matrices: cores ordered row-group major, 128 B each, 16 B per core row.
+__device__ __forceinline__ uint32_t core_off(int r, int c, int C) {
+  return (uint32_t)(((r >> 3) * (C >> 3) + (c >> 3)) * 128 + (r & 7) * 16 + (c & 7) * 2);
+}
+
+__device__ __forceinline__ void st_bf16(unsigned char* tile, int r, int c, int C, float v) {
+  *(__nv_bfloat16*)(tile + core_off(r, c, C)) = __float2bfloat16_rn(v);
+}
+__device__ __forceinline__ float ld_bf16(const unsigned char* tile, int r, int c, int C) {
+  return __bfloat162float(*(const __nv_bfloat16*)(tile + core_off(r, c, C)));
+}
+
+// Tile sizes (bytes).
+constexpr int kTileT = 128 * PTG_K * 2;   // activation tile, 128 x 80
+constexpr int kTileW = PTG_H * PTG_K * 2; // W1..W4, 64 x 80
+constexpr int kTileW5 = PTG_NOUT * PTG_K * 2;
+constexpr int kWeights = 4 * kTileW + kTileW5;
+constexpr int kTileG = 128 * PTG_H * 2;   // gradient tile, 128 x 64
+constexpr int kGuard = 2048;              // the weight-gradient MMA reads M = 128 rows of
+                                          // a 48/64-row operand: the extra rows land here
+// TMEM columns of the training kernel: [0,64) layer accumulator, then the
+// five weight gradients, 80 columns each.
+constexpr int kTmemAcc = 0;
+constexpr int kTmemDW = 64;
+
+__device__ __forceinline__ int layer_rows(int l) { return l == 4 ? PTG_NOUT : PTG_H; }
+
+// Weights (BF16, row-major [rows][80]) into K-major core tiles.
+__device__ void load_weights(unsigned char* W, const __nv_bfloat16* __restrict__ wg) {
+  for (int l = 0; l < 5; l++) {
+    unsigned char* t = W + l * kTileW;
+    const __nv_bfloat16* src = wg + PTG_LAYER_OFF(l);
+    int n = layer_rows(l) * PTG_K;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+      int r = e / PTG_K, c = e % PTG_K;
+      *(__nv_bfloat16*)(t + core_off(r, c, PTG_K)) = src[e];
+    }
+  }
+}
+
+// Forward MMAs of layer l: acc[N] = T (128 x 80, K-major) * W_l^T.
+__device__ __forceinline__ void issue_forward(uint32_t tmem, const unsigned char* T,
+                                              const unsigned char* W, int l) {
+  const int n = layer_rows(l);
+  const uint32_t id = idesc(n, 0, 0);
+  const uint32_t ta = smem_u32(T), tw = smem_u32(W + l * kTileW);
+#pragma unroll
+  for (int ks = 0; ks < PTG_K / 16; ks++)
+    mma(tmem + kTmemAcc, sdesc(ta + ks * 256, 128, (PTG_K / 8) * 128),
+        sdesc(tw + ks * 256, 128, (PTG_K / 8) * 128), id, ks > 0 ? 1u : 0u);
+}
+
+// Row `row` of a 128 x 80 activation tile from 64 values (ReLU applied by
+// the caller), the ones column and zero padding.
+__device__ __forceinline__ void write_hidden_row(unsigned char* T, int row, const float* h) {
+  for (int c = 0; c < PTG_H; c++) st_bf16(T, row, c, PTG_K, h[c]);
+  st_bf16(T, row, PTG_H, PTG_K, 1.f);
+  for (int c = PTG_H + 1; c < PTG_K; c++) st_bf16(T, row, c, PTG_K, 0.f);
+}
+
+__device__ __forceinline__ void write_feature_row(unsigned char* T, int row, const float* f,
+                                                  bool valid) {
+  for (int c = 0; c < PTG_FEAT; c++) st_bf16(T, row, c, PTG_K, valid ? f[c] : 0.f);
+  st_bf16(T, row, PTG_FEAT, PTG_K, 1.f);
+  for (int c = PTG_FEAT + 1; c < PTG_K; c++) st_bf16(T, row, c, PTG_K, 0.f);
+}
+
+struct TmemGuard {
+  uint64_t mbar;
+  uint32_t base;
+};
+
+// Runs the 5-layer forward on T[0] (features), leaving the 48 outputs of
+// this thread's row in out[]: with nT == 5 layer l reads T[l] and writes
+// T[l+1] (training keeps every activation), with nT == 2 it ping-pongs.
+// Returns false, in every thread alike, when a wait ran out.
+__device__ bool forward_tile(uint32_t tmem, TmemGuard& g, uint32_t& phase, unsigned char* W,
+                             unsigned char* const* T, int nT, float* out) {
+  const int row = threadIdx.x;
+  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
+  for (int l = 0; l < 5; l++) {
+    const unsigned char* in = T[nT == 5 ? l : (l & 1)];
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (threadIdx.x == 0) {
+      issue_forward(tmem, in, W, l);
+      mma_commit(&g.mbar);
+    }
+    bool ok = mbar_wait(&g.mbar, phase);
+    phase ^= 1u;
+    fence_after();
+    if (!__syncthreads_and(ok)) return false;
+    if (l < 4) {
+      float h[PTG_H];
+      for (int c0 = 0; c0 < PTG_H; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, h + c0);
+      for (int c = 0; c < PTG_H; c++) h[c] = fmaxf(h[c], 0.f);
+      unsigned char* dst = T[nT == 5 ? l + 1 : ((l + 1) & 1)];
+      write_hidden_row(dst, row, h);
+    } else {
+      for (int c0 = 0; c0 < PTG_NOUT; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, out + c0);
+    }
+  }
+  return true;
+}
+
+// d(-wn log q)/d(outputs) of one sample; returns the loss term.
+__device__ float loss_grad(const float* o, float wx, float wy, float wz, float p_bsdf, float wn,
+                           float* d) {
+  for (int k = 0; k < PTG_NOUT; k++) d[k] = 0.f;
+  if (!(wn > 0.f)) return 0.f;
+  GuideParams g;
+  guide_decode(o, g);
+  float v[PTG_LOBES], pi[PTG_LOBES], cj[PTG_LOBES];
+  float pg = 0.f, prev = 0.f;
+  for (int j = 0; j < PTG_LOBES; j++) {
+    pi[j] = g.cdf[j] - prev;
+    prev = g.cdf[j];
+    cj[j] = g.lobe[j].x * wx + g.lobe[j].y * wy + g.lobe[j].z * wz;
+    v[j] = vmf_pdf(g.lobe[j].x, g.lobe[j].y, g.lobe[j].z, g.lobe[j].w, wx, wy, wz);
+    pg += pi[j] * v[j];
+  }
+  float a = g.alpha;
+  float q = a * pg + (1.f - a) * p_bsdf;
+  if (!(q > 1e-30f)) return 0.f;
+  float dq = -wn / q;  // dL/dq
+  float sig = (a - PTG_ALPHA_MIN) / PTG_ALPHA_SPAN;
+  d[40] = dq * (pg - p_bsdf) * PTG_ALPHA_SPAN * sig * (1.f - sig);
+  for (int j = 0; j < PTG_LOBES; j++) {
+    float k = g.lobe[j].w;
+    float common = dq * a * pi[j] * v[j];
+    // mixture logit
+    d[5 * j + 4] = dq * a * pi[j] * (v[j] - pg);
+    // log concentration (zero where clamped or in the uniform branch)
+    float lk = o[5 * j + 3];
+    if (lk > PTG_LOGK_MIN && lk < PTG_LOGK_MAX && k >= 1e-4f)
+      d[5 * j + 3] = common * (1.f + k * (cj[j] - 1.f) - 2.f * k / expm1f(2.f * k));
+    // mean direction through the normalisation
+    float mx = o[5 * j], my = o[5 * j + 1], mz = o[5 * j + 2];
+    float n = sqrtf(mx * mx + my * my + mz * mz);
+    if (n > 1e-12f && k >= 1e-4f) {
+      float s = common * k / n;
+      d[5 * j] = s * (wx - cj[j] * g.lobe[j].x);
+      d[5 * j + 1] = s * (wy - cj[j] * g.lobe[j].y);
+      d[5 * j + 2] = s * (wz - cj[j] * g.lobe[j].z);
+    }
+  }
+  return -wn * logf(q);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ kernels ------
+__global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ TmemGuard g;
+  bool failed = false;  // uniform across the CTA (decided by __syncthreads_and)
+  unsigned char* W = sm;
+  unsigned char* T[5];
+  for (int l = 0; l < 5; l++) T[l] = sm + kWeights + l * kTileT;
+  unsigned char* Gt = sm + kWeights + 5 * kTileT;             // dO (128 x 48) or dH (128 x 64)
+  unsigned char* Gn = Gt + kTileG + kGuard;                   // the other dH
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&g.mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&g.base)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  load_weights(W, A.w);
+  // the guard areas must hold finite numbers (their products land in
+  // ignored rows, but NaN/Inf patterns are avoided all the same)
+  for (int e = tid; e < kGuard / 4; e++) {
+    ((uint32_t*)(Gt + kTileG))[e] = 0u;
+    ((uint32_t*)(Gn + kTileG))[e] = 0u;
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = g.base;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  uint32_t phase = 0;
+  const uint32_t n = *A.count;
+  const float wsum = *A.wsum;
+  const uint32_t ntiles = (n + 127) / 128;
+  bool first = true;
+  float loss_acc = 0.f;
+  for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+    const uint32_t s = tile * 128 + tid;
+    const bool valid = s < n;
+    GuideSample smp;
+    if (valid) smp = A.samples[s];
+    float f[PTG_FEAT];
+    if (valid) guide_features(smp.P, smp.N, smp.Wo, A.bmin, A.binv, f);
+    write_feature_row(T[0], tid, f, valid);
+    float o[PTG_NOUT];
+    if (!forward_tile(tmem, g, phase, W, T, 5, o)) {
+      failed = true;
+      break;
+    }
+    if (A.out && valid)
+      for (int k = 0; k < PTG_NOUT; k++) A.out[(size_t)s * PTG_NOUT + k] = o[k];
+    if (!A.train) continue;
+    // ---- loss gradient of this row -> dO tile (128 x 48, K-major)
+    float d[PTG_NOUT];
+    float wn = valid && wsum > 0.f ? smp.weight / wsum : 0.f;
+    loss_acc += valid ? loss_grad(o, smp.wi[0], smp.wi[1], smp.wi[2], smp.p_bsdf, wn, d)
+                      : loss_grad(o, 0.f, 1.f, 0.f, 0.f, 0.f, d);
+    for (int k = 0; k < PTG_NOUT; k++) st_bf16(Gt, tid, k, PTG_NOUT, d[k]);
+    // ---- backward, layer 4 .. 0
+    unsigned char* G = Gt;
+    unsigned char* Gnext = Gn;
+    for (int l = 4; l >= 0; l--) {
+      const int rows = layer_rows(l);        // width of G (layer outputs)
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+      fence_after();
+      if (tid == 0) {
+        // dW_l += G^T T_l : A = G MN-major (M = rows, padded to 128), K = samples;
+        //                   B = T_l MN-major (N = 80), K = samples
+        const uint32_t ga = smem_u32(G), tb = smem_u32(T[l]);
+        const uint32_t gk = (rows / 8) * 128;  // G: bytes per core row (8 samples)
+        const uint32_t idw = idesc(PTG_K, 1, 1);
+        for (int ks = 0; ks < 8; ks++)
+          mma(tmem + kTmemDW + l * PTG_K, sdesc(ga + ks * 2 * gk, gk, 128),
+              sdesc(tb + ks * 2 * (PTG_K / 8) * 128, (PTG_K / 8) * 128, 128), idw,
+              (first && ks == 0) ? 0u : 1u);
+        if (l > 0) {
+          // dT_l = G * W_l[:, 0:64] : A = G K-major (K = rows); B = W_l MN-major (N = 64)
+          const uint32_t wa = smem_u32(W + l * kTileW);
+          const uint32_t idx = idesc(PTG_H, 0, 1);
+          for (int ks = 0; ks < rows / 16; ks++)
+            mma(tmem + kTmemAcc, sdesc(ga + ks * 256, 128, gk),
+                sdesc(wa + ks * 2 * (PTG_K / 8) * 128, (PTG_K / 8) * 128, 128), idx,
+                ks > 0 ? 1u : 0u);
+        }
+        mma_commit(&g.mbar);
+      }
+      bool ok = mbar_wait(&g.mbar, phase);
+      phase ^= 1u;
+      fence_after();
+      if (!__syncthreads_and(ok)) {
+        failed = true;
+        break;
+      }
+      if (l > 0) {
+        // G_{l-1} = dT_l * (T_l > 0), into the other gradient tile
+        float h[PTG_H];
+        for (int c0 = 0; c0 < PTG_H; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, h + c0);
+        for (int c = 0; c < PTG_H; c++) {
+          float t = ld_bf16(T[l], tid, c, PTG_K);
+          st_bf16(Gnext, tid, c, PTG_H, t > 0.f ? h[c] : 0.f);
+        }
+        unsigned char* tmp = G;
+        G = Gnext;
+        Gnext = tmp;
+      }
+    }
+    if (failed) break;
+    first = false;
+  }
+  // ---- per-CTA partial gradients (rows of dW live in lanes 0..rows-1)
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (A.train && A.partial) {
+    float* P = A.partial + (size_t)blockIdx.x * PTG_PARAMS;
+    for (int l = 0; l < 5; l++) {
+      const int rows = layer_rows(l);
+      if (warp * 32 >= rows) continue;
+      int row = tid;
+      float vals[PTG_K];
+      for (int c0 = 0; c0 < PTG_K; c0 += 16)
+        tmem_ld16(tmem + lane_base + kTmemDW + l * PTG_K + c0, vals + c0);
+      if (row < rows)
+        for (int c = 0; c < PTG_K; c++)
+          P[PTG_LAYER_OFF(l) + row * PTG_K + c] = (first || failed) ? 0.f : vals[c];
+    }
+  }
+  if (loss_acc != 0.f && A.loss) atomicAdd(A.loss, loss_acc);
+  if (failed) {
+    if (tid == 0) atomicOr(A.fail, 1u);
+    // give MMAs still in flight a second bounded wait before freeing TMEM
+    mbar_wait(&g.mbar, phase);
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// Sum of the per-CTA partials (fixed order) and Adam on the FP32 masters;
+// padding entries (rows 41..47 of W5, columns past the bias column) stay 0.
+__global__ void k_guide_adam(GuideAdamArgs A) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= PTG_PARAMS) return;
+  int l = p / PTG_W_LAYER;
+  int e = p - l * PTG_W_LAYER;
+  int r = e / PTG_K, c = e % PTG_K;
+  bool used = r < (l == 4 ? PTG_OUT : PTG_H) && c <= PTG_BIAS_COL(l);
+  float gsum = 0.f;
+  for (int k = 0; k < A.nparts; k++) gsum += A.partial[(size_t)k * PTG_PARAMS + p];
+  if (!used) gsum = 0.f;
+  if (A.grad_out) A.grad_out[p] = gsum;
+  if (!A.update || !used) return;
+  float m = A.b1 * A.m[p] + (1.f - A.b1) * gsum;
+  float v = A.b2 * A.v[p] + (1.f - A.b2) * gsum * gsum;
+  A.m[p] = m;
+  A.v[p] = v;
+  float w = A.w32[p] - A.lr * (m / A.bc1) / (sqrtf(v / A.bc2) + A.eps);
+  A.w32[p] = w;
+  A.wbf[p] = __float2bfloat16_rn(w);
+}
+
+// Inference inside the wavefront: one row per live path of the current
+// buffer; rows whose hit is a guided (non-delta) material get a decoded
+// guide in A.out at the path's position.
+__global__ void __launch_bounds__(128) k_guide_infer(DevScene S, WaveState W,
+                                                     const WaveCtl* __restrict__ ctlp,
+                                                     GuideInferArgs A) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ TmemGuard g;
+  bool failed = false;
+  unsigned char* Wt = sm;
+  unsigned char* T[2] = {sm + kWeights, sm + kWeights + kTileT};
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&g.mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&g.base)),
+                 "r"(64));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  load_weights(Wt, A.w);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = g.base;
+  uint32_t phase = 0;
+  const WaveCounters c = *W.ctr;
+  const WaveCtl ctl = *ctlp;
+  unsigned long long left = ctl.chunk_paths - c.next_path;
+  const uint32_t n = c.n_cur + (uint32_t)min((unsigned long long)((uint32_t)W.slots - c.n_cur), left);
+  const uint32_t ntiles = (n + 127) / 128;
+  const PathBuf& pb = W.path[c.parity];
+  for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+    const uint32_t i = tile * 128 + tid;
+    bool valid = false;
+    float f[PTG_FEAT];
+    if (i < n) {
+      float4 hit = W.hit[i];
+      uint32_t leaf = __float_as_uint(hit.w);
+      if (leaf != PT_NO_HIT) {
+        PrimRec p = load_prim(S.prims, leaf);
+        int type = S.mats[prim_material(p)].type;
+        if (type == PT_MAT_LAMBERTIAN || type == PT_MAT_OREN_NAYAR ||
+            type == PT_MAT_TORRANCE_SPARROW || type == PT_MAT_ASHIKHMIN_SHIRLEY) {
+          float4 ro = pb.ray_o[i], rd = pb.ray_d[i];
+          HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rd), hit.x, hit.y, hit.z, false);
+          float P[3] = {rec.P.x, rec.P.y, rec.P.z};
+          float N[3] = {rec.shading_normal.x, rec.shading_normal.y, rec.shading_normal.z};
+          float Wo[3] = {rec.Wo.x, rec.Wo.y, rec.Wo.z};
+          guide_features(P, N, Wo, A.bmin, A.binv, f);
+          valid = true;
+        }
+      }
+    }
+    write_feature_row(T[0], tid, f, valid);
+    float o[PTG_NOUT];
+    if (!forward_tile(tmem, g, phase, Wt, T, 2, o)) {
+      failed = true;
+      break;
+    }
+    if (valid) {
+      GuideParams gp;
+      guide_decode(o, gp);
+      A.out[i] = gp;
+    }
+  }
+  if (failed) {
+    if (tid == 0) atomicOr(A.fail, 1u);
+    mbar_wait(&g.mbar, phase);
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
+}
+
+// ------------------------------------------------------------ launchers ----
+namespace pt {
+
+size_t guide_train_smem() { return (size_t)kWeights + 5 * kTileT + 2 * (kTileG + kGuard); }
+size_t guide_infer_smem() { return (size_t)kWeights + 2 * kTileT; }
+
+cudaError_t guide_set_smem() {
+  cudaError_t e = cudaFuncSetAttribute(k_guide_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)guide_train_smem());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)guide_infer_smem());
+}
+
+void launch_guide_grad(const GuideTrainArgs& a, int grid, cudaStream_t st) {
+  k_guide_grad<<<grid, 128, guide_train_smem(), st>>>(a);
+}
+
+void launch_guide_adam(const GuideAdamArgs& a, cudaStream_t st) {
+  k_guide_adam<<<(PTG_PARAMS + 255) / 256, 256, 0, st>>>(a);
+}
+
+void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
+                        const GuideInferArgs& a, int grid, cudaStream_t st) {
+  k_guide_infer<<<grid, 128, guide_infer_smem(), st>>>(S, W, ctl, a);
+}
+
+}  // namespace pt

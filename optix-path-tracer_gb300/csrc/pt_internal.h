@@ -181,6 +181,9 @@ void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, d
                     int* valid, cudaStream_t st);
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
                        cudaStream_t st);
+/* acc: 4 doubles per pixel (16-byte aligned) */
+void launch_accumulate64(const float4* results, double* acc, int w, int h, int frames,
+                         cudaStream_t st);
 void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st);
 void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
                        float* t, int max_stack, uint32_t* err, cudaStream_t st);

@@ -1386,6 +1386,28 @@ __global__ void k_accumulate(const float4* __restrict__ results, float4* acc, in
   }
 }
 
+// The same accumulation into double sums (acc holds 4 doubles per pixel):
+// for renders beyond a few thousand frames, where float sums of per-frame
+// values lose the low bits of each new frame.
+__global__ void k_accumulate64(const float4* __restrict__ results, double2* acc, int width,
+                               int height, int frames) {
+  uint32_t WH = (uint32_t)width * (uint32_t)height;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < WH; p += gridDim.x * blockDim.x) {
+    uint32_t x = p % (uint32_t)width, y = p / (uint32_t)width;
+    size_t o = (size_t)(height - 1 - y) * width + x;
+    double2 a0 = acc[2 * o], a1 = acc[2 * o + 1];
+    for (int f = 0; f < frames; f++) {
+      float4 r = results[(size_t)f * WH + p];
+      a0.x += (double)r.x;
+      a0.y += (double)r.y;
+      a1.x += (double)r.z;
+      a1.y += 1.0;
+    }
+    acc[2 * o] = a0;
+    acc[2 * o + 1] = a1;
+  }
+}
+
 __global__ void k_paths_out(const float4* __restrict__ results, float* out, uint32_t n) {
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     float4 r = results[p];
@@ -1607,6 +1629,11 @@ void launch_relocate(uint4* nodes, size_t n_nodes, uint32_t node_off, uint32_t p
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
                        cudaStream_t st) {
   k_accumulate<<<num_sms() * 8, 256, 0, st>>>(results, acc, w, h, frames);
+}
+
+void launch_accumulate64(const float4* results, double* acc, int w, int h, int frames,
+                         cudaStream_t st) {
+  k_accumulate64<<<num_sms() * 8, 256, 0, st>>>(results, (double2*)acc, w, h, frames);
 }
 
 void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st) {

@@ -22,7 +22,8 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
     "-I", CSRC,
 ]
-SOURCES = ["pt_kernels.cu", "pt_api.cu", "pt_batch.cu", "bvh_host.cpp", "bvh_gpu.cu"]
+SOURCES = ["pt_kernels.cu", "pt_api.cu", "pt_batch.cu", "pt_guide.cu", "pt_guide_host.cu", "bvh_host.cpp",
+           "bvh_gpu.cu"]
 
 
 def _nvcc():

@@ -104,10 +104,18 @@ SIGNATURES = {
     "pt_commit": [_P],
     "pt_render": [_P, ctypes.POINTER(RenderParams), _P, _P],
     "pt_render_paths": [_P, ctypes.POINTER(RenderParams), _P, _P],
+    "pt_render_accum64": [_P, ctypes.POINTER(RenderParams), _P, _P],
     "pt_trace_first_hits": [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P],
     "pt_resolve_display": [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P],
     "pt_get_stats": [_P, ctypes.POINTER(Stats)],
     "pt_render_noalloc": [_P, ctypes.POINTER(RenderParams), _P, _P],
+    "pt_guide_init": [_P, ctypes.c_uint64],
+    "pt_guide_get_params": [_P, _P],
+    "pt_guide_set_params": [_P, _P],
+    "pt_guide_bounds": [_P, _P, _P],
+    "pt_guide_eval": [_P, _P, ctypes.c_int, _P],
+    "pt_guide_gradient": [_P, _P, ctypes.c_int, _P, _P],
+    "pt_guide_train": [_P, _P, ctypes.c_int, ctypes.c_float, _P],
     "pt_batch_create": [ctypes.POINTER(Options), ctypes.POINTER(_P)],
     "pt_batch_destroy": [_P],
     "pt_batch_render": [_P, ctypes.POINTER(BatchItem), ctypes.c_int, _P],
@@ -400,6 +408,54 @@ class GpuRenderer:
         ptr = acc if isinstance(acc, int) else _ptr(acc)
         self._c(self.lib.pt_render(self.ctx, ctypes.byref(params), ptr, stream))
         return acc
+
+    def render64(self, params, acc=None, stream=None):
+        """Accumulates into acc (numpy float64 HxWx4, or a device pointer int)."""
+        if acc is None:
+            acc = np.zeros((params.height, params.width, 4), dtype=np.float64)
+        ptr = acc if isinstance(acc, int) else _ptr(acc)
+        self._c(self.lib.pt_render_accum64(self.ctx, ctypes.byref(params), ptr, stream))
+        return acc
+
+    # ---- learned guide
+    GUIDE_PARAMS = 24320
+
+    def guide_init(self, seed=0):
+        self._c(self.lib.pt_guide_init(self.ctx, seed))
+
+    def guide_params(self):
+        out = np.zeros(self.GUIDE_PARAMS, np.float32)
+        self._c(self.lib.pt_guide_get_params(self.ctx, _ptr(out)))
+        return out
+
+    def guide_set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._c(self.lib.pt_guide_set_params(self.ctx, _ptr(w)))
+
+    def guide_bounds(self):
+        bmin = np.zeros(3, np.float32)
+        binv = np.zeros(3, np.float32)
+        self._c(self.lib.pt_guide_bounds(self.ctx, _ptr(bmin), _ptr(binv)))
+        return bmin, binv
+
+    def guide_eval(self, samples):
+        s = np.ascontiguousarray(samples, dtype=np.float32)
+        out = np.zeros((len(s), 48), np.float32)
+        self._c(self.lib.pt_guide_eval(self.ctx, _ptr(s), len(s), _ptr(out)))
+        return out
+
+    def guide_gradient(self, samples):
+        s = np.ascontiguousarray(samples, dtype=np.float32)
+        g = np.zeros(self.GUIDE_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._c(self.lib.pt_guide_gradient(self.ctx, _ptr(s), len(s), _ptr(g), _ptr(loss)))
+        return g, float(loss[0])
+
+    def guide_train(self, samples, lr=1e-2):
+        s = np.ascontiguousarray(samples, dtype=np.float32)
+        loss = np.zeros(1, np.float32)
+        self._c(self.lib.pt_guide_train(self.ctx, _ptr(s), len(s), lr, _ptr(loss)))
+        return float(loss[0])
 
     def render_paths(self, params, out=None):
         if out is None:

@@ -220,3 +220,42 @@ def test_material_sorted_shading_keeps_results(cases, ptgb_mod, name, mode):
     assert np.array_equal(unsorted.render(prm), ref)
     srt.close()
     unsorted.close()
+
+
+def test_double_accumulation(cases, ptgb_mod):
+    """pt_render_accum64: per-pixel sums in double, frame order.  Equals the
+    host's double sum of the per-frame path colours exactly, carries the same
+    counts as the float accumulator, and continues progressively."""
+    g, _, w, h, kw = cases["zoo"]
+    frames = [g.render_paths(ptgb_mod.GpuRenderer.params(w, h, 1, frame0=f, **kw))
+              for f in range(5)]
+    ref = np.zeros((h, w, 3), np.float64)
+    for fr in frames:
+        ref += fr.astype(np.float64)
+    ref = ref[::-1]                           # accumulator rows are y-flipped
+    acc = g.render64(ptgb_mod.GpuRenderer.params(w, h, 3, **kw))
+    acc = g.render64(ptgb_mod.GpuRenderer.params(w, h, 2, frame0=3, **kw), acc)
+    assert np.array_equal(acc[..., :3], ref)
+    assert np.all(acc[..., 3] == 5.0)
+    f32 = g.render(ptgb_mod.GpuRenderer.params(w, h, 5, **kw))
+    assert np.abs(f32[..., :3] - acc[..., :3]).max() <= 1e-5 * max(1.0, np.abs(ref).max())
+
+
+def test_double_accumulation_many_frames(ptgb_mod):
+    """6000 frames (beyond where float sums drop low bits): the double sums
+    of one call equal those of three progressive calls bit for bit (the same
+    additions in the same frame order), the counts are exact, and the mean
+    agrees with the float accumulator's to float accuracy."""
+    g = ptgb_mod.GpuRenderer(ptgb_mod.cornell_c1(8, 8))
+    P = ptgb_mod.GpuRenderer.params
+    n = 6000
+    one = g.render64(P(8, 8, n, rr_depth=3))
+    acc = g.render64(P(8, 8, 2000, rr_depth=3))
+    acc = g.render64(P(8, 8, 2000, frame0=2000, rr_depth=3), acc)
+    acc = g.render64(P(8, 8, 2000, frame0=4000, rr_depth=3), acc)
+    assert np.array_equal(one, acc)
+    assert np.all(one[..., 3] == n)
+    a32 = g.render(P(8, 8, n, rr_depth=3))
+    m64, m32 = one[..., :3] / n, a32[..., :3].astype(np.float64) / n
+    assert np.abs(m64 - m32).max() <= 1e-3 * max(1.0, m64.max())
+    g.close()

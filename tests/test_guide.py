@@ -1,0 +1,177 @@
+"""The learned sampling guide's tensor-core kernels against a float64
+reference: forward outputs and loss gradients (BF16 inputs and stored
+activations on both sides, FP32 tensor-core accumulation on the GPU), and
+Adam steps that lower the loss."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+P_LAYERS = [(64, 76), (64, 64), (64, 64), (64, 64), (41, 64)]  # (rows used, inputs)
+K = 80
+ALPHA_MIN, ALPHA_SPAN, LOGK_MIN, LOGK_MAX = 0.05, 0.9, -6.0, 9.0
+
+
+def layer_off(l):
+    return l * 64 * K
+
+
+def bf16(x, torch):
+    return x.to(torch.bfloat16).to(torch.float64)
+
+
+def features(P, N, Wo, bmin, binv):
+    """The kernels' feature encoding in float32 (the same operation order)."""
+    P, N, Wo = (np.asarray(a, np.float32) for a in (P, N, Wo))
+    x = np.clip((P - bmin) * binv, np.float32(0), np.float32(1)).astype(np.float32)
+    n = len(P)
+    f = np.zeros((n, 76), np.float32)
+    s = np.sin(np.pi * x.astype(np.float64)).astype(np.float32)
+    c = np.cos(np.pi * x.astype(np.float64)).astype(np.float32)
+    two, one = np.float32(2), np.float32(1)
+    for k in range(12):
+        for a in range(3):
+            f[:, a * 24 + 2 * k] = s[:, a]
+            f[:, a * 24 + 2 * k + 1] = c[:, a]
+        s, c = (two * s * c).astype(np.float32), (one - two * s * s).astype(np.float32)
+    for q, d in enumerate((N, Wo)):
+        y = np.clip(d[:, 1], -1, 1)
+        f[:, 72 + 2 * q] = np.arccos(y).astype(np.float32) * np.float32(0.31830988618379067)
+        f[:, 73 + 2 * q] = (np.arctan2(d[:, 2], d[:, 0]).astype(np.float32) *
+                            np.float32(0.15915494309189535) + np.float32(0.5))
+    return f
+
+
+def reference(torch, params, samples, bmin, binv, train=True):
+    """Forward (and loss) in float64 with the GPU's BF16 rounding points;
+    returns outputs [n, 41], loss, and the gradient in the parameter layout."""
+    s = samples
+    f = torch.tensor(features(s[:, 0:3], s[:, 3:6], s[:, 6:9], bmin, binv), dtype=torch.float64)
+    n = len(s)
+    x = torch.zeros((n, K), dtype=torch.float64)
+    x[:, :76] = bf16(f, torch)
+    x[:, 76] = 1.0
+    Ws = []
+    for l, (rows, fan) in enumerate(P_LAYERS):
+        w = torch.tensor(params[layer_off(l):layer_off(l) + (48 if l == 4 else 64) * K],
+                         dtype=torch.float64).reshape(-1, K)[:rows]
+        w = bf16(w, torch).clone().requires_grad_(True)
+        Ws.append(w)
+    h = x
+    for l in range(4):
+        z = h @ Ws[l].t()
+        a = torch.relu(z)
+        a = a + (bf16(a, torch) - a).detach()       # stored as BF16 (straight through)
+        h = torch.cat([a, torch.ones((n, 1), dtype=torch.float64),
+                       torch.zeros((n, K - 65), dtype=torch.float64)], dim=1)
+    o = h @ Ws[4].t()                                # [n, 41]
+    wi = torch.tensor(s[:, 9:12], dtype=torch.float64)
+    pb = torch.tensor(s[:, 12], dtype=torch.float64)
+    w = torch.tensor(s[:, 13], dtype=torch.float64)
+    m = o[:, :40].reshape(n, 8, 5)
+    mu = m[:, :, 0:3] / torch.linalg.norm(m[:, :, 0:3], dim=2, keepdim=True)
+    kap = torch.exp(torch.clamp(m[:, :, 3], LOGK_MIN, LOGK_MAX))
+    pi = torch.softmax(m[:, :, 4], dim=1)
+    c = (mu * wi[:, None, :]).sum(2)
+    v = kap / (2 * np.pi * -torch.expm1(-2 * kap)) * torch.exp(kap * (c - 1))
+    pg = (pi * v).sum(1)
+    alpha = ALPHA_MIN + ALPHA_SPAN * torch.sigmoid(o[:, 40])
+    q = alpha * pg + (1 - alpha) * pb
+    loss = -(w * torch.log(q)).sum() / w.sum()
+    grad = None
+    if train:
+        loss.backward()
+        grad = np.zeros(24320)
+        for l, (rows, fan) in enumerate(P_LAYERS):
+            gl = Ws[l].grad.numpy()
+            for r in range(rows):
+                grad[layer_off(l) + r * K: layer_off(l) + r * K + K] = gl[r]
+            # only used columns carry gradient (features/activations + bias)
+            bias_col = 76 if l == 0 else 64
+            for r in range(rows):
+                grad[layer_off(l) + r * K + bias_col + 1: layer_off(l) + (r + 1) * K] = 0
+    return o.detach().numpy(), float(loss.detach()), grad
+
+
+def random_samples(rng, n, bmin, binv):
+    lo = bmin
+    ext = 1.0 / binv
+    P = lo + rng.random((n, 3)) * ext
+    def unit(k):
+        d = rng.normal(size=(k, 3))
+        return d / np.linalg.norm(d, axis=1, keepdims=True)
+    N = unit(n)
+    Wo = unit(n)
+    wi = unit(n)
+    s = np.zeros((n, 16), np.float32)
+    s[:, 0:3], s[:, 3:6], s[:, 6:9], s[:, 9:12] = P, N, Wo, wi
+    s[:, 12] = 0.02 + rng.random(n) * 0.3
+    s[:, 13] = np.exp(rng.normal(size=n))
+    return s
+
+
+@pytest.fixture(scope="module")
+def guide(ptgb_mod):
+    torch = pytest.importorskip("torch")
+    g = ptgb_mod.GpuRenderer(ptgb_mod.material_zoo(32, 24))
+    g.guide_init(7)
+    # a livelier network than the initialisation (larger last layer)
+    w = g.guide_params()
+    w[layer_off(4):] *= 8.0
+    g.guide_set_params(w)
+    yield g, torch
+    g.close()
+
+
+def test_forward_matches_reference(guide):
+    g, torch = guide
+    bmin, binv = g.guide_bounds()
+    s = random_samples(np.random.default_rng(1), 1000, bmin, binv)
+    out = g.guide_eval(s)
+    ref, _, _ = reference(torch, g.guide_params(), s, bmin, binv, train=False)
+    err = np.abs(out[:, :41] - ref)
+    scale = np.abs(ref).max()
+    assert np.median(err) <= 2e-3 * scale
+    assert err.max() <= 5e-2 * scale, err.max() / scale
+    assert np.all(out[:, 41:] == 0)
+
+
+def test_gradient_matches_reference(guide):
+    g, torch = guide
+    bmin, binv = g.guide_bounds()
+    s = random_samples(np.random.default_rng(2), 3000, bmin, binv)  # several tiles and CTAs
+    grad, loss = g.guide_gradient(s)
+    _, rloss, rgrad = reference(torch, g.guide_params(), s, bmin, binv)
+    assert abs(loss - rloss) <= 1e-2 * max(1.0, abs(rloss))
+    for l in range(5):
+        a = grad[layer_off(l):layer_off(l + 1) if l < 4 else None]
+        b = rgrad[layer_off(l):layer_off(l + 1) if l < 4 else None]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        cos = float(a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30))
+        assert rel <= 5e-2 and cos >= 0.998, (l, rel, cos)
+
+
+def test_training_lowers_loss(ptgb_mod):
+    """Directions drawn from a position-dependent lobe: Adam steps with the
+    benchmark's learning rate must fit it (the loss falls well below the
+    uniform-mixture loss)."""
+    pytest.importorskip("torch")
+    g = ptgb_mod.GpuRenderer(ptgb_mod.material_zoo(32, 24))
+    g.guide_init(3)
+    bmin, binv = g.guide_bounds()
+    rng = np.random.default_rng(5)
+    n = 8192
+    s = random_samples(rng, n, bmin, binv)
+    # target: directions near a mean that depends on x
+    x01 = (s[:, 0] - bmin[0]) * binv[0]
+    mean = np.stack([np.cos(np.pi * x01), np.full(n, 0.6), np.sin(np.pi * x01)], 1)
+    mean /= np.linalg.norm(mean, axis=1, keepdims=True)
+    wi = mean + 0.15 * rng.normal(size=(n, 3))
+    s[:, 9:12] = wi / np.linalg.norm(wi, axis=1, keepdims=True)
+    s[:, 12] = 1.0 / (4 * np.pi)
+    s[:, 13] = 1.0
+    losses = [g.guide_train(s, lr=1e-2) for _ in range(150)]
+    _, final = g.guide_gradient(s)
+    g.close()
+    assert np.all(np.isfinite(losses))
+    assert final < losses[0] - 1.0, (losses[0], final)

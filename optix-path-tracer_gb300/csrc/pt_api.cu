@@ -229,6 +229,21 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_results.release();
   ctx->d_acc.release();
   ctx->d_acc64.release();
+  {
+    GuideState& G = ctx->guide;
+    G.w32.release();
+    G.m.release();
+    G.v.release();
+    G.wbf.release();
+    G.partial.release();
+    G.grad.release();
+    G.scalars.release();
+    G.counters.release();
+    G.samples.release();
+    G.eval_out.release();
+    G.out.release();
+    G.rec.release();
+  }
   ctx->d_tmp.release();
   ctx->d_tmpu.release();
   if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
@@ -803,8 +818,12 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     ctx->tev.resize(6 * kItersPerGraph);
     for (auto& e : ctx->tev) CK(cudaEventCreate(&e));
   }
+  const bool guide = p->guide != 0;
+  GuideInferArgs gi;
+  if (guide) gi = guide_infer_args(ctx);
   if (!ctx->graph || ctx->graph_counters != counters || ctx->graph_timing != timing ||
-      ctx->graph_mode != p->mode) {
+      ctx->graph_mode != p->mode || ctx->graph_guide != guide ||
+      memcmp(&ctx->graph_W, &ctx->W, sizeof(WaveState)) != 0) {
     if (ctx->graph) {
       cudaGraphExecDestroy(ctx->graph);
       ctx->graph = nullptr;
@@ -813,7 +832,8 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < kItersPerGraph; i++)
       pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters, ctx->lc,
-                           st, timing ? &ctx->tev[6 * i] : nullptr, p->mode, nullptr, false, 0);
+                           st, timing ? &ctx->tev[6 * i] : nullptr, p->mode, nullptr, false, 0,
+                           guide ? &gi : nullptr);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
     cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
@@ -822,6 +842,8 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
     ctx->graph_counters = counters;
     ctx->graph_timing = timing;
     ctx->graph_mode = p->mode;
+    ctx->graph_guide = guide;
+    ctx->graph_W = ctx->W;
   }
   // bounded host loop: a path needs at most max_depth iterations after its
   // generation, and every iteration generates at least one path while any
@@ -886,7 +908,9 @@ int pth::check_params(pt_context* ctx, const pt_render_params* p) {
     return fail(ctx, PT_EINVAL, "image too large");
   if (p->mode != PT_MODE_REF && p->mode != PT_MODE_CONSISTENT)
     return fail(ctx, PT_EINVAL, "unknown integrator mode");
-  if (p->guide != 0) return fail(ctx, PT_EINVAL, "guide not available in this build");
+  if (p->guide != 0 && p->guide != 1) return fail(ctx, PT_EINVAL, "guide must be 0 or 1");
+  if (p->guide && p->mode != PT_MODE_CONSISTENT)
+    return fail(ctx, PT_EINVAL, "the learned guide needs the consistent integrator mode");
   if (!ctx->committed) return fail(ctx, PT_ESTATE, "scene not committed (call pt_commit)");
   return PT_OK;
 }
@@ -901,18 +925,43 @@ static int render_device(pt_context* ctx, const pt_render_params* p, void* d_acc
   size_t WH = (size_t)p->width * p->height;
   const size_t results_cap = (size_t)1 << 27;  // 128 M paths = 2 GiB of results
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)p->spp, results_cap / WH));
+  if (p->guide) chunk = 1;  // the guide trains between frames
   int rc = ensure_wave(ctx, (size_t)chunk * WH);
   if (rc) return rc;
+  if (p->guide) {
+    rc = guide_prepare(ctx);
+    if (rc) return rc;
+    if (!ctx->guide.ready && (rc = pt_guide_init(ctx, 0)) != PT_OK) return rc;
+    CK(ctx->guide.out.ensure((size_t)ctx->slots));
+    ctx->W.guide = ctx->guide.out.p;
+  }
   if (p->frame0 == 0) CK(cudaMemsetAsync(d_acc, 0, WH * (acc64 ? 32 : 16), st));
   for (int f = 0; f < p->spp; f += chunk) {
     int frames = std::min(chunk, p->spp - f);
+    if (p->guide) {
+      rc = guide_frame_begin(ctx, p->width, p->height);
+      if (rc) return rc;
+      ctx->W.grec = ctx->guide.rec.p;
+      ctx->W.grec_stride = ctx->guide.rec_stride;
+      ctx->W.grec_n = ctx->guide.rec_n;
+    }
     rc = run_chunk(ctx, p, p->frame0 + f, frames);
     if (rc) return rc;
+    if (p->guide) {
+      rc = guide_frame_train(ctx);
+      if (rc) return rc;
+    }
     if (acc64)
       pt::launch_accumulate64(ctx->d_results.p, (double*)d_acc, p->width, p->height, frames, st);
     else
       pt::launch_accumulate(ctx->d_results.p, (float4*)d_acc, p->width, p->height, frames, st);
     ctx->stats.kernel_launches += 1;
+  }
+  if (p->guide) {
+    uint32_t fl[4];
+    CK(cudaMemcpyAsync(fl, ctx->guide.counters.p, 16, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (fl[1] || fl[2]) return fail(ctx, PT_ETIMEOUT, "guide kernel: tensor-core wait ran out");
   }
   return PT_OK;
 }
@@ -991,6 +1040,7 @@ PT_API int pt_render_paths(pt_context* ctx, const pt_render_params* params, floa
   int rc = check_params(ctx, params);
   if (rc) return rc;
   if (!out_rgb) return fail(ctx, PT_EINVAL, "null output");
+  if (params->guide) return fail(ctx, PT_EINVAL, "pt_render_paths renders without the guide");
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
   CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
@@ -1145,6 +1195,7 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
   if (!ctx) return PT_EINVAL;
   int rc = check_params(ctx, p);
   if (rc) return rc;
+  if (p->guide) return fail(ctx, PT_EINVAL, "pt_render_noalloc renders without the guide");
   size_t WH = (size_t)p->width * p->height;
   if (WH > kNoAllocMaxPixels)
     return fail(ctx, PT_EINVAL,

@@ -394,6 +394,7 @@ static int check_items(pt_batch* b, const pt_batch_item* items, int n) {
     if (!it.accum_rgba) return bfail(b, PT_EINVAL, at + "null accumulator");
     if (it.params.mode != items[0].params.mode)
       return bfail(b, PT_EINVAL, at + "all items of a batch use one integrator mode");
+    if (it.params.guide) return bfail(b, PT_EINVAL, at + "batches render without the guide");
   }
   return PT_OK;
 }

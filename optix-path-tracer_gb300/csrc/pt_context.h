@@ -65,6 +65,9 @@ struct GuideState {
   DevBuf<GuideSample> samples;
   DevBuf<float> eval_out;
   DevBuf<GuideParams> out;   // per path slot: decoded guide
+  DevBuf<GuideSample> rec;   // training records of the current frame
+  uint32_t rec_stride = 1, rec_n = 0;
+  float lr = 1e-2f;          // Adam learning rate of the online training
   float bmin[3] = {0, 0, 0}, binv[3] = {1, 1, 1};
   int step = 0;
   int grid = 0;
@@ -123,6 +126,8 @@ struct pt_context {
   bool graph_counters = false;
   bool graph_timing = false;
   int graph_mode = 0;
+  WaveState graph_W{};       // the buffers the captured graph refers to
+  bool graph_guide = false;
   std::vector<cudaEvent_t> tev;  // 6 per iteration of the graph (timing)
   int max_stack = 0;
   LaunchCfg lc{};
@@ -149,6 +154,13 @@ pt::Box prim_bounds(const pt_context* ctx, const HostPrim& p);
 /* Allocates the guide's buffers and finds the scene box of its position
  * encoding; returns a PT_ status. */
 int guide_prepare(pt_context* ctx);
+/* Online training around a guided frame (enqueued on the context's stream):
+ * clear the record buffer for a frame of w x h paths (and size it), then
+ * collect the frame's records and take one Adam step. */
+int guide_frame_begin(pt_context* ctx, int w, int h);
+int guide_frame_train(pt_context* ctx);
+/* Inference arguments for the current buffers. */
+GuideInferArgs guide_infer_args(pt_context* ctx);
 /* Render parameters valid for the context (sets ctx->err otherwise). */
 int check_params(pt_context* ctx, const pt_render_params* p);
 }  // namespace pth

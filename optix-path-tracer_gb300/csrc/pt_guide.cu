@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
   const uint32_t tmem = g.base;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
   uint32_t phase = 0;
-  const uint32_t n = *A.count;
+  uint32_t n = *A.count;
+  if (A.max_count && n > A.max_count) n = A.max_count;
   const float wsum = *A.wsum;
   const uint32_t ntiles = (n + 127) / 128;
   bool first = true;
@@ -502,8 +503,48 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, WaveState W,
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
 }
 
+// Completed training records with a positive weight, appended to the
+// training array (warp-aggregated atomics).
+__global__ void k_guide_collect(const GuideSample* __restrict__ rec, uint32_t n, GuideSample* out,
+                                uint32_t* count, float* wsum, uint32_t cap) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t it = 0; it < iters; it++, i += stride) {
+    GuideSample r;
+    bool take = false;
+    if (i < n) {
+      r = rec[i];
+      take = r.pad[1] == 2.f && r.weight > 0.f;
+    }
+    uint32_t mask = __ballot_sync(0xffffffffu, take);
+    uint32_t base = 0;
+    int lane = threadIdx.x & 31;
+    if (mask) {
+      int leader = __ffs(mask) - 1;
+      if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+      base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    if (take) {
+      uint32_t k = base + __popc(mask & ((1u << lane) - 1u));
+      if (k < cap) {
+        out[k] = r;
+        atomicAdd(wsum, r.weight);
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------ launchers ----
 namespace pt {
+
+void launch_guide_collect(const GuideSample* rec, uint32_t n, GuideSample* out, uint32_t* count,
+                          float* wsum, uint32_t cap, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_guide_collect<<<sms * 4, 256, 0, st>>>(rec, n, out, count, wsum, cap);
+}
 
 size_t guide_train_smem() { return (size_t)kWeights + 5 * kTileT + 2 * (kTileG + kGuard); }
 size_t guide_infer_smem() { return (size_t)kWeights + 2 * kTileT; }

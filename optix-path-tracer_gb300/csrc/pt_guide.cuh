@@ -81,6 +81,7 @@ struct GuideTrainArgs {
   float* out;               // evaluation: 48 outputs per sample, or null
   float bmin[3], binv[3];
   int train;                // 1: backward + partial gradients
+  uint32_t max_count;       // use at most this many samples (0: all)
   uint32_t* fail;
 };
 
@@ -109,6 +110,10 @@ void launch_guide_grad(const GuideTrainArgs& a, int grid, cudaStream_t st);
 void launch_guide_adam(const GuideAdamArgs& a, cudaStream_t st);
 void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                         const GuideInferArgs& a, int grid, cudaStream_t st);
+/* Appends the completed records with a positive weight to out (at most cap;
+ * count and wsum accumulate on the device). */
+void launch_guide_collect(const GuideSample* rec, uint32_t n, GuideSample* out, uint32_t* count,
+                          float* wsum, uint32_t cap, cudaStream_t st);
 }  // namespace pt
 #endif
 

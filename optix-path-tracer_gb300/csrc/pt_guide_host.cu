@@ -66,7 +66,8 @@ int pth::guide_prepare(pt_context* ctx) {
     GK(G.wbf.ensure(PTG_PARAMS));
     GK(G.grad.ensure(PTG_PARAMS));
     GK(G.scalars.ensure(2));
-    GK(G.counters.ensure(2));
+    GK(G.counters.ensure(4));
+    GK(cudaMemset(G.counters.p, 0, 16));
     int dev = 0, sms = 0;
     GK(cudaGetDevice(&dev));
     GK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -97,6 +98,72 @@ int pth::guide_prepare(pt_context* ctx) {
   return PT_OK;
 }
 
+GuideInferArgs pth::guide_infer_args(pt_context* ctx) {
+  GuideState& G = ctx->guide;
+  GuideInferArgs a;
+  memset(&a, 0, sizeof(a));
+  a.w = (const __nv_bfloat16*)G.wbf.p;
+  a.out = G.out.p;
+  memcpy(a.bmin, G.bmin, sizeof(a.bmin));
+  memcpy(a.binv, G.binv, sizeof(a.binv));
+  a.fail = G.counters.p + 2;  // read back at the end of a guided render
+  return a;
+}
+
+int pth::guide_frame_begin(pt_context* ctx, int w, int h) {
+  GuideState& G = ctx->guide;
+  const size_t target = (size_t)1 << 17;  // recording paths per frame (2 records each)
+  size_t wh = (size_t)w * h;
+  G.rec_stride = (uint32_t)std::max<size_t>(1, (wh + target - 1) / target);
+  G.rec_n = (uint32_t)(2 * ((wh + G.rec_stride - 1) / G.rec_stride));
+  GK(G.rec.ensure(G.rec_n));
+  GK(G.samples.ensure((size_t)1 << 18));
+  GK(cudaMemsetAsync(G.rec.p, 0, (size_t)G.rec_n * sizeof(GuideSample), ctx->stream));
+  return PT_OK;
+}
+
+int pth::guide_frame_train(pt_context* ctx) {
+  GuideState& G = ctx->guide;
+  cudaStream_t st = ctx->stream;
+  const uint32_t cap = 1u << 18;
+  GK(cudaMemsetAsync(G.counters.p, 0, 4, st));  // the failure flags stay
+  GK(cudaMemsetAsync(G.scalars.p, 0, 8, st));
+  pt::launch_guide_collect(G.rec.p, G.rec_n, G.samples.p, G.counters.p, G.scalars.p + 1, cap, st);
+  GuideTrainArgs a;
+  memset(&a, 0, sizeof(a));
+  a.w = (const __nv_bfloat16*)G.wbf.p;
+  a.samples = G.samples.p;
+  a.count = G.counters.p;
+  a.wsum = G.scalars.p + 1;
+  a.partial = G.partial.p;
+  a.loss = G.scalars.p;
+  memcpy(a.bmin, G.bmin, sizeof(a.bmin));
+  memcpy(a.binv, G.binv, sizeof(a.binv));
+  a.train = 1;
+  a.max_count = cap;
+  a.fail = G.counters.p + 1;
+  pt::launch_guide_grad(a, G.grid, st);
+  GuideAdamArgs d;
+  memset(&d, 0, sizeof(d));
+  d.partial = G.partial.p;
+  d.nparts = G.grid;
+  d.w32 = G.w32.p;
+  d.wbf = (__nv_bfloat16*)G.wbf.p;
+  d.m = G.m.p;
+  d.v = G.v.p;
+  d.update = 1;
+  G.step++;
+  d.lr = G.lr;
+  d.b1 = 0.9f;
+  d.b2 = 0.99f;
+  d.eps = 1e-8f;
+  d.bc1 = 1.f - powf(d.b1, (float)G.step);
+  d.bc2 = 1.f - powf(d.b2, (float)G.step);
+  pt::launch_guide_adam(d, st);
+  GK(cudaGetLastError());
+  return PT_OK;
+}
+
 static int upload_params(pt_context* ctx, const std::vector<float>& w) {
   GuideState& G = ctx->guide;
   std::vector<uint16_t> bf(PTG_PARAMS);
@@ -122,8 +189,6 @@ static int guide_step(pt_context* ctx, int n, bool update, float lr, float* loss
   cudaStream_t st = ctx->stream;
   uint32_t cnt[2] = {(uint32_t)n, 0u};
   GK(cudaMemcpyAsync(G.counters.p, cnt, sizeof(cnt), cudaMemcpyHostToDevice, st));
-  std::vector<GuideSample> hs;  // weight sum on the device would need a pass; the host has them
-  (void)hs;
   GuideTrainArgs a;
   memset(&a, 0, sizeof(a));
   a.w = (const __nv_bfloat16*)G.wbf.p;

@@ -132,6 +132,10 @@ struct ShadowBuf {
   uint4* st;
 };
 
+struct GuideParams;
+struct GuideSample;
+struct GuideInferArgs;
+
 struct WaveState {
   PathBuf path[2];            /* ping-pong: path[parity] is current */
   float4* hit;                /* t, u, v, leaf index: by position in the current buffer */
@@ -139,6 +143,11 @@ struct WaveState {
   WaveCounters* ctr;
   float4* results;            /* per path of the chunk: colour */
   int slots;                  /* capacity of each buffer */
+  /* learned guide (consistent mode, guide = 1): decoded guide by position;
+   * training records, 2 per recording path (path id % grec_stride == 0) */
+  GuideParams* guide;
+  GuideSample* grec;
+  uint32_t grec_stride, grec_n;
 };
 
 /* float4 arrays per slot: 2 x 4 (path buffers) + 1 (hit) + 7 (shadow), and
@@ -159,11 +168,13 @@ LaunchCfg default_launch(int max_stack);
 /* One wavefront iteration (7 kernels).  ev, if not null, holds 6 events
  * recorded between the stages.  br: batch tables, or null for one scene.
  * use_cond: the queue-advance kernel sets graph conditional `cond` to
- * whether the chunk has work left (device-side iteration loop). */
+ * whether the chunk has work left (device-side iteration loop).  gi: the
+ * learned guide (consistent mode only): its inference kernel runs between
+ * trace and shade (counted in the shade stage) and shading samples from it. */
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
                       bool counters, const LaunchCfg& lc, cudaStream_t st, cudaEvent_t* ev,
                       int mode, const BatchRefs* br, bool use_cond,
-                      unsigned long long cond);
+                      unsigned long long cond, const GuideInferArgs* gi = nullptr);
 /* Batch chunk boundaries: begin loads chunk c.chunk into *ctl and resets the
  * queues (and sets conditional `inner` to 1); end accumulates the chunk's
  * results into the scenes' accumulators, moves to the next chunk and sets

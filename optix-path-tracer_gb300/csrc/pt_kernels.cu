@@ -25,6 +25,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include "pt_device.cuh"
+#include "pt_guide.cuh"
 #include "pt_internal.h"
 
 using namespace ptd;
@@ -1034,33 +1035,66 @@ __device__ __forceinline__ float lights_pdf_c(const DevScene& S, V3 P, V3 d, int
   return acc / (float)n_sel;
 }
 
-// Appends a continuing path (consistent mode) to the next buffer.
+// Appends a continuing path (consistent mode) to the next buffer; rad_w is
+// the guide-record word carried in the radiance's w (0 without the guide).
 __device__ __forceinline__ void path_push(const WaveState& W, const WaveCounters& c, uint4 st,
-                                          V3 thr, V3 rad, V3 o, V3 d, bool cont) {
+                                          V3 thr, V3 rad, V3 o, V3 d, bool cont,
+                                          float rad_w = 0.f) {
   uint32_t pos = warp_push(&W.ctr->n_next, cont);
   if (cont) {
     const PathBuf& nb = W.path[c.parity ^ 1u];
     nb.ray_o[pos] = make_float4(o.x, o.y, o.z, 1e-3f);
     nb.ray_d[pos] = make_float4(d.x, d.y, d.z, PT_RAY_TMAX);
     nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, 0.f);
-    nb.rad[pos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    nb.rad[pos] = make_float4(rad.x, rad.y, rad.z, rad_w);
     nb.st[pos] = st;
+  }
+}
+
+// ---------------------------------------------------- guide training data --
+// A path whose id is a multiple of W.grec_stride records its first two
+// guided vertices (shading point, sampled direction, BSDF pdf) in
+// W.grec[2 * (id / stride) + v], with the throughput arriving at the vertex
+// (luminance, kept in .weight) and the radiance collected so far (pad[0]).
+// The record word in the path's radiance w is 2 * records + (1 if the
+// current vertex recorded), so the NEE term of that vertex, known after its
+// shadow ray, joins the mark.  At the end of the path each record's weight
+// becomes (radiance after the vertex) / (throughput at it) = F / q of its
+// direction, the training signal.
+__device__ __forceinline__ float lum3(V3 c) {
+  return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
+}
+
+__device__ __forceinline__ void guide_end(const WaveState& W, uint32_t pid, float code,
+                                          V3 rad_end) {
+  int count = (int)code >> 1;
+  if (count <= 0) return;
+  uint32_t base = 2u * (pid / W.grec_stride);
+  float le = lum3(rad_end);
+  for (int v = 0; v < count; v++) {
+    GuideSample& r = W.grec[base + v];
+    float T = r.weight, w = (le - r.pad[0]) / T;
+    r.weight = (T > 0.f && w > 0.f && w < 1e30f) ? fminf(w, 1e6f) : 0.f;
+    r.pad[1] = 2.f;  // complete
   }
 }
 
 // One bounce of the consistent integrator (the oracle's color_c): emission
 // with MIS at hits and misses, NEE over lights + environment, BSDF
 // continuation, Russian roulette.  The NEE term waits for its shadow ray in
-// the shadow buffer together with the already-sampled continuation.
-// One path of k_shade_c (see shade_path).
-template <bool BATCH>
+// the shadow buffer together with the already-sampled continuation.  With
+// GUIDE the continuation is drawn from alpha * guide + (1 - alpha) * BSDF
+// (the guide of this position from k_guide_infer) and that mixture density is
+// the MIS partner of NEE and of emitter hits at the next vertex.  One path of
+// k_shade_c (see shade_path).
+template <bool BATCH, bool GUIDE>
 __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState& W,
                                            const WaveCounters& c, const WaveCtl& ctl,
                                            const BatchRefs& br, uint32_t i, bool active) {
   const PathBuf& pb = W.path[c.parity];
   uint4 st = make_uint4(0, 0, 0, 0);
   V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), Wi = v3(0.f), dcont = v3(0.f), C = v3(0.f);
-  float tmax = 0.f;
+  float tmax = 0.f, code = 0.f;
   bool ended = false, shadow = false;
   if (active) st = pb.st[i];
   const DevScene& S = path_scene<BATCH>(S0, br, st.z);
@@ -1068,7 +1102,9 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
   if (active) {
     const PathCtl pc = path_ctl<BATCH>(ctl, br, st.z);
     thr = f4xyz(pb.thr[i]);
-    rad = f4xyz(pb.rad[i]);
+    float4 r4 = pb.rad[i];
+    rad = f4xyz(r4);
+    code = GUIDE ? r4.w : 0.f;
     float4 hit = W.hit[i];
     float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
     V3 d = f4xyz(rdv);
@@ -1123,6 +1159,8 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
       } else {
         Frame fr(N);
         V3 wo_l = fr.to_local(Wo);
+        GuideParams G;
+        if (GUIDE) G = W.guide[i];
         if (n_sel > 0) {
           int k = (int)(rnd(st.x) * (float)n_sel);
           if (k > n_sel - 1) k = n_sel - 1;
@@ -1159,6 +1197,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
             V3 wi_l = fr.to_local(wi_n);
             V3 f = bsdf_f_c(m, wo_l, wi_l);
             float pbs = bsdf_pdf_c(m, wo_l, wi_l);
+            if (GUIDE) pbs = G.alpha * guide_pdf(G, wi_n.x, wi_n.y, wi_n.z) + (1.f - G.alpha) * pbs;
             V3 cv = f * Le * (cs * power_mis(pls, pbs) / pls);
             if (!isNull(cv)) {
               shadow = true;
@@ -1166,16 +1205,48 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
             }
           }
         }
-        V3 wi_l = bsdf_sample_c(m, wo_l, st.x);
+        V3 wi_l, wdir;
+        if (GUIDE && rnd(st.x) < G.alpha) {
+          float u0 = rnd(st.x);
+          float u1 = rnd(st.x);
+          float u2 = rnd(st.x);
+          guide_sample(G, u0, u1, u2, wdir.x, wdir.y, wdir.z);
+          wi_l = fr.to_local(wdir);
+        } else {
+          wi_l = bsdf_sample_c(m, wo_l, st.x);
+          wdir = fr.to_world(wi_l);
+        }
         float pbs = bsdf_pdf_c(m, wo_l, wi_l);
+        float q = pbs;
+        if (GUIDE) q = G.alpha * guide_pdf(G, wdir.x, wdir.y, wdir.z) + (1.f - G.alpha) * pbs;
         V3 f = bsdf_f_c(m, wo_l, wi_l);
-        if (!(pbs > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
+        if (!(q > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
           ended = true;
         } else {
-          thr *= f * (wi_l.y / pbs);
+          if (GUIDE) {
+            int count = (int)code >> 1;
+            code = (float)(2 * count);
+            if (count < 2 && st.y % W.grec_stride == 0) {
+              uint32_t slot = 2u * (st.y / W.grec_stride) + (uint32_t)count;
+              if (slot < W.grec_n) {
+                GuideSample r;
+                r.P[0] = P.x; r.P[1] = P.y; r.P[2] = P.z;
+                r.N[0] = N.x; r.N[1] = N.y; r.N[2] = N.z;
+                r.Wo[0] = Wo.x; r.Wo[1] = Wo.y; r.Wo[2] = Wo.z;
+                r.wi[0] = wdir.x; r.wi[1] = wdir.y; r.wi[2] = wdir.z;
+                r.p_bsdf = pbs;
+                r.weight = lum3(thr);
+                r.pad[0] = lum3(rad);
+                r.pad[1] = 1.f;
+                W.grec[slot] = r;
+                code = (float)(2 * (count + 1) + 1);
+              }
+            }
+          }
+          thr *= f * (wi_l.y / q);
           prev_spec = false;
-          pdf_prev = pbs;
-          dcont = fr.to_world(wi_l);
+          pdf_prev = q;
+          dcont = wdir;
         }
       }
       if (!ended) {
@@ -1200,14 +1271,19 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
     W.sh.C[spos] = make_float4(C.x, C.y, C.z, tmax);
     W.sh.Wo[spos] = make_float4(dcont.x, dcont.y, dcont.z, ended ? 1.f : 0.f);
     W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
-    W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, code);
     W.sh.st[spos] = st;
   }
-  if (active && !shadow && ended) finalize_path(W, st.y, rad);
-  path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended);
+  if (active && !shadow && ended) {
+    finalize_path(W, st.y, rad);
+    if (GUIDE) guide_end(W, st.y, code, rad);
+  }
+  // the next vertex starts without a pending record of its own
+  float cw = GUIDE ? (float)(((int)code >> 1) * 2) : 0.f;
+  path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended, cw);
 }
 
-template <bool BATCH, bool SORT>
+template <bool BATCH, bool SORT, bool GUIDE>
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S0, WaveState W,
                                                             const WaveCtl* __restrict__ ctlp,
                                                             BatchRefs br) {
@@ -1215,7 +1291,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S0, WaveSta
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
-  SHADE_LOOP(shade_c_path<BATCH>(S0, W, c, ctl, br, i, i < n))
+  SHADE_LOOP((shade_c_path<BATCH, GUIDE>(S0, W, c, ctl, br, i, i < n)))
 }
 
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveState W,
@@ -1232,18 +1308,31 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveSta
     uint4 st = make_uint4(0, 0, 0, 0);
     V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), dcont = v3(0.f);
     bool ended = false;
+    float code = 0.f;
     if (active) {
       st = W.sh.st[i];
       thr = f4xyz(W.sh.thr[i]);
-      rad = f4xyz(W.sh.rad[i]);
+      float4 r4 = W.sh.rad[i];
+      rad = f4xyz(r4);
+      code = r4.w;
       float4 Wi4 = W.sh.Wi[i], C4 = W.sh.C[i], Wo4 = W.sh.Wo[i];
       P = f4xyz(W.sh.P[i]);
-      if (Wi4.w == 0.f) rad += f4xyz(C4);  // unoccluded
+      if (Wi4.w == 0.f) {  // unoccluded
+        rad += f4xyz(C4);
+        // the vertex that just recorded a guide sample: its NEE light did
+        // not come along the recorded direction
+        int ci = (int)code;
+        if (ci & 1) W.grec[2u * (st.y / W.grec_stride) + (uint32_t)(ci >> 1) - 1u].pad[0] +=
+            lum3(f4xyz(C4));
+      }
       dcont = f4xyz(Wo4);
       ended = Wo4.w != 0.f;
-      if (ended) finalize_path(W, st.y, rad);
+      if (ended) {
+        finalize_path(W, st.y, rad);
+        if (code != 0.f) guide_end(W, st.y, code, rad);
+      }
     }
-    path_push(W, c, st, thr, rad, P, dcont, active && !ended);
+    path_push(W, c, st, thr, rad, P, dcont, active && !ended, (float)(((int)code >> 1) * 2));
   }
 }
 
@@ -1558,7 +1647,7 @@ template <bool BATCH>
 static void launch_iteration_t(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                                int max_stack, bool counters, const LaunchCfg& lc, cudaStream_t st,
                                cudaEvent_t* ev, int mode, const BatchRefs& br, bool use_cond,
-                               unsigned long long cond) {
+                               unsigned long long cond, const GuideInferArgs* gi) {
   size_t sm = trace_smem(max_stack, lc.trace_block);
   FirstHitOut none{};
   const int tb = lc.trace_block, tg = lc.trace_grid, sb = lc.shade_block, sg = lc.shade_grid;
@@ -1570,9 +1659,13 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
   else
     k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
-  if (mode == 1) {
-    if (lc.sort) k_shade_c<BATCH, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
-    else k_shade_c<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  if (mode == 1 && gi) {
+    launch_guide_infer(S, W, ctl, *gi, 2 * num_sms(), st);
+    if (lc.sort) k_shade_c<BATCH, true, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade_c<BATCH, false, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  } else if (mode == 1) {
+    if (lc.sort) k_shade_c<BATCH, true, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade_c<BATCH, false, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
   } else {
     if (lc.sort) k_shade<BATCH, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
     else k_shade<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
@@ -1594,12 +1687,14 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
 // One wavefront iteration (7 launches).
 void launch_iteration(const DevScene& S, const WaveState& W, const WaveCtl* ctl, int max_stack,
                       bool counters, const LaunchCfg& lc, cudaStream_t st, cudaEvent_t* ev,
-                      int mode, const BatchRefs* br, bool use_cond, unsigned long long cond) {
+                      int mode, const BatchRefs* br, bool use_cond, unsigned long long cond,
+                      const GuideInferArgs* gi) {
   if (br)
-    launch_iteration_t<true>(S, W, ctl, max_stack, counters, lc, st, ev, mode, *br, use_cond, cond);
+    launch_iteration_t<true>(S, W, ctl, max_stack, counters, lc, st, ev, mode, *br, use_cond, cond,
+                             nullptr);
   else
     launch_iteration_t<false>(S, W, ctl, max_stack, counters, lc, st, ev, mode, BatchRefs{},
-                              use_cond, cond);
+                              use_cond, cond, gi);
 }
 
 void launch_batch_begin(const WaveState& W, WaveCtl* ctl, const BatchChunk* chunks,

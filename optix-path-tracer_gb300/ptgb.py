@@ -769,6 +769,40 @@ def heightfield_scene(width=1920, height=1080, cells=1024, seed=0, env_w=2048, e
     return s
 
 
+def guide_box_scene(width=1920, height=1080, cells=1024, seed=0, env_w=2048, env_h=1024,
+                    env=None, opening=0.005):
+    """The hard-indirect variant of the heightfield scene (the learned-guide
+    configuration): the terrain inside a closed white Lambertian box whose
+    only opening, a square in the ceiling covering `opening` of the box's
+    surface, lets the HDR sky in.  The camera is inside the box."""
+    s = heightfield_scene(width, height, cells=cells, seed=seed, env_w=env_w, env_h=env_h,
+                          env=env)
+    wall = s.lambertian((0.7, 0.7, 0.7))
+    x0, x1, y0, y1, z0, z1 = -1.02, 1.02, -0.2, 1.2, -1.02, 1.02
+    area = 2 * (x1 - x0) * (z1 - z0) + 2 * (x1 - x0) * (y1 - y0) + 2 * (z1 - z0) * (y1 - y0)
+    side = (opening * area) ** 0.5
+    hx0, hz0 = 0.35 - side / 2, 0.25 - side / 2
+    hx1, hz1 = hx0 + side, hz0 + side
+    s.rect(y0, y1, z0, z1, x0, False, PT_X_AXIS, wall)       # normals face inside
+    s.rect(y0, y1, z0, z1, x1, True, PT_X_AXIS, wall)
+    s.rect(x0, x1, y0, y1, z0, False, PT_Z_AXIS, wall)
+    s.rect(x0, x1, y0, y1, z1, True, PT_Z_AXIS, wall)
+    s.rect(x0, x1, z0, z1, y0, False, PT_Y_AXIS, wall)       # floor under the terrain
+    s.rect(x0, hx0, z0, z1, y1, True, PT_Y_AXIS, wall)       # ceiling around the opening
+    s.rect(hx1, x1, z0, z1, y1, True, PT_Y_AXIS, wall)
+    s.rect(hx0, hx1, z0, hz0, y1, True, PT_Y_AXIS, wall)
+    s.rect(hx0, hx1, hz1, z1, y1, True, PT_Y_AXIS, wall)
+    s.set_camera((0.0, 0.75, 0.98), (0.0, 0.0, -0.3), (0, 1, 0), 60.0, width / height, 0.0, 2.0)
+    return s
+
+
+def rel_mse(img, ref, eps=1e-2):
+    """Mean over pixels and channels of (x - r)^2 / (r^2 + eps)."""
+    x = np.asarray(img, np.float64)[..., :3]
+    r = np.asarray(ref, np.float64)[..., :3]
+    return float(np.mean((x - r) ** 2 / (r * r + eps)))
+
+
 def batch_workload(n=64, seed=4, env_w=1024, env_h=512):
     """The batched multi-scene workload: n seeded heightfield scenes with
     triangle counts log-uniform over [1e3, 1e6], square images of 256, 512 or

@@ -175,3 +175,56 @@ def test_training_lowers_loss(ptgb_mod):
     g.close()
     assert np.all(np.isfinite(losses))
     assert final < losses[0] - 1.0, (losses[0], final)
+
+
+def _box(ptgb, w):
+    return ptgb.guide_box_scene(w, w, cells=32, env_w=256, env_h=128)
+
+
+def test_guided_render_is_unbiased(ptgb_mod):
+    """The guided estimator (one-sample MIS of guide and BSDF, weights
+    f cos / q) converges to the plain render: the image means agree within
+    the noise while the guide trains frame by frame."""
+    P = ptgb_mod.GpuRenderer.params
+    s = _box(ptgb_mod, 64)
+    plain = ptgb_mod.GpuRenderer(s)
+    ref = plain.render64(P(64, 64, 4096, mode=1, frame0=1 << 20))[..., :3].mean() / 4096
+    g = ptgb_mod.GpuRenderer(s)
+    g.guide_init(11)
+    acc = g.render64(P(64, 64, 384, mode=1, guide=1))
+    assert np.all(acc[..., 3] == 384)
+    mean = acc[..., :3].mean() / 384
+    assert abs(mean - ref) <= 0.02 * ref, (mean, ref)
+    plain.close()
+    g.close()
+
+
+def test_guide_lowers_error_at_equal_samples(ptgb_mod):
+    """On the hard-indirect box (light only through a 0.5 % opening), the
+    trained guide gives a lower relMSE than plain BSDF + light MIS at the same
+    sample count."""
+    P = ptgb_mod.GpuRenderer.params
+    w, spp = 128, 256
+    s = _box(ptgb_mod, w)
+    r = ptgb_mod.GpuRenderer(s)
+    ref = r.render64(P(w, w, 8192, mode=1, frame0=1 << 20)) / 8192
+    plain = r.render64(P(w, w, spp, mode=1)) / spp
+    g = ptgb_mod.GpuRenderer(s)
+    g.guide_init(1)
+    guided = g.render64(P(w, w, spp, mode=1, guide=1)) / spp
+    e_plain, e_guided = ptgb_mod.rel_mse(plain, ref), ptgb_mod.rel_mse(guided, ref)
+    assert e_guided < 0.75 * e_plain, (e_guided, e_plain)
+    r.close()
+    g.close()
+
+
+def test_guide_argument_checks(ptgb_mod):
+    P = ptgb_mod.GpuRenderer.params
+    g = ptgb_mod.GpuRenderer(_box(ptgb_mod, 16))
+    with pytest.raises(ptgb_mod.PtError):        # reference mode has no guide
+        g.render(P(16, 16, 1, mode=0, guide=1))
+    with pytest.raises(ptgb_mod.PtError):
+        g.render_paths(P(16, 16, 1, mode=1, guide=1))
+    with pytest.raises(ptgb_mod.PtError):
+        g.render(P(16, 16, 1, mode=1, guide=2))
+    g.close()

@@ -64,10 +64,12 @@ struct GuideState {
   DevBuf<uint32_t> counters; // [0] samples in the training array, [1] failure flag
   DevBuf<GuideSample> samples;
   DevBuf<float> eval_out;
-  DevBuf<GuideParams> out;   // per path slot: decoded guide
+  DevBuf<GuidePacked> out;   // per path slot: decoded guide
   DevBuf<GuideSample> rec;   // training records of the current frame
   uint32_t rec_stride = 1, rec_n = 0;
   float lr = 1e-2f;          // Adam learning rate of the online training
+  int steps = 8;             // Adam steps per frame on the frame's samples
+  float exponent = 1.f;      // training weight = (F/q)^exponent (1: the KL target)
   float bmin[3] = {0, 0, 0}, binv[3] = {1, 1, 1};
   int step = 0;
   int grid = 0;

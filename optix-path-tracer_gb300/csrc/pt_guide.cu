@@ -425,44 +425,121 @@ __global__ void k_guide_adam(GuideAdamArgs A) {
   A.wbf[p] = __float2bfloat16_rn(w);
 }
 
-// Inference inside the wavefront: one row per live path of the current
-// buffer; rows whose hit is a guided (non-delta) material get a decoded
-// guide in A.out at the path's position.
-__global__ void __launch_bounds__(128) k_guide_infer(DevScene S, WaveState W,
+// ------------------------------------------------------ inference --------
+__device__ __forceinline__ void bar_group(int id) {
+  asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+}
+// AND of v over the 128 threads of named barrier id.
+__device__ __forceinline__ bool group_and(bool v, int id) {
+  uint32_t r;
+  asm volatile(
+      "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred p, %2, 128, q;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *(uint32_t*)&h;
+}
+// 8 consecutive columns (c0 % 8 == 0) of row r as one 16-byte store.
+__device__ __forceinline__ void st_row8(unsigned char* tile, int r, int c0, const float* v) {
+  uint4 q = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                       pack_bf16x2(v[6], v[7]));
+  *(uint4*)(tile + core_off(r, c0, PTG_K)) = q;
+}
+
+// The feature row of guide_features, written 8 columns at a time (the same
+// arithmetic, so inference and training see identical features), then the
+// ones column and padding.
+__device__ void write_features_vec(unsigned char* T, int row, const float* P, const float* N,
+                                   const float* Wo, const float* bmin, const float* binv,
+                                   bool valid) {
+  float v[8];
+  if (!valid) {
+    for (int q = 0; q < 8; q++) v[q] = 0.f;
+    for (int c0 = 0; c0 < 72; c0 += 8) st_row8(T, row, c0, v);
+  } else {
+    for (int a = 0; a < 3; a++) {
+      float x = (P[a] - bmin[a]) * binv[a];
+      x = fminf(fmaxf(x, 0.f), 1.f);
+      float s, c;
+      sincospif(x, &s, &c);
+      for (int k = 0; k < PTG_FREQ; k++) {
+        v[(2 * k) & 7] = s;
+        v[(2 * k + 1) & 7] = c;
+        if (((2 * k + 2) & 7) == 0) st_row8(T, row, a * 2 * PTG_FREQ + 2 * k - 6, v);
+        float s2 = 2.f * s * c, c2 = 1.f - 2.f * s * s;
+        s = s2;
+        c = c2;
+      }
+    }
+  }
+  // 72..75 directions, 76 one, 77..79 zero
+  for (int q = 0; q < 8; q++) v[q] = 0.f;
+  if (valid) {
+    const float* dirs[2] = {N, Wo};
+    for (int q = 0; q < 2; q++) {
+      const float* d = dirs[q];
+      float y = fminf(fmaxf(d[1], -1.f), 1.f);
+      v[2 * q] = acosf(y) * 0.31830988618379067f;
+      v[2 * q + 1] = atan2f(d[2], d[0]) * 0.15915494309189535f + 0.5f;
+    }
+  }
+  v[4] = 1.f;
+  st_row8(T, row, 72, v);
+}
+
+// Inference inside the wavefront, one row per live path of the current
+// buffer; rows whose hit is a guided (non-delta) material get their packed
+// guide in A.out at the path's position.  Each CTA runs two independent
+// 128-row pipelines (warps 0-3 and 4-7) that share the weights: each has
+// its own activation tile (updated in place: the epilogue writes a layer's
+// output over its input once the MMA has read it), mbarrier, 64 TMEM columns
+// and named barrier, so one pipeline's epilogue overlaps the other's MMAs.
+__global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
                                                      const WaveCtl* __restrict__ ctlp,
                                                      GuideInferArgs A) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ TmemGuard g;
-  bool failed = false;
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t tbase;
   unsigned char* Wt = sm;
-  unsigned char* T[2] = {sm + kWeights, sm + kWeights + kTileT};
-  const int tid = threadIdx.x, warp = tid >> 5;
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&g.mbar)), "r"(1));
+  const int grp = threadIdx.x >> 7, row = threadIdx.x & 127, warp = threadIdx.x >> 5;
+  const int bar_id = 1 + grp;
+  unsigned char* T = sm + kWeights + grp * kTileT;
+  if (threadIdx.x == 0) {
+    for (int g = 0; g < 2; g++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[g])), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(&g.base)),
-                 "r"(64));
+                     smem_u32(&tbase)),
+                 "r"(128));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   load_weights(Wt, A.w);
   fence_before();
   __syncthreads();
   fence_after();
-  const uint32_t tmem = g.base;
+  const uint32_t tmem = tbase + (uint32_t)(grp * 64);
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   uint32_t phase = 0;
+  bool failed = false;
   const WaveCounters c = *W.ctr;
   const WaveCtl ctl = *ctlp;
   unsigned long long left = ctl.chunk_paths - c.next_path;
-  const uint32_t n = c.n_cur + (uint32_t)min((unsigned long long)((uint32_t)W.slots - c.n_cur), left);
+  const uint32_t n =
+      c.n_cur + (uint32_t)min((unsigned long long)((uint32_t)W.slots - c.n_cur), left);
   const uint32_t ntiles = (n + 127) / 128;
   const PathBuf& pb = W.path[c.parity];
-  for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-    const uint32_t i = tile * 128 + tid;
+  for (uint32_t tile = blockIdx.x * 2 + grp; tile < ntiles; tile += gridDim.x * 2) {
+    const uint32_t i = tile * 128 + row;
     bool valid = false;
-    float f[PTG_FEAT];
+    float P[3], N[3], Wo[3];
     if (i < n) {
       float4 hit = W.hit[i];
       uint32_t leaf = __float_as_uint(hit.w);
@@ -473,40 +550,70 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, WaveState W,
             type == PT_MAT_TORRANCE_SPARROW || type == PT_MAT_ASHIKHMIN_SHIRLEY) {
           float4 ro = pb.ray_o[i], rd = pb.ray_d[i];
           HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rd), hit.x, hit.y, hit.z, false);
-          float P[3] = {rec.P.x, rec.P.y, rec.P.z};
-          float N[3] = {rec.shading_normal.x, rec.shading_normal.y, rec.shading_normal.z};
-          float Wo[3] = {rec.Wo.x, rec.Wo.y, rec.Wo.z};
-          guide_features(P, N, Wo, A.bmin, A.binv, f);
+          P[0] = rec.P.x; P[1] = rec.P.y; P[2] = rec.P.z;
+          N[0] = rec.shading_normal.x; N[1] = rec.shading_normal.y; N[2] = rec.shading_normal.z;
+          Wo[0] = rec.Wo.x; Wo[1] = rec.Wo.y; Wo[2] = rec.Wo.z;
           valid = true;
         }
       }
     }
-    write_feature_row(T[0], tid, f, valid);
+    write_features_vec(T, row, P, N, Wo, A.bmin, A.binv, valid);
     float o[PTG_NOUT];
-    if (!forward_tile(tmem, g, phase, Wt, T, 2, o)) {
-      failed = true;
-      break;
+    for (int l = 0; l < 5 && !failed; l++) {
+      fence_async_smem();
+      fence_before();
+      bar_group(bar_id);
+      fence_after();
+      if (row == 0) {
+        issue_forward(tmem, T, Wt, l);
+        mma_commit(&mbar[grp]);
+      }
+      bool ok = mbar_wait(&mbar[grp], phase);
+      phase ^= 1u;
+      fence_after();
+      if (!group_and(ok, bar_id)) {
+        failed = true;
+        break;
+      }
+      if (l < 4) {
+        // ReLU, BF16, in place; then the ones column and padding
+        float h[16];
+        for (int c0 = 0; c0 < PTG_H; c0 += 16) {
+          tmem_ld16(tmem + lane_base + kTmemAcc + c0, h);
+          for (int q = 0; q < 16; q++) h[q] = fmaxf(h[q], 0.f);
+          st_row8(T, row, c0, h);
+          st_row8(T, row, c0 + 8, h + 8);
+        }
+        for (int q = 0; q < 16; q++) h[q] = 0.f;
+        h[0] = 1.f;
+        st_row8(T, row, PTG_H, h);
+        h[0] = 0.f;
+        st_row8(T, row, PTG_H + 8, h);
+      } else {
+        for (int c0 = 0; c0 < PTG_NOUT; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, o + c0);
+      }
     }
+    if (failed) break;
     if (valid) {
       GuideParams gp;
       guide_decode(o, gp);
-      A.out[i] = gp;
+      A.out[i] = guide_pack(gp);
     }
   }
   if (failed) {
-    if (tid == 0) atomicOr(A.fail, 1u);
-    mbar_wait(&g.mbar, phase);
+    if (row == 0) atomicOr(A.fail, 1u);
+    mbar_wait(&mbar[grp], phase);
   }
   fence_before();
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(128));
 }
 
 // Completed training records with a positive weight, appended to the
 // training array (warp-aggregated atomics).
 __global__ void k_guide_collect(const GuideSample* __restrict__ rec, uint32_t n, GuideSample* out,
-                                uint32_t* count, float* wsum, uint32_t cap) {
+                                uint32_t* count, float* wsum, uint32_t cap, float exponent) {
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t iters = (n + stride - 1) / stride;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -516,6 +623,7 @@ __global__ void k_guide_collect(const GuideSample* __restrict__ rec, uint32_t n,
     if (i < n) {
       r = rec[i];
       take = r.pad[1] == 2.f && r.weight > 0.f;
+      if (take && exponent != 1.f) r.weight = powf(r.weight, exponent);
     }
     uint32_t mask = __ballot_sync(0xffffffffu, take);
     uint32_t base = 0;
@@ -539,15 +647,15 @@ __global__ void k_guide_collect(const GuideSample* __restrict__ rec, uint32_t n,
 namespace pt {
 
 void launch_guide_collect(const GuideSample* rec, uint32_t n, GuideSample* out, uint32_t* count,
-                          float* wsum, uint32_t cap, cudaStream_t st) {
+                          float* wsum, uint32_t cap, float exponent, cudaStream_t st) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_guide_collect<<<sms * 4, 256, 0, st>>>(rec, n, out, count, wsum, cap);
+  k_guide_collect<<<sms * 4, 256, 0, st>>>(rec, n, out, count, wsum, cap, exponent);
 }
 
 size_t guide_train_smem() { return (size_t)kWeights + 5 * kTileT + 2 * (kTileG + kGuard); }
-size_t guide_infer_smem() { return (size_t)kWeights + 2 * kTileT; }
+size_t guide_infer_smem() { return (size_t)kWeights + 2 * kTileT; }  // 2 pipelines
 
 cudaError_t guide_set_smem() {
   cudaError_t e = cudaFuncSetAttribute(k_guide_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -567,7 +675,7 @@ void launch_guide_adam(const GuideAdamArgs& a, cudaStream_t st) {
 
 void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                         const GuideInferArgs& a, int grid, cudaStream_t st) {
-  k_guide_infer<<<grid, 128, guide_infer_smem(), st>>>(S, W, ctl, a);
+  k_guide_infer<<<grid, 256, guide_infer_smem(), st>>>(S, W, ctl, a);
 }
 
 }  // namespace pt

@@ -50,6 +50,18 @@ struct GuideParams {
   float pad[3];
 };
 
+/* The guide as stored per path between inference and shading (96 B): eight
+ * lobes as half (mean x, y, z, concentration), the cumulative mixture
+ * weights as half (the last forced to 1) and alpha.  Sampling and density
+ * both read these same values (means renormalised), so they stay
+ * consistent. */
+struct GuidePacked {
+  uint2 lobe[PTG_LOBES];   /* half2 (mx, my), half2 (mz, kappa) */
+  uint4 cdf;               /* 8 x half */
+  float alpha;
+  uint32_t pad[3];
+};
+
 /* A training sample: the shading point, the sampled direction, the BSDF pdf
  * of that direction and the sample's weight F/q (radiance carried back along
  * it times the BSDF and cosine, over the density it was sampled with). */
@@ -60,12 +72,13 @@ struct GuideSample {
 
 #ifdef __CUDACC__
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 /* Kernel arguments (pt_guide.cu). */
 struct GuideInferArgs {
   const __nv_bfloat16* w;   // BF16 weights, row-major, PTG_PARAMS
-  GuideParams* out;         // per buffer position
+  GuidePacked* out;         // per buffer position
   float bmin[3], binv[3];   // scene box for the position encoding
   uint32_t* fail;
 };
@@ -113,7 +126,7 @@ void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ct
 /* Appends the completed records with a positive weight to out (at most cap;
  * count and wsum accumulate on the device). */
 void launch_guide_collect(const GuideSample* rec, uint32_t n, GuideSample* out, uint32_t* count,
-                          float* wsum, uint32_t cap, cudaStream_t st);
+                          float* wsum, uint32_t cap, float exponent, cudaStream_t st);
 }  // namespace pt
 #endif
 
@@ -233,5 +246,116 @@ PTG_FN void guide_sample(const GuideParams& g, float u0, float u1, float u2, flo
   wy = r * c * ty + r * s * by + w * my;
   wz = r * c * tz + r * s * bz + w * mz;
 }
+
+#ifdef __CUDACC__
+/* ---- packed guide (device) ---------------------------------------------- */
+__device__ __forceinline__ GuidePacked guide_pack(const GuideParams& g) {
+  GuidePacked p;
+  for (int j = 0; j < PTG_LOBES; j++) {
+    __half2 a = __floats2half2_rn(g.lobe[j].x, g.lobe[j].y);
+    __half2 b = __floats2half2_rn(g.lobe[j].z, g.lobe[j].w);
+    p.lobe[j] = make_uint2(*(uint32_t*)&a, *(uint32_t*)&b);
+  }
+  __half2 c0 = __floats2half2_rn(g.cdf[0], g.cdf[1]), c1 = __floats2half2_rn(g.cdf[2], g.cdf[3]);
+  __half2 c2 = __floats2half2_rn(g.cdf[4], g.cdf[5]), c3 = __floats2half2_rn(g.cdf[6], 1.f);
+  p.cdf = make_uint4(*(uint32_t*)&c0, *(uint32_t*)&c1, *(uint32_t*)&c2, *(uint32_t*)&c3);
+  p.alpha = g.alpha;
+  p.pad[0] = p.pad[1] = p.pad[2] = 0u;
+  return p;
+}
+
+/* Shading reads the packed guide with fast intrinsics (rsqrt, exp, divide):
+ * the guide has no bit-exact contract, only that its sampler and its density
+ * agree, which they do to float rounding (both use these same functions). */
+/* Lobe j of a packed guide in global memory: unit mean and concentration. */
+__device__ __forceinline__ void guide_lobe(const GuidePacked* __restrict__ g, int j, float& mx,
+                                           float& my, float& mz, float& k) {
+  uint2 v = __ldg(&g->lobe[j]);
+  float2 a = __half22float2(*(__half2*)&v.x), b = __half22float2(*(__half2*)&v.y);
+  float n2 = a.x * a.x + a.y * a.y + b.x * b.x;
+  if (n2 > 1e-20f) {
+    float inv = rsqrtf(n2);
+    mx = a.x * inv;
+    my = a.y * inv;
+    mz = b.x * inv;
+  } else {
+    mx = 0.f;
+    my = 1.f;
+    mz = 0.f;
+  }
+  k = b.y;
+}
+
+__device__ __forceinline__ void guide_cdf(const GuidePacked* __restrict__ g, float* cdf) {
+  uint4 v = __ldg(&g->cdf);
+  uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    float2 f = __half22float2(*(__half2*)&w[q]);
+    cdf[2 * q] = f.x;
+    cdf[2 * q + 1] = f.y;
+  }
+  cdf[PTG_LOBES - 1] = 1.f;
+}
+
+// vMF density with intrinsics; a series near k = 0 keeps the normaliser
+// k / (1 - e^{-2k}) accurate where the exponential cancels.
+__device__ __forceinline__ float vmf_pdf_fast(float mx, float my, float mz, float k, float wx,
+                                              float wy, float wz) {
+  float c = mx * wx + my * wy + mz * wz;
+  float norm;
+  if (k < 1e-3f) norm = 0.5f + 0.5f * k;  // k / (1 - e^{-2k}) = 1/2 + k/2 + O(k^2)
+  else norm = __fdividef(k, 1.f - __expf(-2.f * k));
+  return norm * 0.15915494309189535f * __expf(k * (c - 1.f));
+}
+
+__device__ __forceinline__ float guide_pdf_packed(const GuidePacked* __restrict__ g, float wx,
+                                                  float wy, float wz) {
+  float cdf[PTG_LOBES];
+  guide_cdf(g, cdf);
+  float p = 0.f, prev = 0.f;
+#pragma unroll
+  for (int j = 0; j < PTG_LOBES; j++) {
+    float mx, my, mz, k;
+    guide_lobe(g, j, mx, my, mz, k);
+    p += (cdf[j] - prev) * vmf_pdf_fast(mx, my, mz, k, wx, wy, wz);
+    prev = cdf[j];
+  }
+  return p;
+}
+
+/* Samples lobe j with probability cdf[j] - cdf[j-1], then the lobe's vMF
+ * (Jakob 2012); the same lobe values as guide_pdf_packed. */
+__device__ __forceinline__ void guide_sample_packed(const GuidePacked* __restrict__ g, float u0,
+                                                    float u1, float u2, float& wx, float& wy,
+                                                    float& wz) {
+  float cdf[PTG_LOBES];
+  guide_cdf(g, cdf);
+  int j = 0;
+#pragma unroll
+  for (int q = 0; q < PTG_LOBES - 1; q++) j += u0 >= cdf[q] ? 1 : 0;
+  float mx, my, mz, k;
+  guide_lobe(g, j, mx, my, mz, k);
+  float w;
+  if (k < 1e-3f) {
+    // series of log(u + (1-u) e^{-2k}) / k for small k: -2(1-u) + ...; the
+    // uniform limit at k -> 0
+    w = 1.f - 2.f * (1.f - u1) * (1.f - k * u1);
+  } else {
+    w = 1.f + __logf(u1 + (1.f - u1) * __expf(-2.f * k)) / k;
+  }
+  w = fminf(fmaxf(w, -1.f), 1.f);
+  float r = sqrtf(fmaxf(0.f, 1.f - w * w));
+  float s, c;
+  __sincosf(6.283185307179586f * u2, &s, &c);
+  float sign = mz >= 0.f ? 1.f : -1.f;
+  float a = -1.f / (sign + mz), b = mx * my * a;
+  float tx = 1.f + sign * mx * mx * a, ty = sign * b, tz = -sign * mx;
+  float bx = b, by = sign + my * my * a, bz = -my;
+  wx = r * c * tx + r * s * bx + w * mx;
+  wy = r * c * ty + r * s * by + w * my;
+  wz = r * c * tz + r * s * bz + w * mz;
+}
+#endif
 
 #endif

@@ -128,7 +128,8 @@ int pth::guide_frame_train(pt_context* ctx) {
   const uint32_t cap = 1u << 18;
   GK(cudaMemsetAsync(G.counters.p, 0, 4, st));  // the failure flags stay
   GK(cudaMemsetAsync(G.scalars.p, 0, 8, st));
-  pt::launch_guide_collect(G.rec.p, G.rec_n, G.samples.p, G.counters.p, G.scalars.p + 1, cap, st);
+  pt::launch_guide_collect(G.rec.p, G.rec_n, G.samples.p, G.counters.p, G.scalars.p + 1, cap,
+                           G.exponent, st);
   GuideTrainArgs a;
   memset(&a, 0, sizeof(a));
   a.w = (const __nv_bfloat16*)G.wbf.p;
@@ -142,24 +143,26 @@ int pth::guide_frame_train(pt_context* ctx) {
   a.train = 1;
   a.max_count = cap;
   a.fail = G.counters.p + 1;
-  pt::launch_guide_grad(a, G.grid, st);
-  GuideAdamArgs d;
-  memset(&d, 0, sizeof(d));
-  d.partial = G.partial.p;
-  d.nparts = G.grid;
-  d.w32 = G.w32.p;
-  d.wbf = (__nv_bfloat16*)G.wbf.p;
-  d.m = G.m.p;
-  d.v = G.v.p;
-  d.update = 1;
-  G.step++;
-  d.lr = G.lr;
-  d.b1 = 0.9f;
-  d.b2 = 0.99f;
-  d.eps = 1e-8f;
-  d.bc1 = 1.f - powf(d.b1, (float)G.step);
-  d.bc2 = 1.f - powf(d.b2, (float)G.step);
-  pt::launch_guide_adam(d, st);
+  for (int k = 0; k < G.steps; k++) {
+    pt::launch_guide_grad(a, G.grid, st);
+    GuideAdamArgs d;
+    memset(&d, 0, sizeof(d));
+    d.partial = G.partial.p;
+    d.nparts = G.grid;
+    d.w32 = G.w32.p;
+    d.wbf = (__nv_bfloat16*)G.wbf.p;
+    d.m = G.m.p;
+    d.v = G.v.p;
+    d.update = 1;
+    G.step++;
+    d.lr = G.lr;
+    d.b1 = 0.9f;
+    d.b2 = 0.99f;
+    d.eps = 1e-8f;
+    d.bc1 = 1.f - powf(d.b1, (float)G.step);
+    d.bc2 = 1.f - powf(d.b2, (float)G.step);
+    pt::launch_guide_adam(d, st);
+  }
   GK(cudaGetLastError());
   return PT_OK;
 }
@@ -257,7 +260,8 @@ PT_API int pt_guide_init(pt_context* ctx, uint64_t seed) {
   int rc = guide_prepare(ctx);
   if (rc) return rc;
   // He-uniform hidden layers; a small last layer so the first mixture is
-  // broad (concentration ~1, equal weights, alpha = 0.5); biases zero
+  // broad (concentration ~1, equal weights, alpha = 0.5); biases zero.  The
+  // training options keep their values.
   Mix64 r{seed ^ 0x6A09E667F3BCC909ull};
   std::vector<float> w(PTG_PARAMS, 0.f);
   for (int l = 0; l < 5; l++) {
@@ -269,6 +273,17 @@ PT_API int pt_guide_init(pt_context* ctx, uint64_t seed) {
         w[PTG_LAYER_OFF(l) + i * PTG_K + c] = (2.f * r.uniform() - 1.f) * lim;
   }
   return upload_params(ctx, w);
+}
+
+PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent) {
+  if (!ctx) return PT_EINVAL;
+  if (!(lr > 0.f) || lr > 1.f || steps_per_frame < 1 || steps_per_frame > 64 ||
+      !(exponent > 0.f) || exponent > 1.f)
+    return gfail(ctx, PT_EINVAL, "guide training: lr in (0,1], 1..64 steps, exponent in (0,1]");
+  ctx->guide.lr = lr;
+  ctx->guide.steps = steps_per_frame;
+  ctx->guide.exponent = exponent;
+  return PT_OK;
 }
 
 PT_API int pt_guide_get_params(pt_context* ctx, float* params) {

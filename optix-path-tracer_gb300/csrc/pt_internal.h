@@ -132,7 +132,7 @@ struct ShadowBuf {
   uint4* st;
 };
 
-struct GuideParams;
+struct GuidePacked;
 struct GuideSample;
 struct GuideInferArgs;
 
@@ -145,7 +145,7 @@ struct WaveState {
   int slots;                  /* capacity of each buffer */
   /* learned guide (consistent mode, guide = 1): decoded guide by position;
    * training records, 2 per recording path (path id % grec_stride == 0) */
-  GuideParams* guide;
+  GuidePacked* guide;
   GuideSample* grec;
   uint32_t grec_stride, grec_n;
 };

@@ -1159,8 +1159,8 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
       } else {
         Frame fr(N);
         V3 wo_l = fr.to_local(Wo);
-        GuideParams G;
-        if (GUIDE) G = W.guide[i];
+        const GuidePacked* G = GUIDE ? W.guide + i : nullptr;
+        const float G_alpha = GUIDE ? __ldg(&G->alpha) : 0.f;
         if (n_sel > 0) {
           int k = (int)(rnd(st.x) * (float)n_sel);
           if (k > n_sel - 1) k = n_sel - 1;
@@ -1197,7 +1197,8 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
             V3 wi_l = fr.to_local(wi_n);
             V3 f = bsdf_f_c(m, wo_l, wi_l);
             float pbs = bsdf_pdf_c(m, wo_l, wi_l);
-            if (GUIDE) pbs = G.alpha * guide_pdf(G, wi_n.x, wi_n.y, wi_n.z) + (1.f - G.alpha) * pbs;
+            if (GUIDE)
+              pbs = G_alpha * guide_pdf_packed(G, wi_n.x, wi_n.y, wi_n.z) + (1.f - G_alpha) * pbs;
             V3 cv = f * Le * (cs * power_mis(pls, pbs) / pls);
             if (!isNull(cv)) {
               shadow = true;
@@ -1206,11 +1207,11 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
           }
         }
         V3 wi_l, wdir;
-        if (GUIDE && rnd(st.x) < G.alpha) {
+        if (GUIDE && rnd(st.x) < G_alpha) {
           float u0 = rnd(st.x);
           float u1 = rnd(st.x);
           float u2 = rnd(st.x);
-          guide_sample(G, u0, u1, u2, wdir.x, wdir.y, wdir.z);
+          guide_sample_packed(G, u0, u1, u2, wdir.x, wdir.y, wdir.z);
           wi_l = fr.to_local(wdir);
         } else {
           wi_l = bsdf_sample_c(m, wo_l, st.x);
@@ -1218,7 +1219,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
         }
         float pbs = bsdf_pdf_c(m, wo_l, wi_l);
         float q = pbs;
-        if (GUIDE) q = G.alpha * guide_pdf(G, wdir.x, wdir.y, wdir.z) + (1.f - G.alpha) * pbs;
+        if (GUIDE) q = G_alpha * guide_pdf_packed(G, wdir.x, wdir.y, wdir.z) + (1.f - G_alpha) * pbs;
         V3 f = bsdf_f_c(m, wo_l, wi_l);
         if (!(q > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
           ended = true;

@@ -12,6 +12,12 @@ bounded sample of the same workload with all host threads.
 `--workload batch` is the batched multi-scene configuration: 64 seeded
 heightfield scenes (1e3..1e6 triangles, 256^2..1024^2, 16..256 spp) in one
 pt_batch_render per step, after pt_batch_autotune.
+
+`--workload guide` is the learned-guide configuration: the heightfield in a
+closed box lit through a 0.5 % opening, 1920x1080, consistent mode with the
+guide trained online; one step = 16 guided frames.  After the timed steps it
+compares guided and plain MIS at equal device time against a high-spp FP64
+plain render (relMSE, eps 1e-2).
 """
 import argparse
 import json
@@ -47,6 +53,12 @@ BATCH_DESC = ("batched multi-scene render: 64 seeded heightfield scenes, triangl
               "max depth 50, RR after depth 10; one pt_batch_render (one CUDA-graph launch) "
               "per step")
 BATCH_KW = dict(max_depth=50, rr_depth=10, mode=1)
+GUIDE_DESC = ("learned-guide form: 2,097,152-triangle heightfield (TS/AS/ON tiles) inside a closed "
+              "white Lambertian box lit only through a ceiling opening of 0.5 % of the box area "
+              "onto a 2048x1024 HDR sky; 1920x1080, consistent mode (NEE + MIS), max depth 50, "
+              "RR after depth 10; MLP 76 -> 4x64 -> 8 vMF lobes + selection, BF16 tensor-core "
+              "inference and training (<= 2^18 samples per frame, 8 Adam steps per frame, "
+              "lr 1e-2); one step = 16 guided frames")
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
@@ -516,6 +528,111 @@ def run_batch(args):
         torch.distributed.destroy_process_group()
 
 
+def run_guide(args):
+    import numpy as np
+    import torch
+    import ptgb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    W, H = 1920, 1080
+    kw = dict(max_depth=50, rr_depth=10, mode=1)
+    scene = ptgb.guide_box_scene(W, H)
+    P = ptgb.GpuRenderer.params
+    g = ptgb.GpuRenderer(scene, device=local)
+    g.guide_init(1)
+    acc = torch.zeros((H, W, 4), dtype=torch.float64, device=f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    spp_step = 16
+    base = rank * 100000
+    frame = 0
+    for _ in range(args.warmup):
+        g.render64(P(W, H, spp_step, frame0=base + frame, guide=1, **kw), acc.data_ptr())
+        frame += spp_step
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    dev_ms, paths, rays, launches = 0.0, 0, 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        g.render64(P(W, H, spp_step, frame0=base + frame, guide=1, **kw), acc.data_ptr())
+        frame += spp_step
+        st = g.stats()
+        dev_ms += st["render_ms"]
+        paths += st["paths"]
+        rays += st["ext_rays"] + st["shadow_rays"]
+        launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    value = paths / (dev_ms / 1e3)
+
+    # ---- equal-time study (rank 0): plain and guided (fresh guide) against
+    # an FP64 plain reference of --ref-spp frames
+    study = None
+    if rank == 0:
+        ref_r = ptgb.GpuRenderer(scene, device=local)
+        t_ref = time.perf_counter()
+        ref = ref_r.render64(P(W, H, args.ref_spp, frame0=1 << 24, **kw)) / args.ref_spp
+        t_ref = time.perf_counter() - t_ref
+        curves = {}
+        for guide in (0, 1):
+            r = ref_r if guide == 0 else ptgb.GpuRenderer(scene, device=local)
+            if guide:
+                r.guide_init(1)
+            a = np.zeros((H, W, 4))
+            done, tt, pts = 0, 0.0, []
+            for chunk in (4, 4, 8, 16, 32, 64):
+                img = r.render64(P(W, H, chunk, frame0=done, guide=guide, **kw))
+                tt += r.stats()["render_ms"]
+                a[..., :3] += img[..., :3]
+                done += chunk
+                pts.append((tt, ptgb.rel_mse(a / done, ref), done))
+            curves[guide] = pts
+            if guide:
+                r.close()
+        ref_r.close()
+        gt = np.array([p[0] for p in curves[1]])
+        ge = np.array([p[1] for p in curves[1]])
+        t_plain, e_plain, spp_plain = curves[0][-1]
+        if ge.min() <= e_plain:
+            t_guided = float(np.exp(np.interp(np.log(e_plain), np.log(ge[::-1]), np.log(gt[::-1]))))
+        else:  # extrapolate along relMSE ~ 1/time from the last point
+            t_guided = float(gt[-1] * ge[-1] / e_plain)
+        study = {"reference": f"plain consistent render, {args.ref_spp} spp, FP64 sums "
+                              f"({t_ref:.0f} s); the configuration names 16384 spp",
+                 "relmse_eps": 1e-2,
+                 "plain": [{"ms": round(t, 1), "relmse": e, "spp": n} for t, e, n in curves[0]],
+                 "guided": [{"ms": round(t, 1), "relmse": e, "spp": n} for t, e, n in curves[1]],
+                 "plain_final_relmse": e_plain,
+                 "guided_time_to_plain_final_ms": t_guided,
+                 "plain_time_ms": t_plain,
+                 "time_ratio": t_guided / t_plain}
+
+    if rank == 0:
+        line = {
+            "metric": "paths/s", "value": value, "unit": "paths/s",
+            "mrays_per_s": rays / (dev_ms / 1e3) / 1e6, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP bf16, fp32 accumulation)",
+            "data": "synthetic",
+            "config": {"workload": GUIDE_DESC, "frames_per_step": spp_step,
+                       "l2": "flushed between steps (256 MiB write); per-step working set exceeds L2",
+                       "parallelism": f"replicas{world}" if world > 1 else "single"},
+            "e2e": None, "gpu_launches": launches, "roofline": None, "cpu_baseline": None,
+            "equal_time": study, "wall_s": wall, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -523,13 +640,23 @@ def main():
                     help="timed steps (default 5; 2 for the batch workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS) + ["batch", "guide"])
+    ap.add_argument("--ref-spp", type=int, default=1024,
+                    help="guide workload: spp of the FP64 plain reference")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spp", type=int, default=0, help="override spp (small profiling cases)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 2 if args.workload == "batch" else 5
+    if args.workload == "guide":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the learned guide has no "
+                              "counterpart in the reference (plain MIS is its own arm: "
+                              "--workload heightfield)"}), flush=True)
+        else:
+            run_guide(args)
+        return
     if args.workload == "batch":
         if args.impl == "reference":
             run_reference(args, ("batch_workload", 0, 0, 0, BATCH_KW, BATCH_DESC))

@@ -245,11 +245,14 @@ PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params* params, fl
 #define PT_GUIDE_SAMPLE_FLOATS 16
 /* Seeded He-uniform initialisation; resets the Adam state. */
 PT_API int pt_guide_init(pt_context* ctx, uint64_t seed);
-/* Online training during guided renders: Adam learning rate (default 1e-2),
- * Adam steps per frame on that frame's samples (1), and the exponent applied
- * to the sample weights F/q (1 = the KL target; below 1 tempers the heavy
- * tail of bright, rare paths).  Defaults: 1e-2, 8 steps, exponent 1. */
-PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent);
+/* Online training during guided renders: Adam learning rate, Adam steps
+ * per frame on that frame's samples, the exponent applied to the sample
+ * weights F/q (1 = the KL target; below 1 tempers the heavy tail of bright,
+ * rare paths), and how many bounces of a path are guided (0 = all; deeper
+ * bounces sample the BSDF alone).  Defaults: 1e-2, 8 steps, exponent 1,
+ * 4 bounces. */
+PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent,
+                                 int max_bounces);
 PT_API int pt_guide_get_params(pt_context* ctx, float* params);
 PT_API int pt_guide_set_params(pt_context* ctx, const float* params);
 /* Scene box of the position encoding: x01 = (p - bmin) * binv. */

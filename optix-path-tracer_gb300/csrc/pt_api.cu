@@ -805,6 +805,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   ctl.rr_depth = p->rr_depth;
   ctl.mode = p->mode;
   ctl.guide = p->guide;
+  ctl.guide_depth = ctx->guide.max_bounces > 0 ? (uint32_t)ctx->guide.max_bounces : 0xffffffffu;
   ctl.chunk_paths = (unsigned long long)p->width * p->height * frames;
   fastdiv_magic((uint32_t)(p->width * p->height), &ctl.wh_m, &ctl.wh_l);
   fastdiv_magic((uint32_t)p->width, &ctl.w_m, &ctl.w_l);

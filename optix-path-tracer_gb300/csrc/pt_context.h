@@ -70,6 +70,7 @@ struct GuideState {
   float lr = 1e-2f;          // Adam learning rate of the online training
   int steps = 8;             // Adam steps per frame on the frame's samples
   float exponent = 1.f;      // training weight = (F/q)^exponent (1: the KL target)
+  int max_bounces = 4;       // guided bounces per path (0: all)
   float bmin[3] = {0, 0, 0}, binv[3] = {1, 1, 1};
   int step = 0;
   int grid = 0;

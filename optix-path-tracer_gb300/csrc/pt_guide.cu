@@ -109,11 +109,72 @@ __device__ __forceinline__ uint32_t core_off(int r, int c, int C) {
   return (uint32_t)(((r >> 3) * (C >> 3) + (c >> 3)) * 128 + (r & 7) * 16 + (c & 7) * 2);
 }
 
-__device__ __forceinline__ void st_bf16(unsigned char* tile, int r, int c, int C, float v) {
-  *(__nv_bfloat16*)(tile + core_off(r, c, C)) = __float2bfloat16_rn(v);
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *(uint32_t*)&h;
 }
-__device__ __forceinline__ float ld_bf16(const unsigned char* tile, int r, int c, int C) {
-  return __bfloat162float(*(const __nv_bfloat16*)(tile + core_off(r, c, C)));
+// 8 consecutive columns (c0 % 8 == 0) of row r of a C-column tile, one
+// 16-byte access.
+__device__ __forceinline__ void st_row8c(unsigned char* tile, int r, int c0, int C, const float* v) {
+  uint4 q = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                       pack_bf16x2(v[6], v[7]));
+  *(uint4*)(tile + core_off(r, c0, C)) = q;
+}
+__device__ __forceinline__ void ld_row8c(const unsigned char* tile, int r, int c0, int C, float* v) {
+  uint4 q = *(const uint4*)(tile + core_off(r, c0, C));
+  uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    float2 f = __bfloat1622float2(*(__nv_bfloat162*)&w[k]);
+    v[2 * k] = f.x;
+    v[2 * k + 1] = f.y;
+  }
+}
+
+__device__ __forceinline__ void st_row8(unsigned char* tile, int r, int c0, const float* v) {
+  st_row8c(tile, r, c0, PTG_K, v);
+}
+
+// The feature row of guide_features, written 8 columns at a time (the same
+// arithmetic, so inference and training see identical features), then the
+// ones column and padding.
+__device__ void write_features_vec(unsigned char* T, int row, const float* P, const float* N,
+                                   const float* Wo, const float* bmin, const float* binv,
+                                   bool valid) {
+  float v[8];
+  if (!valid) {
+    for (int q = 0; q < 8; q++) v[q] = 0.f;
+    for (int c0 = 0; c0 < 72; c0 += 8) st_row8(T, row, c0, v);
+  } else {
+    for (int a = 0; a < 3; a++) {
+      float x = (P[a] - bmin[a]) * binv[a];
+      x = fminf(fmaxf(x, 0.f), 1.f);
+      float s, c;
+      sincospif(x, &s, &c);
+      for (int k = 0; k < PTG_FREQ; k++) {
+        v[(2 * k) & 7] = s;
+        v[(2 * k + 1) & 7] = c;
+        if (((2 * k + 2) & 7) == 0) st_row8(T, row, a * 2 * PTG_FREQ + 2 * k - 6, v);
+        float s2 = 2.f * s * c, c2 = 1.f - 2.f * s * s;
+        s = s2;
+        c = c2;
+      }
+    }
+  }
+  // 72..75 directions, 76 one, 77..79 zero
+  for (int q = 0; q < 8; q++) v[q] = 0.f;
+  if (valid) {
+    const float* dirs[2] = {N, Wo};
+    for (int q = 0; q < 2; q++) {
+      const float* d = dirs[q];
+      float y = fminf(fmaxf(d[1], -1.f), 1.f);
+      v[2 * q] = acosf(y) * 0.31830988618379067f;
+      v[2 * q + 1] = atan2f(d[2], d[0]) * 0.15915494309189535f + 0.5f;
+    }
+  }
+  v[4] = 1.f;
+  st_row8(T, row, 72, v);
 }
 
 // Tile sizes (bytes).
@@ -156,20 +217,7 @@ __device__ __forceinline__ void issue_forward(uint32_t tmem, const unsigned char
         sdesc(tw + ks * 256, 128, (PTG_K / 8) * 128), id, ks > 0 ? 1u : 0u);
 }
 
-// Row `row` of a 128 x 80 activation tile from 64 values (ReLU applied by
-// the caller), the ones column and zero padding.
-__device__ __forceinline__ void write_hidden_row(unsigned char* T, int row, const float* h) {
-  for (int c = 0; c < PTG_H; c++) st_bf16(T, row, c, PTG_K, h[c]);
-  st_bf16(T, row, PTG_H, PTG_K, 1.f);
-  for (int c = PTG_H + 1; c < PTG_K; c++) st_bf16(T, row, c, PTG_K, 0.f);
-}
 
-__device__ __forceinline__ void write_feature_row(unsigned char* T, int row, const float* f,
-                                                  bool valid) {
-  for (int c = 0; c < PTG_FEAT; c++) st_bf16(T, row, c, PTG_K, valid ? f[c] : 0.f);
-  st_bf16(T, row, PTG_FEAT, PTG_K, 1.f);
-  for (int c = PTG_FEAT + 1; c < PTG_K; c++) st_bf16(T, row, c, PTG_K, 0.f);
-}
 
 struct TmemGuard {
   uint64_t mbar;
@@ -199,11 +247,19 @@ __device__ bool forward_tile(uint32_t tmem, TmemGuard& g, uint32_t& phase, unsig
     fence_after();
     if (!__syncthreads_and(ok)) return false;
     if (l < 4) {
-      float h[PTG_H];
-      for (int c0 = 0; c0 < PTG_H; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, h + c0);
-      for (int c = 0; c < PTG_H; c++) h[c] = fmaxf(h[c], 0.f);
       unsigned char* dst = T[nT == 5 ? l + 1 : ((l + 1) & 1)];
-      write_hidden_row(dst, row, h);
+      float h[16];
+      for (int c0 = 0; c0 < PTG_H; c0 += 16) {
+        tmem_ld16(tmem + lane_base + kTmemAcc + c0, h);
+        for (int q = 0; q < 16; q++) h[q] = fmaxf(h[q], 0.f);
+        st_row8c(dst, row, c0, PTG_K, h);
+        st_row8c(dst, row, c0 + 8, PTG_K, h + 8);
+      }
+      for (int q = 0; q < 16; q++) h[q] = 0.f;
+      h[0] = 1.f;
+      st_row8c(dst, row, PTG_H, PTG_K, h);
+      h[0] = 0.f;
+      st_row8c(dst, row, PTG_H + 8, PTG_K, h);
     } else {
       for (int c0 = 0; c0 < PTG_NOUT; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, out + c0);
     }
@@ -300,11 +356,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
   for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
     const uint32_t s = tile * 128 + tid;
     const bool valid = s < n;
-    GuideSample smp;
+    GuideSample smp = {};
     if (valid) smp = A.samples[s];
-    float f[PTG_FEAT];
-    if (valid) guide_features(smp.P, smp.N, smp.Wo, A.bmin, A.binv, f);
-    write_feature_row(T[0], tid, f, valid);
+    write_features_vec(T[0], tid, smp.P, smp.N, smp.Wo, A.bmin, A.binv, valid);
     float o[PTG_NOUT];
     if (!forward_tile(tmem, g, phase, W, T, 5, o)) {
       failed = true;
@@ -318,7 +372,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
     float wn = valid && wsum > 0.f ? smp.weight / wsum : 0.f;
     loss_acc += valid ? loss_grad(o, smp.wi[0], smp.wi[1], smp.wi[2], smp.p_bsdf, wn, d)
                       : loss_grad(o, 0.f, 1.f, 0.f, 0.f, 0.f, d);
-    for (int k = 0; k < PTG_NOUT; k++) st_bf16(Gt, tid, k, PTG_NOUT, d[k]);
+    for (int k = 0; k < PTG_NOUT; k += 8) st_row8c(Gt, tid, k, PTG_NOUT, d + k);
     // ---- backward, layer 4 .. 0
     unsigned char* G = Gt;
     unsigned char* Gnext = Gn;
@@ -358,11 +412,14 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
       }
       if (l > 0) {
         // G_{l-1} = dT_l * (T_l > 0), into the other gradient tile
-        float h[PTG_H];
-        for (int c0 = 0; c0 < PTG_H; c0 += 16) tmem_ld16(tmem + lane_base + kTmemAcc + c0, h + c0);
-        for (int c = 0; c < PTG_H; c++) {
-          float t = ld_bf16(T[l], tid, c, PTG_K);
-          st_bf16(Gnext, tid, c, PTG_H, t > 0.f ? h[c] : 0.f);
+        float h[16], t[8];
+        for (int c0 = 0; c0 < PTG_H; c0 += 16) {
+          tmem_ld16(tmem + lane_base + kTmemAcc + c0, h);
+          for (int half = 0; half < 2; half++) {
+            ld_row8c(T[l], tid, c0 + 8 * half, PTG_K, t);
+            for (int q = 0; q < 8; q++) h[8 * half + q] = t[q] > 0.f ? h[8 * half + q] : 0.f;
+            st_row8c(Gnext, tid, c0 + 8 * half, PTG_H, h + 8 * half);
+          }
         }
         unsigned char* tmp = G;
         G = Gnext;
@@ -441,57 +498,6 @@ __device__ __forceinline__ bool group_and(bool v, int id) {
   return r != 0;
 }
 
-__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *(uint32_t*)&h;
-}
-// 8 consecutive columns (c0 % 8 == 0) of row r as one 16-byte store.
-__device__ __forceinline__ void st_row8(unsigned char* tile, int r, int c0, const float* v) {
-  uint4 q = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
-                       pack_bf16x2(v[6], v[7]));
-  *(uint4*)(tile + core_off(r, c0, PTG_K)) = q;
-}
-
-// The feature row of guide_features, written 8 columns at a time (the same
-// arithmetic, so inference and training see identical features), then the
-// ones column and padding.
-__device__ void write_features_vec(unsigned char* T, int row, const float* P, const float* N,
-                                   const float* Wo, const float* bmin, const float* binv,
-                                   bool valid) {
-  float v[8];
-  if (!valid) {
-    for (int q = 0; q < 8; q++) v[q] = 0.f;
-    for (int c0 = 0; c0 < 72; c0 += 8) st_row8(T, row, c0, v);
-  } else {
-    for (int a = 0; a < 3; a++) {
-      float x = (P[a] - bmin[a]) * binv[a];
-      x = fminf(fmaxf(x, 0.f), 1.f);
-      float s, c;
-      sincospif(x, &s, &c);
-      for (int k = 0; k < PTG_FREQ; k++) {
-        v[(2 * k) & 7] = s;
-        v[(2 * k + 1) & 7] = c;
-        if (((2 * k + 2) & 7) == 0) st_row8(T, row, a * 2 * PTG_FREQ + 2 * k - 6, v);
-        float s2 = 2.f * s * c, c2 = 1.f - 2.f * s * s;
-        s = s2;
-        c = c2;
-      }
-    }
-  }
-  // 72..75 directions, 76 one, 77..79 zero
-  for (int q = 0; q < 8; q++) v[q] = 0.f;
-  if (valid) {
-    const float* dirs[2] = {N, Wo};
-    for (int q = 0; q < 2; q++) {
-      const float* d = dirs[q];
-      float y = fminf(fmaxf(d[1], -1.f), 1.f);
-      v[2 * q] = acosf(y) * 0.31830988618379067f;
-      v[2 * q + 1] = atan2f(d[2], d[0]) * 0.15915494309189535f + 0.5f;
-    }
-  }
-  v[4] = 1.f;
-  st_row8(T, row, 72, v);
-}
 
 // Inference inside the wavefront, one row per live path of the current
 // buffer; rows whose hit is a guided (non-delta) material get their packed
@@ -540,7 +546,7 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
     const uint32_t i = tile * 128 + row;
     bool valid = false;
     float P[3], N[3], Wo[3];
-    if (i < n) {
+    if (i < n && (pb.st[i].z & PT_ST_DEPTH_MASK) < ctl.guide_depth) {
       float4 hit = W.hit[i];
       uint32_t leaf = __float_as_uint(hit.w);
       if (leaf != PT_NO_HIT) {
@@ -557,6 +563,8 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
         }
       }
     }
+    // a pipeline whose 128 rows all need no guide skips the network
+    if (group_and(!valid, bar_id)) continue;
     write_features_vec(T, row, P, N, Wo, A.bmin, A.binv, valid);
     float o[PTG_NOUT];
     for (int l = 0; l < 5 && !failed; l++) {

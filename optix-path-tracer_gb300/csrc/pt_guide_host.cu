@@ -275,14 +275,17 @@ PT_API int pt_guide_init(pt_context* ctx, uint64_t seed) {
   return upload_params(ctx, w);
 }
 
-PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent) {
+PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent,
+                                 int max_bounces) {
   if (!ctx) return PT_EINVAL;
   if (!(lr > 0.f) || lr > 1.f || steps_per_frame < 1 || steps_per_frame > 64 ||
-      !(exponent > 0.f) || exponent > 1.f)
-    return gfail(ctx, PT_EINVAL, "guide training: lr in (0,1], 1..64 steps, exponent in (0,1]");
+      !(exponent > 0.f) || exponent > 1.f || max_bounces < 0)
+    return gfail(ctx, PT_EINVAL,
+                 "guide training: lr in (0,1], 1..64 steps, exponent in (0,1], bounces >= 0");
   ctx->guide.lr = lr;
   ctx->guide.steps = steps_per_frame;
   ctx->guide.exponent = exponent;
+  ctx->guide.max_bounces = max_bounces;
   return PT_OK;
 }
 

@@ -60,7 +60,8 @@ struct WaveCtl {
   unsigned long long chunk_paths; /* paths in this chunk */
   uint32_t wh_m, wh_l, w_m, w_l;  /* invariant-divisor constants for W*H and W */
   /* batch: segments [seg_begin, seg_end) make up this chunk, `pixels` pixels */
-  uint32_t seg_begin, seg_end, pixels, pad;
+  uint32_t seg_begin, seg_end, pixels;
+  uint32_t guide_depth;           /* guided bounces: depth < guide_depth */
   unsigned long long max_iter;    /* device-side iteration bound of this chunk */
 };
 

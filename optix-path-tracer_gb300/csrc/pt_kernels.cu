@@ -1159,8 +1159,10 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
       } else {
         Frame fr(N);
         V3 wo_l = fr.to_local(Wo);
+        // bounces past the guided depth use the BSDF alone (alpha = 0)
+        const bool guided = GUIDE && depth < ctl.guide_depth;
         const GuidePacked* G = GUIDE ? W.guide + i : nullptr;
-        const float G_alpha = GUIDE ? __ldg(&G->alpha) : 0.f;
+        const float G_alpha = guided ? __ldg(&G->alpha) : 0.f;
         if (n_sel > 0) {
           int k = (int)(rnd(st.x) * (float)n_sel);
           if (k > n_sel - 1) k = n_sel - 1;
@@ -1197,7 +1199,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
             V3 wi_l = fr.to_local(wi_n);
             V3 f = bsdf_f_c(m, wo_l, wi_l);
             float pbs = bsdf_pdf_c(m, wo_l, wi_l);
-            if (GUIDE)
+            if (guided)
               pbs = G_alpha * guide_pdf_packed(G, wi_n.x, wi_n.y, wi_n.z) + (1.f - G_alpha) * pbs;
             V3 cv = f * Le * (cs * power_mis(pls, pbs) / pls);
             if (!isNull(cv)) {
@@ -1207,7 +1209,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
           }
         }
         V3 wi_l, wdir;
-        if (GUIDE && rnd(st.x) < G_alpha) {
+        if (guided && rnd(st.x) < G_alpha) {
           float u0 = rnd(st.x);
           float u1 = rnd(st.x);
           float u2 = rnd(st.x);
@@ -1219,12 +1221,12 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
         }
         float pbs = bsdf_pdf_c(m, wo_l, wi_l);
         float q = pbs;
-        if (GUIDE) q = G_alpha * guide_pdf_packed(G, wdir.x, wdir.y, wdir.z) + (1.f - G_alpha) * pbs;
+        if (guided) q = G_alpha * guide_pdf_packed(G, wdir.x, wdir.y, wdir.z) + (1.f - G_alpha) * pbs;
         V3 f = bsdf_f_c(m, wo_l, wi_l);
         if (!(q > 0.f) || isNull(f) || !(wi_l.y > 0.f)) {
           ended = true;
         } else {
-          if (GUIDE) {
+          if (guided) {
             int count = (int)code >> 1;
             code = (float)(2 * count);
             if (count < 2 && st.y % W.grec_stride == 0) {

@@ -110,7 +110,7 @@ SIGNATURES = {
     "pt_get_stats": [_P, ctypes.POINTER(Stats)],
     "pt_render_noalloc": [_P, ctypes.POINTER(RenderParams), _P, _P],
     "pt_guide_init": [_P, ctypes.c_uint64],
-    "pt_guide_set_training": [_P, ctypes.c_float, ctypes.c_int, ctypes.c_float],
+    "pt_guide_set_training": [_P, ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int],
     "pt_guide_get_params": [_P, _P],
     "pt_guide_set_params": [_P, _P],
     "pt_guide_bounds": [_P, _P, _P],
@@ -424,8 +424,8 @@ class GpuRenderer:
     def guide_init(self, seed=0):
         self._c(self.lib.pt_guide_init(self.ctx, seed))
 
-    def guide_training(self, lr=1e-2, steps=1, exponent=1.0):
-        self._c(self.lib.pt_guide_set_training(self.ctx, lr, steps, exponent))
+    def guide_training(self, lr=1e-2, steps=8, exponent=1.0, max_bounces=4):
+        self._c(self.lib.pt_guide_set_training(self.ctx, lr, steps, exponent, max_bounces))
 
     def guide_params(self):
         out = np.zeros(self.GUIDE_PARAMS, np.float32)

@@ -587,7 +587,7 @@ def run_guide(args):
                 r.guide_init(1)
             a = np.zeros((H, W, 4))
             done, tt, pts = 0, 0.0, []
-            for chunk in (4, 4, 8, 16, 32, 64):
+            for chunk in (4, 4, 8, 16, 32, 64, 128):
                 img = r.render64(P(W, H, chunk, frame0=done, guide=guide, **kw))
                 tt += r.stats()["render_ms"]
                 a[..., :3] += img[..., :3]

@@ -35,6 +35,10 @@ namespace {
 const float PI_F = 3.141592654f;
 }  // namespace
 
+#ifndef PT_TREELET_ROUNDS
+#define PT_TREELET_ROUNDS 4  /* SAH treelet restructuring passes of the GPU builder */
+#endif
+
 using namespace pth;
 
 static int fail(pt_context* ctx, int code, const std::string& msg) {
@@ -606,7 +610,7 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
     uint32_t nodes = 0;
     int depth = 0;
     CK(pt::build_bvh8_gpu(ctx->d_rec_in.p, ctx->d_xforms.p, (uint32_t)n, d_nodes.p,
-                          d_prims.p, d_leaf_of_id.p, &nodes, &depth, 2, width, st));
+                          d_prims.p, d_leaf_of_id.p, &nodes, &depth, PT_TREELET_ROUNDS, width, st));
     if (depth < 0)
       return fail(ctx, PT_EINVAL,
                   "GPU BVH8 failed validation (collapse check " + std::to_string(-depth) + ")");

@@ -422,6 +422,14 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         best_id = (uint32_t)k;
       }
     }
+    // ---- consistent-mode shadow rays ask only whether anything lies before
+    // tmax: the first confirmed hit ends the ray
+    if (consistent && active && best_id != PT_NO_HIT) {
+      finish();
+      i += stride;
+      active = false;
+      idle = true;
+    }
     // ---- next node: nearest internal child, else the deepest pending group
     if (active) {
       if (nint == 1) {

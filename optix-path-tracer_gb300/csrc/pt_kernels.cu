@@ -80,6 +80,31 @@ struct WarpShared {
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
 
+// Three-input max / min (one instruction each on sm_100+) and the paired
+// FP32 fused multiply-add: a node step evaluates 8 children x 3 axes of
+// (near, far) slab distances, so pairs share one instruction.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+// (a.x * s + t, a.y * s + t), each rounded once.
+__device__ __forceinline__ float2 fma2s(float ax, float ay, float s, float t) {
+  unsigned long long a, b, c, d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(ax), "f"(ay));
+  asm("mov.b64 %0, {%1, %1};" : "=l"(b) : "f"(s));
+  asm("mov.b64 %0, {%1, %1};" : "=l"(c) : "f"(t));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
+  return r;
+}
+
 __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
   uint32_t lo = min(a, b), hi = max(a, b);
   a = lo;
@@ -322,14 +347,14 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       for (int k = 0; k < 8; k++) {
         const uint32_t sel = 0x7604u | ((uint32_t)(k & 3) << 4);
         uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
-        float tnx = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x3F800000u, sel)), Ax, Bx);
-        float tfx = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x3F800000u, sel)), Ax, Bx);
-        float tny = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x3F800000u, sel)), Ay, By);
-        float tfy = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x3F800000u, sel)), Ay, By);
-        float tnz = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x3F800000u, sel)), Az, Bz);
-        float tfz = __fmaf_rn(__uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
-        float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-        float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
+        float2 tx = fma2s(__uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x3F800000u, sel)),
+                          __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x3F800000u, sel)), Ax, Bx);
+        float2 ty = fma2s(__uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x3F800000u, sel)),
+                          __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x3F800000u, sel)), Ay, By);
+        float2 tz = fma2s(__uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x3F800000u, sel)),
+                          __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
+        float tn = max3f(tx.x, ty.x, fmaxf(tz.x, tmin));
+        float tf = min3f(tx.y, ty.y, fminf(tz.y, tlim));
         if (meta != 0 && tn <= tf) {
           if (meta & 0x80u) {
             uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);

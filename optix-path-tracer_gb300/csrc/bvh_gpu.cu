@@ -3,7 +3,8 @@
  * reference requests for every group, e.g. host_includes/scenes.hpp:32).
  *
  *  1. k_bounds      padded world AABB and centroid of every primitive record
- *  2. k_morton      30-bit Morton code of the centroid (10 bits per axis)
+ *  2. k_morton      30-bit Morton code of the centroid (10 bits per axis, one
+ *                   scale for all axes: the centroid box's longest side)
  *  3. radix sort    CUB DeviceRadixSort over (code, primitive) pairs
  *  4. k_karras      binary radix tree, Karras, "Maximizing Parallelism in the
  *                   Construction of BVHs, Octrees, and k-d Trees", HPG 2012
@@ -179,10 +180,14 @@ __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict
   if (i >= n) return;
   float4 a = lo[i], b = hi[i];
   float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+  // one scale for all axes (the centroid box's longest side): a flat scene
+  // (a heightfield) is not split along its thin axis as often as along the
+  // wide ones, which would give siblings that overlap over their whole area
+  float e = 0.f;
+  for (int k = 0; k < 3; k++) e = fmaxf(e, unmap(cbox[3 + k]) - unmap(cbox[k]));
   uint32_t code = 0;
   for (int k = 0; k < 3; k++) {
-    float l = unmap(cbox[k]), h = unmap(cbox[3 + k]);
-    float e = h - l;
+    float l = unmap(cbox[k]);
     float t = e > 0.f ? (c[k] - l) / e : 0.5f;
     uint32_t q = (uint32_t)fminf(fmaxf(t * 1024.f, 0.f), 1023.f);
     code |= spread10(q) << (2 - k);

@@ -15,6 +15,9 @@
 #define PT_TRACE_MINBLOCKS 3     /* of 256 threads: <= 80 registers per thread, no spills */
 #endif
 #define PT_SHADE_BLOCK 256       /* default and largest shade block */
+#ifndef PT_SHADE_MINBLOCKS
+#define PT_SHADE_MINBLOCKS 4     /* of 256 threads: <= 64 registers, 1024 resident threads per SM */
+#endif
 
 /* Path state word st.z: depth (bits 0-15), previous bounce specular (bit 16),
  * scene of a batch (bits 17-31). */

@@ -377,13 +377,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         cnt += byte_of(k < 4 ? mlo : mhi, k & 3) >> 5;
       }
     }
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int dd = 1; dd < 32; dd <<= 1) {
-      uint32_t t = __shfl_up_sync(0xffffffffu, incl, dd);
-      if (lane >= dd) incl += t;
-    }
-    uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
     uint32_t mx = __reduce_max_sync(0xffffffffu, cnt);
     if (total && mx * 32u <= 2u * total) {
       // balanced: each lane tests its own primitives (at least half the
@@ -414,6 +408,12 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       }
     } else if (total) {
       // unbalanced: spread the (ray, primitive) pairs over the warp
+      uint32_t incl = cnt;
+#pragma unroll
+      for (int dd = 1; dd < 32; dd <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, dd);
+        if (lane >= dd) incl += t;
+      }
       uint32_t off = incl - cnt;
       uint32_t m = leafmask;
       while (m) {
@@ -816,7 +816,9 @@ __device__ __forceinline__ V3 miss_color(const GpuMiss& ms, V3 d) {
 // thread the key offsets).  Warps then run one material's code instead of a
 // mix, which is what bounds these kernels (SIMT efficiency and instruction
 // fetch).  The order does not change any path's result.
+#ifndef PT_SORT_ITEMS
 #define PT_SORT_ITEMS 4
+#endif
 #define PT_SORT_KEYS (PT_NUM_MAT_TYPES + 2)
 
 struct SortTile {
@@ -1016,7 +1018,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
 }
 
 template <bool BATCH, bool SORT>
-__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade(DevScene S0, WaveState W,
+__global__ void __launch_bounds__(PT_SHADE_BLOCK, PT_SHADE_MINBLOCKS) k_shade(DevScene S0, WaveState W,
                                                           const WaveCtl* __restrict__ ctlp,
                                                           BatchRefs br) {
   __shared__ SortTile tile;
@@ -1320,7 +1322,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
 }
 
 template <bool BATCH, bool SORT, bool GUIDE>
-__global__ void __launch_bounds__(PT_SHADE_BLOCK) k_shade_c(DevScene S0, WaveState W,
+__global__ void __launch_bounds__(PT_SHADE_BLOCK, PT_SHADE_MINBLOCKS) k_shade_c(DevScene S0, WaveState W,
                                                             const WaveCtl* __restrict__ ctlp,
                                                             BatchRefs br) {
   __shared__ SortTile tile;

@@ -150,7 +150,14 @@ struct FirstHitOut {
   uint32_t* err;
 };
 
-enum { TRACE_EXT = 0, TRACE_SHADOW = 1, TRACE_FIRST = 2 };
+// TRACE_SHADOW: closest hit of a shadow ray (reference mode: the light must
+// be the first thing hit); TRACE_OCCLUDED: any hit before tmax (consistent
+// mode), traversed without ordering the children
+enum { TRACE_EXT = 0, TRACE_SHADOW = 1, TRACE_FIRST = 2, TRACE_OCCLUDED = 3 };
+
+#ifndef PT_ANYHIT_NEAREST
+#define PT_ANYHIT_NEAREST 1  // occlusion rays enter the nearest child first
+#endif
 
 size_t trace_smem_bytes(int max_stack, int block) {
   return (size_t)(block / 32) * sizeof(WarpShared) +
@@ -173,11 +180,12 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
 
   uint32_t n;
   WaveCounters c;
-  const bool consistent = MODE == TRACE_SHADOW && ctlp->mode == 1;
+  constexpr bool consistent = MODE == TRACE_OCCLUDED;
+  constexpr bool SHADOWRAY = MODE == TRACE_SHADOW || MODE == TRACE_OCCLUDED;
   if (MODE == TRACE_EXT) {
     c = *W.ctr;
     n = c.n_cur + gen_count(c, *ctlp, (uint32_t)W.slots);
-  } else if (MODE == TRACE_SHADOW) {
+  } else if (SHADOWRAY) {
     n = W.ctr->n_shadow;
   } else {
     n = (uint32_t)fo.width * (uint32_t)fo.height;
@@ -202,7 +210,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       d = f4xyz(rdv);
       tmin = ro.w;
       tmax = rdv.w;
-    } else if (MODE == TRACE_SHADOW) {
+    } else if (SHADOWRAY) {
       slot = i;
       o = f4xyz(W.sh.P[i]);
       d = f4xyz(W.sh.Wi[i]);
@@ -230,7 +238,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         h = make_float4(tbest, bu, bv, __uint_as_float(leaf));
       }
       W.hit[slot] = h;
-    } else if (MODE == TRACE_SHADOW) {
+    } else if (SHADOWRAY) {
       bool occluded = true;
       if (consistent) {
         occluded = best_id != PT_NO_HIT;  // anything before the light
@@ -313,7 +321,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       busy = __ballot_sync(0xffffffffu, active);
     }
     if (!busy) break;
-    uint32_t leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0, kmin = 0xffffffffu;
+    uint32_t leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0, kmin = 0xffffffffu, imask = 0;
     uint32_t keys[8];
     int nint = 0;
 #pragma unroll
@@ -356,7 +364,10 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         float tn = max3f(tx.x, ty.x, fmaxf(tz.x, tmin));
         float tf = min3f(tx.y, ty.y, fminf(tz.y, tlim));
         if (meta != 0 && tn <= tf) {
-          if (meta & 0x80u) {
+          if (consistent && (meta & 0x80u)) {
+            imask |= 1u << (meta & 7u);
+            if (PT_ANYHIT_NEAREST) kmin = min(kmin, (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u));
+          } else if (meta & 0x80u) {
             uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
             keys[k] = key;
             kmin = min(kmin, key);
@@ -455,8 +466,41 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       active = false;
       idle = true;
     }
+    // ---- occlusion rays: the nearest hit child (or the lowest slot), the
+    // others pushed as one mask and taken lowest slot first
+    if (consistent && active) {
+      if (imask) {
+        uint32_t b = PT_ANYHIT_NEAREST ? (kmin & 7u) : (uint32_t)(__ffs(imask) - 1);
+        cur = child_base + b;
+        imask &= ~(1u << b);
+        if (imask) {
+          if (sp >= max_stack) {
+            atomicOr(&W.ctr->error, 1u);
+            sp = 0;  // abandon this ray (the host reports the error)
+            finish();
+            i += stride;
+            active = false;
+            idle = true;
+          } else {
+            stk[sp * bd] = make_uint2(child_base, imask);
+            sp++;
+          }
+        }
+      } else if (sp > 0) {
+        uint2 e = stk[(sp - 1) * bd];
+        cur = e.x + (uint32_t)(__ffs(e.y) - 1);
+        e.y &= e.y - 1;
+        if (e.y == 0) sp--;
+        else stk[(sp - 1) * bd].y = e.y;
+      } else {
+        finish();
+        i += stride;
+        active = false;
+        idle = true;
+      }
+    }
     // ---- next node: nearest internal child, else the deepest pending group
-    if (active) {
+    if (!consistent && active) {
       if (nint == 1) {
         cur = child_base + (kmin & 7u);
       } else if (nint > 1) {
@@ -1676,6 +1720,10 @@ cudaError_t set_trace_smem() {
   if ((e = smem_attr(k_trace_t<TRACE_EXT, true, true>, optin)) != cudaSuccess) return e;
   if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false, true>, optin)) != cudaSuccess) return e;
   if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true, true>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, false, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, true, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, false, true>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, true, true>, optin)) != cudaSuccess) return e;
   if ((e = smem_attr(k_trace_t<TRACE_FIRST, false, false>, optin)) != cudaSuccess) return e;
   if (dev >= 0 && dev < kMaxDev) g_smem_set[dev] = true;
   return cudaSuccess;
@@ -1709,7 +1757,11 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
     else k_shade<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
   }
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
-  if (counters)
+  if (mode == 1 && counters)
+    k_trace_t<TRACE_OCCLUDED, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+  else if (mode == 1)
+    k_trace_t<TRACE_OCCLUDED, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+  else if (counters)
     k_trace_t<TRACE_SHADOW, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
   else
     k_trace_t<TRACE_SHADOW, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);

@@ -71,6 +71,8 @@ typedef struct pt_options {
   int shade_order;     /* 0 automatic (material-sorted tiles when the scene uses
                           Oren-Nayar, Torrance-Sparrow or Ashikhmin-Shirley), 1 sorted,
                           2 path order */
+  int refetch_lanes;   /* idle lanes of a trace warp that take new rays together, 1..32;
+                          0 automatic (24 for scenes of more than 2^16 primitives, else 32) */
 } pt_options;
 
 typedef struct pt_render_params {
@@ -292,6 +294,7 @@ typedef struct pt_tune {
   int bvh_width;            /* most children per BVH node, 2..8 */
   int chunk_paths;          /* paths per chunk (per-path result area), 0 = 2^27 */
   int shade_order;          /* as pt_options.shade_order */
+  int refetch_lanes;        /* as pt_options.refetch_lanes */
   double sample_paths_per_s;/* autotune: throughput of this configuration on its sample */
 } pt_tune;
 

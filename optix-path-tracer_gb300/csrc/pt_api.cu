@@ -184,7 +184,8 @@ PT_API int pt_context_create(const pt_options* opt, pt_context** out) {
   if (!out) return PT_EINVAL;
   *out = nullptr;
   if (opt && ((opt->bvh_width != 0 && (opt->bvh_width < 2 || opt->bvh_width > 8)) ||
-              opt->shade_order < 0 || opt->shade_order > 2))
+              opt->shade_order < 0 || opt->shade_order > 2 || opt->refetch_lanes < 0 ||
+              opt->refetch_lanes > 32))
     return PT_EINVAL;
   pt_context* ctx = new (std::nothrow) pt_context();
   if (!ctx) return PT_ENOMEM;
@@ -733,6 +734,7 @@ PT_API int pt_commit(pt_context* ctx) {
   CK(pt::set_trace_smem());
   ctx->lc = pt::default_launch(ctx->max_stack);
   ctx->lc.sort = ctx->opt.shade_order == 1 || (ctx->opt.shade_order == 0 && pth::sort_pays(ctx));
+  ctx->lc.refetch = ctx->opt.refetch_lanes ? ctx->opt.refetch_lanes : pth::auto_refetch(n);
   auto t1 = std::chrono::steady_clock::now();
   ctx->stats.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   ctx->stats.bvh_nodes = nn;
@@ -895,6 +897,13 @@ static void reset_render_stats(pt_context* ctx) {
 }
 
 }  // extern "C"
+
+// Rays through a large scene take many more steps, with a wider spread, so
+// lanes refill earlier (a quarter of the warp idle) rather than waiting for
+// the whole warp; rays through a small scene are short and alike.  (GB300,
+// 1080p: 2.1M-triangle heightfield 24 lanes +6% over 32; 488 spheres 32
+// lanes +1% over 24.)
+int pth::auto_refetch(size_t num_prims) { return num_prims > ((size_t)1 << 16) ? 24 : 32; }
 
 bool pth::sort_pays(const pt_context* ctx) {
   for (const GpuMaterial& m : ctx->mats)

@@ -128,7 +128,7 @@ static bool tune_valid(const pt_tune& t) {
          (t.trace_block == 64 || t.trace_block == 128 || t.trace_block == 256) &&
          t.shade_block >= 64 && t.shade_block <= PT_SHADE_BLOCK && t.shade_block % 32 == 0 &&
          t.bvh_width >= 2 && t.bvh_width <= 8 && t.chunk_paths >= 0 &&
-         t.shade_order >= 0 && t.shade_order <= 2;
+         t.shade_order >= 0 && t.shade_order <= 2 && t.refetch_lanes >= 0 && t.refetch_lanes <= 32;
 }
 
 static void drop_graph(pt_batch* b) {
@@ -415,6 +415,12 @@ static int batch_render(pt_batch* b, const pt_batch_item* items, int n, float4* 
   lc.sort = b->tune.shade_order == 1;
   if (b->tune.shade_order == 0)
     for (const ScenePart& p : b->parts) lc.sort = lc.sort || sort_pays(p.ctx);
+  lc.refetch = b->tune.refetch_lanes;
+  if (lc.refetch == 0) {  // automatic: by the largest scene of the batch
+    size_t most = 0;
+    for (const ScenePart& p : b->parts) most = std::max(most, p.ctx->prims.size());
+    lc.refetch = auto_refetch(most);
+  }
   b->lc = lc;
   // accumulators: the items' device buffers, or device copies of host ones
   std::vector<float4*> acc(n);
@@ -649,6 +655,7 @@ PT_API int pt_batch_create(const pt_options* opt, pt_batch** out) {
   b->tune.shade_block = PT_SHADE_BLOCK;
   b->tune.bvh_width = (opt && opt->bvh_width) ? opt->bvh_width : 8;
   b->tune.shade_order = opt ? opt->shade_order : 0;
+  b->tune.refetch_lanes = opt ? opt->refetch_lanes : 0;
   if (!tune_valid(b->tune)) {
     delete b;
     return PT_EINVAL;
@@ -788,6 +795,7 @@ PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_
   const int sb_opts[] = {128, 256};
   const int w_opts[] = {8, 4};
   const int order_opts[] = {1, 2};
+  const int refetch_opts[] = {24, 32};
   for (int v : slot_opts) {
     pt_tune t = best;
     t.path_slots = v;
@@ -811,6 +819,11 @@ PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_
   for (int v : order_opts) {
     pt_tune t = best;
     t.shade_order = v;
+    if ((rc = consider(t))) return rc;
+  }
+  for (int v : refetch_opts) {
+    pt_tune t = best;
+    t.refetch_lanes = v;
     if ((rc = consider(t))) return rc;
   }
   best.sample_paths_per_s = best_pps;

@@ -152,6 +152,7 @@ bool is_device_ptr(const void* p);
  * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
  * is present, whose code paths diverge most in a mixed warp. */
 bool sort_pays(const pt_context* ctx);
+int auto_refetch(size_t num_prims);
 /* Padded world box of one primitive (the BVH builders' leaf box). */
 pt::Box prim_bounds(const pt_context* ctx, const HostPrim& p);
 /* Allocates the guide's buffers and finds the scene box of its position

@@ -32,6 +32,7 @@ struct LaunchCfg {
   int trace_block, trace_grid;
   int shade_block, shade_grid;
   int sort;            /* shade in material-sorted tiles */
+  int refetch;         /* idle lanes of a trace warp that take new rays together (1..32) */
 };
 
 struct Ray3 {
@@ -52,6 +53,7 @@ struct WaveCounters {
   unsigned long long iters_total; /* iterations over all chunks (batch) */
   uint32_t chunk;        /* current chunk of a batch */
   uint32_t n_chunks;     /* chunks of the batch (set by the host) */
+  uint32_t ray_next[2];  /* rays taken by trace warps this iteration (extension, shadow) */
 };
 
 /* Per-chunk render controls, in device memory (kernels read them, so one

@@ -65,9 +65,6 @@ __device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uin
 // next ray at once (persistent threads), and a stack group whose nearest
 // child lies beyond the closest hit is dropped without visiting it.
 #define PT_MAX_PAIRS (32 * 24)
-#ifndef PT_REFETCH_MIN
-#define PT_REFETCH_MIN 32  // idle lanes that trigger loading new rays (32: the whole warp)
-#endif
 
 struct WarpShared {
   float4 ro[32];                  // origin, tmin
@@ -169,7 +166,7 @@ size_t trace_smem_bytes(int max_stack, int block) {
 template <int MODE, bool COUNT, bool BATCH>
 __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     k_trace_t(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp, int max_stack,
-              FirstHitOut fo, BatchRefs br) {
+              FirstHitOut fo, BatchRefs br, int refetch) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   WarpShared& ws = ((WarpShared*)smem)[threadIdx.x >> 5];
@@ -190,8 +187,12 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
   } else {
     n = (uint32_t)fo.width * (uint32_t)fo.height;
   }
+  // rays are handed out to warps in arrival order from a per-launch counter
+  // (first-hit queries: a fixed grid-stride assignment)
   const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t* take = MODE == TRACE_EXT ? &W.ctr->ray_next[0] : (SHADOWRAY ? &W.ctr->ray_next[1] : nullptr);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool started = false;
   uint32_t nn = 0, np = 0;
 
   // per-lane ray state
@@ -262,23 +263,25 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     }
   };
 
+  bool idle = true;  // wants a ray (finished one, or none taken yet)
+  // loads ray i (< n) and sets up its traversal
   auto fetch = [&]() {
     // a ray with a NaN in its origin or direction hits nothing (every
     // primitive test fails or yields a NaN distance, which never wins the
     // closest-hit minimum), and neither does any ray of an empty scene: both
     // end here, without a traversal (a NaN ray would pass every box test)
-    while (i < n) {
-      load_ray();
-      bool nan = !(o.x == o.x && o.y == o.y && o.z == o.z && d.x == d.x && d.y == d.y &&
-                   d.z == d.z);
-      if (!nan && S.num_prims != 0) break;
+    load_ray();
+    bool nan = !(o.x == o.x && o.y == o.y && o.z == o.z && d.x == d.x && d.y == d.y &&
+                 d.z == d.z);
+    if (nan || S.num_prims == 0) {
       best_id = PT_NO_HIT;
       tbest = tmax;
       finish();
-      i += stride;
+      active = false;
+      idle = true;
+      return;
     }
-    active = i < n;
-    if (!active) return;
+    active = true;
     const float eps = 1e-18f;
     float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
     float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
@@ -306,19 +309,35 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     sp = 0;
   };
 
-  fetch();
-  bool idle = false;  // finished a ray, next one not loaded yet
   while (true) {
-    // idle lanes load their next rays together once half the warp waits
-    // (or nothing else runs), so the warp pays one load latency per batch
+    // idle lanes take and load their next rays together once `refetch`
+    // lanes wait (or nothing else runs), so the warp pays one load latency
+    // per batch; a lane whose index is past the end has no more work (the
+    // counter only grows)
     uint32_t busy = __ballot_sync(0xffffffffu, active);
     uint32_t waiting = __ballot_sync(0xffffffffu, idle);
-    if (waiting && (__popc(waiting) >= PT_REFETCH_MIN || busy == 0)) {
+    if (waiting && (__popc(waiting) >= refetch || busy == 0)) {
+      if (MODE == TRACE_FIRST) {
+        if (idle) {
+          if (started) i += stride;
+          started = true;
+        }
+      } else {
+        const int leader = __ffs(waiting) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(take, (uint32_t)__popc(waiting));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (idle) i = base + (uint32_t)__popc(waiting & ((1u << lane) - 1u));
+      }
       if (idle) {
         idle = false;
-        fetch();
+        if (i < n) fetch();
       }
       busy = __ballot_sync(0xffffffffu, active);
+      if (!busy) {
+        if (__ballot_sync(0xffffffffu, idle)) continue;  // only rays that ended at load
+        break;
+      }
     }
     if (!busy) break;
     uint32_t leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0, kmin = 0xffffffffu, imask = 0;
@@ -462,7 +481,6 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     // tmax: the first confirmed hit ends the ray
     if (consistent && active && best_id != PT_NO_HIT) {
       finish();
-      i += stride;
       active = false;
       idle = true;
     }
@@ -478,7 +496,6 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
             atomicOr(&W.ctr->error, 1u);
             sp = 0;  // abandon this ray (the host reports the error)
             finish();
-            i += stride;
             active = false;
             idle = true;
           } else {
@@ -494,7 +511,6 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         else stk[(sp - 1) * bd].y = e.y;
       } else {
         finish();
-        i += stride;
         active = false;
         idle = true;
       }
@@ -519,7 +535,6 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
           atomicOr(MODE == TRACE_FIRST ? fo.err : &W.ctr->error, 1u);
           sp = 0;  // abandon this ray (the host reports the error)
           finish();
-          i += stride;
           active = false;
           idle = true;
         } else {
@@ -547,7 +562,6 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         }
         if (!found) {
           finish();
-          i += stride;
           active = false;
           idle = true;
         }
@@ -862,6 +876,9 @@ __device__ __forceinline__ V3 miss_color(const GpuMiss& ms, V3 d) {
 // fetch).  The order does not change any path's result.
 #ifndef PT_SORT_ITEMS
 #define PT_SORT_ITEMS 4
+#endif
+#ifndef PT_SHADE_TILE_GRID
+#define PT_SHADE_TILE_GRID 1
 #endif
 #define PT_SORT_KEYS (PT_NUM_MAT_TYPES + 2)
 
@@ -1434,6 +1451,8 @@ __global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp, int use
   c.n_cur = c.n_next;
   c.n_next = 0;
   c.n_shadow = 0;
+  c.ray_next[0] = 0;
+  c.ray_next[1] = 0;
   c.parity ^= 1u;
   c.iter++;
   c.iters_total++;
@@ -1684,6 +1703,7 @@ LaunchCfg default_launch(int max_stack) {
   lc.trace_block = PT_TRACE_BLOCK;
   lc.shade_block = PT_SHADE_BLOCK;
   lc.sort = 1;
+  lc.refetch = 32;
   lc.trace_grid = wave_grid(0, max_stack, lc.trace_block);
   lc.shade_grid = wave_grid(1, max_stack, lc.shade_block);
   return lc;
@@ -1737,34 +1757,42 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
   size_t sm = trace_smem(max_stack, lc.trace_block);
   FirstHitOut none{};
   const int tb = lc.trace_block, tg = lc.trace_grid, sb = lc.shade_block, sg = lc.shade_grid;
+  // sorted shading: one block per tile of the buffer (blocks past the live
+  // paths return at once), so the block scheduler balances uneven tiles
+  const int tile = sb * PT_SORT_ITEMS;
+#if PT_SHADE_TILE_GRID
+  const int tgs = W.slots > 0 ? (W.slots + tile - 1) / tile : 1;
+#else
+  const int tgs = sg;
+#endif
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
   k_generate<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
   if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
   if (counters)
-    k_trace_t<TRACE_EXT, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+    k_trace_t<TRACE_EXT, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   else
-    k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+    k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
   if (mode == 1 && gi) {
     launch_guide_infer(S, W, ctl, *gi, 2 * num_sms(), st);
-    if (lc.sort) k_shade_c<BATCH, true, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    if (lc.sort) k_shade_c<BATCH, true, true><<<tgs, sb, 0, st>>>(S, W, ctl, br);
     else k_shade_c<BATCH, false, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
   } else if (mode == 1) {
-    if (lc.sort) k_shade_c<BATCH, true, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    if (lc.sort) k_shade_c<BATCH, true, false><<<tgs, sb, 0, st>>>(S, W, ctl, br);
     else k_shade_c<BATCH, false, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
   } else {
-    if (lc.sort) k_shade<BATCH, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
+    if (lc.sort) k_shade<BATCH, true><<<tgs, sb, 0, st>>>(S, W, ctl, br);
     else k_shade<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
   }
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
   if (mode == 1 && counters)
-    k_trace_t<TRACE_OCCLUDED, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+    k_trace_t<TRACE_OCCLUDED, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   else if (mode == 1)
-    k_trace_t<TRACE_OCCLUDED, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+    k_trace_t<TRACE_OCCLUDED, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   else if (counters)
-    k_trace_t<TRACE_SHADOW, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+    k_trace_t<TRACE_SHADOW, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   else
-    k_trace_t<TRACE_SHADOW, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br);
+    k_trace_t<TRACE_SHADOW, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
   if (mode == 1)
     k_finish_c<<<sg, sb, 0, st>>>(S, W, ctl);
@@ -1831,7 +1859,7 @@ void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* pri
   WaveState none{};
   k_trace_t<TRACE_FIRST, false, false>
       <<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack, PT_TRACE_BLOCK), st>>>(
-          S, none, nullptr, max_stack, fo, BatchRefs{});
+          S, none, nullptr, max_stack, fo, BatchRefs{}, 32);
 }
 
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,

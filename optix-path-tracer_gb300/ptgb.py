@@ -40,7 +40,7 @@ class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("path_slots", ctypes.c_int),
                 ("enable_counters", ctypes.c_int), ("enable_timing", ctypes.c_int),
                 ("bvh_builder", ctypes.c_int), ("bvh_width", ctypes.c_int),
-                ("shade_order", ctypes.c_int)]
+                ("shade_order", ctypes.c_int), ("refetch_lanes", ctypes.c_int)]
 
 
 class RenderParams(ctypes.Structure):
@@ -68,7 +68,7 @@ class Tune(ctypes.Structure):
     _fields_ = [("path_slots", ctypes.c_int), ("trace_block", ctypes.c_int),
                 ("shade_block", ctypes.c_int), ("bvh_width", ctypes.c_int),
                 ("chunk_paths", ctypes.c_int), ("shade_order", ctypes.c_int),
-                ("sample_paths_per_s", ctypes.c_double)]
+                ("refetch_lanes", ctypes.c_int), ("sample_paths_per_s", ctypes.c_double)]
 
 
 _F3 = ctypes.c_float * 3
@@ -311,10 +311,10 @@ class GpuRenderer:
     """One pt_context with a committed scene."""
 
     def __init__(self, scene, device=0, path_slots=0, counters=False, timing=False, builder=0,
-                 bvh_width=0, shade_order=0):
+                 bvh_width=0, shade_order=0, refetch_lanes=0):
         self.lib = load_library()
         opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, builder,
-                      bvh_width, shade_order)
+                      bvh_width, shade_order, refetch_lanes)
         ctx = _P()
         rc = self.lib.pt_context_create(ctypes.byref(opt), ctypes.byref(ctx))
         if rc != 0:
@@ -498,10 +498,10 @@ class Batch:
     one wavefront."""
 
     def __init__(self, device=0, path_slots=0, counters=False, timing=False, bvh_width=0,
-                 shade_order=0):
+                 shade_order=0, refetch_lanes=0):
         self.lib = load_library()
         opt = Options(device, path_slots, 1 if counters else 0, 1 if timing else 0, 0, bvh_width,
-                      shade_order)
+                      shade_order, refetch_lanes)
         b = _P()
         rc = self.lib.pt_batch_create(ctypes.byref(opt), ctypes.byref(b))
         if rc != 0:
@@ -546,8 +546,9 @@ class Batch:
         return {k: getattr(t, k) for k, _ in Tune._fields_}
 
     def set_tune(self, path_slots, trace_block, shade_block, bvh_width, chunk_paths=0,
-                 shade_order=0):
-        t = Tune(path_slots, trace_block, shade_block, bvh_width, chunk_paths, shade_order, 0.0)
+                 shade_order=0, refetch_lanes=0):
+        t = Tune(path_slots, trace_block, shade_block, bvh_width, chunk_paths, shade_order,
+                 refetch_lanes, 0.0)
         self._c(self.lib.pt_batch_set_tune(self.b, ctypes.byref(t)))
 
     def tune(self):

@@ -587,7 +587,7 @@ def run_guide(args):
                 r.guide_init(1)
             a = np.zeros((H, W, 4))
             done, tt, pts = 0, 0.0, []
-            for chunk in (4, 4, 8, 16, 32, 64, 128):
+            for chunk in (4, 4, 8, 16, 32, 64, 128, 256, 512):
                 img = r.render64(P(W, H, chunk, frame0=done, guide=guide, **kw))
                 tt += r.stats()["render_ms"]
                 a[..., :3] += img[..., :3]
@@ -599,11 +599,23 @@ def run_guide(args):
         ref_r.close()
         gt = np.array([p[0] for p in curves[1]])
         ge = np.array([p[1] for p in curves[1]])
+
+        def guided_time(e):
+            if ge.min() <= e <= ge.max():
+                return float(np.exp(np.interp(np.log(e), np.log(ge[::-1]), np.log(gt[::-1]))))
+            if e < ge.min():  # extrapolate along relMSE ~ 1/time from the last point
+                return float(gt[-1] * ge[-1] / e)
+            return None
+
+        # the ratio at every plain budget from 128 spp on (the guide's online
+        # training is paid back over more frames at larger budgets)
+        ratios = {}
+        for t, e, n in curves[0]:
+            tg = guided_time(e) if n >= 128 else None
+            if tg is not None:
+                ratios[str(n)] = round(tg / t, 3)
         t_plain, e_plain, spp_plain = curves[0][-1]
-        if ge.min() <= e_plain:
-            t_guided = float(np.exp(np.interp(np.log(e_plain), np.log(ge[::-1]), np.log(gt[::-1]))))
-        else:  # extrapolate along relMSE ~ 1/time from the last point
-            t_guided = float(gt[-1] * ge[-1] / e_plain)
+        t_guided = guided_time(e_plain)
         study = {"reference": f"plain consistent render, {args.ref_spp} spp, FP64 sums "
                               f"({t_ref:.0f} s); the configuration names 16384 spp",
                  "relmse_eps": 1e-2,
@@ -612,7 +624,9 @@ def run_guide(args):
                  "plain_final_relmse": e_plain,
                  "guided_time_to_plain_final_ms": t_guided,
                  "plain_time_ms": t_plain,
-                 "time_ratio": t_guided / t_plain}
+                 "plain_budget_spp": spp_plain,
+                 "time_ratio": t_guided / t_plain,
+                 "time_ratio_by_plain_spp": ratios}
 
     if rank == 0:
         line = {
@@ -641,7 +655,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS) + ["batch", "guide"])
-    ap.add_argument("--ref-spp", type=int, default=1024,
+    ap.add_argument("--ref-spp", type=int, default=4096,
                     help="guide workload: spp of the FP64 plain reference")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -247,6 +247,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
     G.samples.release();
     G.eval_out.release();
     G.out.release();
+    G.rows.release();
     G.rec.release();
   }
   ctx->d_tmp.release();
@@ -947,6 +948,7 @@ static int render_device(pt_context* ctx, const pt_render_params* p, void* d_acc
     if (rc) return rc;
     if (!ctx->guide.ready && (rc = pt_guide_init(ctx, 0)) != PT_OK) return rc;
     CK(ctx->guide.out.ensure((size_t)ctx->slots));
+    CK(ctx->guide.rows.ensure((size_t)ctx->slots));
     ctx->W.guide = ctx->guide.out.p;
   }
   if (p->frame0 == 0) CK(cudaMemsetAsync(d_acc, 0, WH * (acc64 ? 32 : 16), st));

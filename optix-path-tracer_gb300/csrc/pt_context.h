@@ -65,6 +65,7 @@ struct GuideState {
   DevBuf<GuideSample> samples;
   DevBuf<float> eval_out;
   DevBuf<GuidePacked> out;   // per path slot: decoded guide
+  DevBuf<uint32_t> rows;     // per path slot: positions selected for inference
   DevBuf<GuideSample> rec;   // training records of the current frame
   uint32_t rec_stride = 1, rec_n = 0;
   float lr = 1e-2f;          // Adam learning rate of the online training

@@ -192,15 +192,17 @@ constexpr int kTmemDW = 64;
 
 __device__ __forceinline__ int layer_rows(int l) { return l == 4 ? PTG_NOUT : PTG_H; }
 
-// Weights (BF16, row-major [rows][80]) into K-major core tiles.
+// Weights (BF16, row-major [rows][80]) into K-major core tiles, 16 bytes
+// (one core-matrix row: 8 consecutive columns) per copy.
 __device__ void load_weights(unsigned char* W, const __nv_bfloat16* __restrict__ wg) {
+  constexpr int kChunks = PTG_K / 8;  // 16-byte chunks per row
   for (int l = 0; l < 5; l++) {
     unsigned char* t = W + l * kTileW;
-    const __nv_bfloat16* src = wg + PTG_LAYER_OFF(l);
-    int n = layer_rows(l) * PTG_K;
+    const uint4* src = (const uint4*)(wg + PTG_LAYER_OFF(l));
+    int n = layer_rows(l) * kChunks;
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
-      int r = e / PTG_K, c = e % PTG_K;
-      *(__nv_bfloat16*)(t + core_off(r, c, PTG_K)) = src[e];
+      int r = e / kChunks, c = (e % kChunks) * 8;
+      *(uint4*)(t + core_off(r, c, PTG_K)) = __ldg(src + e);
     }
   }
 }
@@ -499,9 +501,47 @@ __device__ __forceinline__ bool group_and(bool v, int id) {
 }
 
 
-// Inference inside the wavefront, one row per live path of the current
-// buffer; rows whose hit is a guided (non-delta) material get their packed
-// guide in A.out at the path's position.  Each CTA runs two independent
+// Lists the positions of the current buffer whose path needs a guide at
+// this bounce (depth below the guided-bounce limit, a hit on a non-delta
+// material), so that inference runs the network on those rows only; the
+// list order does not matter (rows are independent).
+__global__ void __launch_bounds__(256) k_guide_select(DevScene S, WaveState W,
+                                                      const WaveCtl* __restrict__ ctlp,
+                                                      uint32_t* rows) {
+  const WaveCounters c = *W.ctr;
+  const WaveCtl ctl = *ctlp;
+  unsigned long long left = ctl.chunk_paths - c.next_path;
+  const uint32_t n =
+      c.n_cur + (uint32_t)min((unsigned long long)((uint32_t)W.slots - c.n_cur), left);
+  const PathBuf& pb = W.path[c.parity];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  const int lane = threadIdx.x & 31;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t it = 0; it < iters; it++, i += stride) {
+    bool take = false;
+    if (i < n && (pb.st[i].z & PT_ST_DEPTH_MASK) < ctl.guide_depth) {
+      uint32_t leaf = __float_as_uint(W.hit[i].w);
+      if (leaf != PT_NO_HIT) {
+        uint32_t mid = __float_as_uint(__ldg(&S.prims[3 * (size_t)leaf + 2].w));
+        int type = __ldg(&S.mats[mid].type);
+        take = type == PT_MAT_LAMBERTIAN || type == PT_MAT_OREN_NAYAR ||
+               type == PT_MAT_TORRANCE_SPARROW || type == PT_MAT_ASHIKHMIN_SHIRLEY;
+      }
+    }
+    uint32_t mask = __ballot_sync(0xffffffffu, take);
+    if (!mask) continue;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&W.ctr->guide_rows, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take) rows[base + __popc(mask & ((1u << lane) - 1u))] = i;
+  }
+}
+
+// Inference inside the wavefront, one row per position listed by
+// k_guide_select; each row's packed guide goes to A.out at the path's
+// position.  Each CTA runs two independent
 // 128-row pipelines (warps 0-3 and 4-7) that share the weights: each has
 // its own activation tile (updated in place: the epilogue writes a layer's
 // output over its input once the MMA has read it), mbarrier, 64 TMEM columns
@@ -516,6 +556,11 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
   const int grp = threadIdx.x >> 7, row = threadIdx.x & 127, warp = threadIdx.x >> 5;
   const int bar_id = 1 + grp;
   unsigned char* T = sm + kWeights + grp * kTileT;
+  const WaveCounters c = *W.ctr;
+  const WaveCtl ctl = *ctlp;
+  const uint32_t nl = min(c.guide_rows, (uint32_t)W.slots);  // listed by k_guide_select
+  const uint32_t ntiles = (nl + 127) / 128;
+  if (blockIdx.x * 2 >= ntiles) return;  // no tile for this CTA: skip the setup
   if (threadIdx.x == 0) {
     for (int g = 0; g < 2; g++)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[g])), "r"(1));
@@ -535,18 +580,13 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   uint32_t phase = 0;
   bool failed = false;
-  const WaveCounters c = *W.ctr;
-  const WaveCtl ctl = *ctlp;
-  unsigned long long left = ctl.chunk_paths - c.next_path;
-  const uint32_t n =
-      c.n_cur + (uint32_t)min((unsigned long long)((uint32_t)W.slots - c.n_cur), left);
-  const uint32_t ntiles = (n + 127) / 128;
   const PathBuf& pb = W.path[c.parity];
   for (uint32_t tile = blockIdx.x * 2 + grp; tile < ntiles; tile += gridDim.x * 2) {
-    const uint32_t i = tile * 128 + row;
+    const uint32_t li = tile * 128 + row;
+    const uint32_t i = li < nl ? A.rows[li] : 0xffffffffu;
     bool valid = false;
     float P[3], N[3], Wo[3];
-    if (i < n && (pb.st[i].z & PT_ST_DEPTH_MASK) < ctl.guide_depth) {
+    if (i < (uint32_t)W.slots && (pb.st[i].z & PT_ST_DEPTH_MASK) < ctl.guide_depth) {
       float4 hit = W.hit[i];
       uint32_t leaf = __float_as_uint(hit.w);
       if (leaf != PT_NO_HIT) {
@@ -683,6 +723,7 @@ void launch_guide_adam(const GuideAdamArgs& a, cudaStream_t st) {
 
 void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                         const GuideInferArgs& a, int grid, cudaStream_t st) {
+  k_guide_select<<<grid * 4, 256, 0, st>>>(S, W, ctl, a.rows);
   k_guide_infer<<<grid, 256, guide_infer_smem(), st>>>(S, W, ctl, a);
 }
 

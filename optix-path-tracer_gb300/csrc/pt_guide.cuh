@@ -33,7 +33,9 @@
 #define PTG_W5 (48 * 80)
 #define PTG_PARAMS (4 * PTG_W_LAYER + PTG_W5)  /* flat parameter vector (with padding) */
 #define PTG_ALPHA_MIN 0.05f
+#ifndef PTG_ALPHA_SPAN
 #define PTG_ALPHA_SPAN 0.9f
+#endif
 #define PTG_LOGK_MIN -6.0f
 #define PTG_LOGK_MAX 9.0f
 
@@ -79,6 +81,7 @@ struct GuideSample {
 struct GuideInferArgs {
   const __nv_bfloat16* w;   // BF16 weights, row-major, PTG_PARAMS
   GuidePacked* out;         // per buffer position
+  uint32_t* rows;           // positions that need a guide this iteration (k_guide_select)
   float bmin[3], binv[3];   // scene box for the position encoding
   uint32_t* fail;
 };

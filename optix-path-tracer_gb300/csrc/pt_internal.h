@@ -54,6 +54,7 @@ struct WaveCounters {
   uint32_t chunk;        /* current chunk of a batch */
   uint32_t n_chunks;     /* chunks of the batch (set by the host) */
   uint32_t ray_next[2];  /* rays taken by trace warps this iteration (extension, shadow) */
+  uint32_t guide_rows;   /* positions listed for guide inference this iteration */
 };
 
 /* Per-chunk render controls, in device memory (kernels read them, so one

@@ -1453,6 +1453,7 @@ __global__ void k_advance(WaveState W, const WaveCtl* __restrict__ ctlp, int use
   c.n_shadow = 0;
   c.ray_next[0] = 0;
   c.ray_next[1] = 0;
+  c.guide_rows = 0;
   c.parity ^= 1u;
   c.iter++;
   c.iters_total++;

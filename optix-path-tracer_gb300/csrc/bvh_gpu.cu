@@ -12,8 +12,9 @@
  *                   at every node with >= 7 primitives below it the treelet of
  *                   up to 7 leaves is rebuilt optimally for SAH by dynamic
  *                   programming over leaf subsets (Karras & Aila, "Fast
- *                   Parallel Construction of High-Quality BVHs", HPG 2013);
- *                   run twice
+ *                   Parallel Construction of High-Quality BVHs", HPG 2013),
+ *                   one warp per treelet; a first pass without restructuring,
+ *                   then one per treelet round
  *  6. k_collapse    one launch per level: each binary node becomes a wide
  *                   node by expanding its largest child until 8 children
  *                   (or the requested width);
@@ -263,9 +264,19 @@ __device__ __forceinline__ void set_parent(const Tree& T, uint32_t r, uint32_t p
   else T.parent_int[r] = p;
 }
 
+// Dynamic-programming state of one treelet, one per warp in shared memory.
+struct TreeletDP {
+  float cost[128];    // SAH cost of the best subtree over each leaf subset
+  float box[6][128];  // bounds of each leaf subset (lo xyz, hi xyz)
+  uint8_t split[128]; // the subset's best first part
+};
+
 // Rebuilds the treelet rooted at internal node `root` (up to 7 leaves) with
-// the SAH-optimal topology; the treelet's internal nodes are reused.
-__device__ void optimize_treelet(const Tree& T, uint32_t root) {
+// the SAH-optimal topology; the treelet's internal nodes are reused.  Called
+// by all 32 lanes of a warp together: every lane forms the same treelet (the
+// same loads), the lanes share the subsets of each size of the dynamic
+// program, and lane 0 writes the new topology.
+__device__ void optimize_treelet(const Tree& T, uint32_t root, TreeletDP& dp, int lane) {
   uint32_t leaves[7], inner[6];
   int nl = 2, ni = 1;
   leaves[0] = left_of(T, root);
@@ -288,86 +299,131 @@ __device__ void optimize_treelet(const Tree& T, uint32_t root) {
     leaves[best] = left_of(T, x);
     leaves[nl++] = right_of(T, x);
   }
-  if (nl < 3) return;
+  if (nl < 3) return;  // the same for every lane
   const int full = (1 << nl) - 1;
-  GBox box[128];
-  float cost[128];
-  uint8_t split[128];
-  for (int k = 0; k < nl; k++) {
-    box[1 << k] = ref_box(T, leaves[k]);
-    cost[1 << k] = ref_cost(T, leaves[k]);
-  }
-  for (int S = 1; S <= full; S++) {
-    int low = S & -S;
-    if (S == low) continue;
-    box[S] = box_union(box[S ^ low], box[low]);
-    // subsets P of S containing the lowest bit, P != S
-    float best = 3.0e38f;
-    int bp = low;
-    int rest = S ^ low;
-    for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {
-      int P = Q | low;  // P ranges over low + proper subsets of rest
-      float c = cost[P] + cost[S ^ P];
-      if (c < best) {
-        best = c;
-        bp = P;
-      }
-      if (Q == 0) break;
+  if (lane < nl) {
+    GBox b = ref_box(T, leaves[lane]);
+    const int S = 1 << lane;
+    for (int a = 0; a < 3; a++) {
+      dp.box[a][S] = b.lo[a];
+      dp.box[3 + a][S] = b.hi[a];
     }
-    cost[S] = C_INNER * box_area(box[S]) + best;
-    split[S] = (uint8_t)bp;
+    dp.cost[S] = ref_cost(T, leaves[lane]);
   }
-  // rewrite: assign internal node indices top-down (root keeps its index)
-  struct Item {
-    int S;
-    uint32_t node;
-  };
-  Item stk[8];
-  int sp = 0, next_inner = 1;
-  stk[sp++] = {full, root};
-  while (sp) {
-    Item it = stk[--sp];
-    int P = split[it.S], R = it.S ^ P;
-    uint32_t ch[2];
-    int sets[2] = {P, R};
-    for (int c = 0; c < 2; c++) {
-      int X = sets[c];
-      if ((X & (X - 1)) == 0) {
-        int k = __ffs(X) - 1;
-        ch[c] = leaves[k];
-      } else {
-        ch[c] = inner[next_inner++];
-        stk[sp++] = {X, ch[c]};
+  __syncwarp();
+  // subsets by size: every proper subset of S is complete before S
+  for (int size = 2; size <= nl; size++) {
+    for (int S = lane + 1; S <= full; S += 32) {
+      if (__popc(S) != size) continue;
+      const int low = S & -S;
+      GBox b;
+      for (int a = 0; a < 3; a++) {
+        b.lo[a] = fminf(dp.box[a][S ^ low], dp.box[a][low]);
+        b.hi[a] = fmaxf(dp.box[3 + a][S ^ low], dp.box[3 + a][low]);
+        dp.box[a][S] = b.lo[a];
+        dp.box[3 + a][S] = b.hi[a];
       }
-      set_parent(T, ch[c], it.node);
+      // subsets P of S containing the lowest bit, P != S
+      float best = 3.0e38f;
+      int bp = low;
+      const int rest = S ^ low;
+      for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {
+        const int P = Q | low;  // P ranges over low + proper subsets of rest
+        float c = dp.cost[P] + dp.cost[S ^ P];
+        if (c < best) {
+          best = c;
+          bp = P;
+        }
+        if (Q == 0) break;
+      }
+      dp.cost[S] = C_INNER * box_area(b) + best;
+      dp.split[S] = (uint8_t)bp;
     }
-    T.left[it.node] = ch[0];
-    T.right[it.node] = ch[1];
-    float cnt = 0.f;
-    // count = sum of leaf counts in S
-    for (int k = 0; k < nl; k++)
-      if (it.S & (1 << k)) cnt += ref_count(T, leaves[k]);
-    box_store(T.ilo, T.ihi, it.node, box[it.S], cost[it.S], cnt);
+    __syncwarp();
   }
+  if (lane == 0) {
+    // rewrite: assign internal node indices top-down (root keeps its index)
+    struct Item {
+      int S;
+      uint32_t node;
+    };
+    Item stk[8];
+    int sp = 0, next_inner = 1;
+    stk[sp++] = {full, root};
+    while (sp) {
+      Item it = stk[--sp];
+      int P = dp.split[it.S], R = it.S ^ P;
+      uint32_t ch[2];
+      int sets[2] = {P, R};
+      for (int c = 0; c < 2; c++) {
+        int X = sets[c];
+        if ((X & (X - 1)) == 0) {
+          int k = __ffs(X) - 1;
+          ch[c] = leaves[k];
+        } else {
+          ch[c] = inner[next_inner++];
+          stk[sp++] = {X, ch[c]};
+        }
+        set_parent(T, ch[c], it.node);
+      }
+      T.left[it.node] = ch[0];
+      T.right[it.node] = ch[1];
+      float cnt = 0.f;
+      // count = sum of leaf counts in S
+      for (int k = 0; k < nl; k++)
+        if (it.S & (1 << k)) cnt += ref_count(T, leaves[k]);
+      GBox b;
+      for (int a = 0; a < 3; a++) {
+        b.lo[a] = dp.box[a][it.S];
+        b.hi[a] = dp.box[3 + a][it.S];
+      }
+      box_store(T.ilo, T.ihi, it.node, b, dp.cost[it.S], cnt);
+    }
+    __threadfence();  // before any lane of this warp reports the root upward
+  }
+  __syncwarp();
 }
 
-// bounds, costs and counts bottom-up; optionally treelet restructuring
-__global__ void k_bottom_up(Tree T, int n, int optimize) {
+// Bounds, costs and counts bottom-up (the second thread to arrive at a node
+// processes it); optionally treelet restructuring, done by the whole warp
+// for each of its lanes' nodes in turn.  Launched with 256 threads.
+__global__ void __launch_bounds__(256) k_bottom_up(Tree T, int n, int optimize) {
+  __shared__ TreeletDP dps[8];
+  const int lane = threadIdx.x & 31;
+  TreeletDP& dp = dps[threadIdx.x >> 5];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  uint32_t node = T.parent_leaf[i];
-  while (node != 0xffffffffu) {
-    __threadfence();
-    if (atomicAdd(&T.flags[node], 1u) == 0) return;
-    __threadfence();
-    uint32_t l = left_of(T, node), r = right_of(T, node);
-    GBox b = box_union(ref_box(T, l), ref_box(T, r));
-    float cnt = ref_count(T, l) + ref_count(T, r);
-    float cost = C_INNER * box_area(b) + ref_cost(T, l) + ref_cost(T, r);
-    box_store(T.ilo, T.ihi, node, b, cost, cnt);
-    if (optimize && cnt >= 7.f) optimize_treelet(T, node);
-    __threadfence();
-    node = __ldcg(T.parent_int + node);
+  bool alive = i < n;
+  uint32_t node = alive ? T.parent_leaf[i] : 0xffffffffu;
+  while (__any_sync(0xffffffffu, alive)) {
+    bool need = false;
+    if (alive) {
+      if (node == 0xffffffffu) {
+        alive = false;
+      } else {
+        __threadfence();
+        if (atomicAdd(&T.flags[node], 1u) == 0) {
+          alive = false;  // the sibling subtree is not done: its thread continues
+        } else {
+          __threadfence();
+          uint32_t l = left_of(T, node), r = right_of(T, node);
+          GBox b = box_union(ref_box(T, l), ref_box(T, r));
+          float cnt = ref_count(T, l) + ref_count(T, r);
+          float cost = C_INNER * box_area(b) + ref_cost(T, l) + ref_cost(T, r);
+          box_store(T.ilo, T.ihi, node, b, cost, cnt);
+          need = optimize && cnt >= 7.f;
+        }
+      }
+    }
+    uint32_t m = __ballot_sync(0xffffffffu, need);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      optimize_treelet(T, __shfl_sync(0xffffffffu, node, src), dp, lane);
+    }
+    if (alive) {
+      __threadfence();
+      node = __ldcg(T.parent_int + node);
+    }
   }
 }
 

@@ -15,7 +15,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/pt.h"
@@ -602,10 +604,23 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
   pt::Bvh8Out bvh;
   size_t nn = 0;
   if (builder == 2 && n > 0) {
-    // records in call order, built into leaf order on the device
-    std::vector<float4> rec(3 * n);
-    for (size_t i = 0; i < n; i++) prim_record(ctx->prims[i], (uint32_t)i, &rec[3 * i]);
-    CK(ctx->d_rec_in.upload(rec.data(), rec.size(), st));
+    // records in call order (filled by several host threads for large
+    // scenes), built into leaf order on the device
+    std::unique_ptr<float4[]> rec(new (std::nothrow) float4[3 * n]);
+    if (!rec) return fail(ctx, PT_ENOMEM, "host memory for the primitive records");
+    {
+      const HostPrim* src = ctx->prims.data();
+      float4* dst = rec.get();
+      auto fill = [src, dst](size_t a, size_t b) {
+        for (size_t i = a; i < b; i++) prim_record(src[i], (uint32_t)i, dst + 3 * i);
+      };
+      const size_t parts = n >= ((size_t)1 << 16) ? 8 : 1;
+      std::vector<std::thread> pool;
+      for (size_t k = 1; k < parts; k++) pool.emplace_back(fill, n * k / parts, n * (k + 1) / parts);
+      fill(0, n / parts);
+      for (std::thread& th : pool) th.join();
+    }
+    CK(ctx->d_rec_in.upload(rec.get(), 3 * n, st));
     CK(d_nodes.ensure(5 * std::max<size_t>(1, n)));
     CK(d_prims.ensure(3 * n));
     CK(d_leaf_of_id.ensure(n));

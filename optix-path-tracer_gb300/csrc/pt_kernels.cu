@@ -1622,49 +1622,97 @@ __global__ void k_resolve(const float4* __restrict__ acc, uchar4* out, int n, in
 }
 
 // ------------------------------------------- environment sampling tables --
-// Weight of texel (r, c) = luminance x sin(theta_r).  One thread per row sums
-// its prefix in double, sequentially, in the oracle's order, so the float
-// CDFs come out identical on both sides; the marginal is summed by one thread.
-__global__ void k_env_rows(const float4* __restrict__ env, int w, int h, float* cond,
-                           double* rows) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= h) return;
-  float theta = PI_F * (((float)r + 0.5f) / (float)h);
-  double sn = (double)pt_sinf(theta);
+// Weight of texel (r, c) = luminance x sin(theta_r).  Each row's prefix is
+// summed in double, sequentially, in the oracle's order, so the float CDFs
+// come out identical on both sides.  One warp owns 32 rows: it stages 32x32
+// weight tiles in shared memory (coalesced texel loads), lane t adds up row
+// t of each tile in column order, and the divisions and stores of a tile run
+// across the lanes.  The first pass gives each row's total, the second the
+// normalised prefixes.
+__global__ void __launch_bounds__(32) k_env_rows(const float4* __restrict__ env, int w, int h,
+                                                 float* cond, double* rows) {
+  __shared__ double tile[32][33];
+  __shared__ double sn[32], tot[32];
+  const int t = threadIdx.x;
+  const int r0 = blockIdx.x * 32;
+  {
+    const int r = r0 + t;
+    float theta = PI_F * (((float)r + 0.5f) / (float)h);
+    sn[t] = r < h ? (double)pt_sinf(theta) : 0.0;
+  }
+  __syncwarp();
   double acc = 0.0;
-  for (int c = 0; c < w; c++) {
-    float4 t = env[(size_t)r * w + c];
-    double lum = 0.2126 * (double)t.x + 0.7152 * (double)t.y + 0.0722 * (double)t.z;
-    if (!(lum > 0.0)) lum = 0.0;
-    acc = acc + lum * sn;
+  for (int pass = 0; pass < 2; pass++) {
+    double run = 0.0;
+    for (int c0 = 0; c0 < w; c0 += 32) {
+      const int c = c0 + t;
+      for (int j = 0; j < 32; j++) {
+        const int r = r0 + j;
+        double v = 0.0;
+        if (r < h && c < w) {
+          float4 tx = env[(size_t)r * w + c];
+          double lum = 0.2126 * (double)tx.x + 0.7152 * (double)tx.y + 0.0722 * (double)tx.z;
+          if (!(lum > 0.0)) lum = 0.0;
+          v = lum * sn[j];
+        }
+        tile[j][t] = v;
+      }
+      __syncwarp();
+      const int kn = min(32, w - c0);
+      for (int k = 0; k < kn; k++) {
+        run = run + tile[t][k];
+        tile[t][k] = run;
+      }
+      __syncwarp();
+      if (pass == 1) {
+        for (int j = 0; j < 32; j++) {
+          const int r = r0 + j;
+          if (r < h && c < w) {
+            const double a = tot[j];
+            cond[(size_t)r * (w + 1) + c + 1] =
+                a > 0.0 ? (float)(tile[j][t] / a) : (float)((double)(c + 1) / (double)w);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (pass == 0) {
+      tot[t] = run;
+      acc = run;
+    }
+    __syncwarp();
   }
-  rows[r] = acc;
-  float* cr = cond + (size_t)r * (w + 1);
-  double pre = 0.0;
-  cr[0] = acc > 0.0 ? (float)(pre / acc) : 0.f;
-  for (int c = 0; c < w; c++) {
-    float4 t = env[(size_t)r * w + c];
-    double lum = 0.2126 * (double)t.x + 0.7152 * (double)t.y + 0.0722 * (double)t.z;
-    if (!(lum > 0.0)) lum = 0.0;
-    pre = pre + lum * sn;
-    cr[c + 1] = acc > 0.0 ? (float)(pre / acc) : (float)((double)(c + 1) / (double)w);
+  const int r = r0 + t;
+  if (r < h) {
+    rows[r] = acc;
+    cond[(size_t)r * (w + 1)] = 0.f;
+    cond[(size_t)r * (w + 1) + w] = 1.f;
   }
-  cr[w] = 1.f;
 }
 
-__global__ void k_env_marg(const double* __restrict__ rows, int h, float* marg, int* valid) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  double tot = 0.0;
-  for (int r = 0; r < h; r++) tot = tot + rows[r];
-  *valid = tot > 0.0 ? 1 : 0;
-  if (!(tot > 0.0)) return;
-  double mp = 0.0;
-  marg[0] = (float)(mp / tot);
-  for (int r = 0; r < h; r++) {
-    mp = mp + rows[r];
-    marg[r + 1] = (float)(mp / tot);
+// Marginal CDF over the row totals: the sums by one thread in the oracle's
+// order (rows[] becomes the running sums), the divisions by the block.
+__global__ void k_env_marg(double* rows, int h, float* marg, int* valid) {
+  __shared__ double tot_s;
+  if (blockIdx.x != 0) return;
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int r = 0; r < h; r++) tot = tot + rows[r];
+    double mp = 0.0;
+    for (int r = 0; r < h; r++) {
+      mp = mp + rows[r];
+      rows[r] = mp;
+    }
+    tot_s = tot;
+    *valid = tot > 0.0 ? 1 : 0;
   }
-  marg[h] = 1.f;
+  __syncthreads();
+  const double tot = tot_s;
+  if (!(tot > 0.0)) return;
+  for (int r = threadIdx.x; r < h; r += blockDim.x) marg[r + 1] = (float)(rows[r] / tot);
+  if (threadIdx.x == 0) marg[0] = 0.f;
+  __syncthreads();
+  if (threadIdx.x == 0) marg[h] = 1.f;
 }
 
 // ------------------------------------------------------- host launchers ---
@@ -1865,8 +1913,8 @@ void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* pri
 
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,
                     int* valid, cudaStream_t st) {
-  k_env_rows<<<(h + 127) / 128, 128, 0, st>>>(env, w, h, cond, rows);
-  k_env_marg<<<1, 32, 0, st>>>(rows, h, marg, valid);
+  k_env_rows<<<(h + 31) / 32, 32, 0, st>>>(env, w, h, cond, rows);
+  k_env_marg<<<1, 256, 0, st>>>(rows, h, marg, valid);
 }
 
 void launch_resolve(const float4* acc, uchar4* out, int n, int frame, cudaStream_t st) {

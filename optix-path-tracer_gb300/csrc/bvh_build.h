@@ -63,7 +63,10 @@ PT_BVH_HD inline void encode_node_dev(const Box& parent, const WideChild* ch, in
   memcpy(&out[1], &p[1], 4);
   memcpy(&out[2], &p[2], 4);
   uint32_t imask = 0, rank = 0;
-  uint32_t meta[2] = {0, 0}, qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  // empty slots keep an inverted box (lo 255, hi 0): no ray passes its slab test
+  uint32_t meta[2] = {0, 0}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  uint32_t qlo[3][2] = {{0xffffffffu, 0xffffffffu}, {0xffffffffu, 0xffffffffu},
+                        {0xffffffffu, 0xffffffffu}};
   for (int i = 0; i < nch; i++) {
     const WideChild& c = ch[i];
     uint32_t m;
@@ -80,7 +83,7 @@ PT_BVH_HD inline void encode_node_dev(const Box& parent, const WideChild* ch, in
       float hi = ceilf((c.box.hi[a] - p[a]) / step[a]) + 1.0f;
       lo = fminf(fmaxf(lo, 0.0f), 255.0f);
       hi = fminf(fmaxf(hi, 0.0f), 255.0f);
-      qlo[a][i >> 2] |= (uint32_t)lo << (8 * (i & 3));
+      qlo[a][i >> 2] = (qlo[a][i >> 2] & ~(0xffu << (8 * (i & 3)))) | ((uint32_t)lo << (8 * (i & 3)));
       qhi[a][i >> 2] |= (uint32_t)hi << (8 * (i & 3));
     }
   }

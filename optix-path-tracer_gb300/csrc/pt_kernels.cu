@@ -382,7 +382,9 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
                           __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
         float tn = max3f(tx.x, ty.x, fmaxf(tz.x, tmin));
         float tf = min3f(tx.y, ty.y, fminf(tz.y, tlim));
-        if (meta != 0 && tn <= tf) {
+        // an empty slot (meta 0) has an inverted box and fails here; were it
+        // to pass (infinite slab distances), it is a leaf of no primitives
+        if (tn <= tf) {
           if (consistent && (meta & 0x80u)) {
             imask |= 1u << (meta & 7u);
             if (PT_ANYHIT_NEAREST) kmin = min(kmin, (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u));

@@ -19,7 +19,8 @@
  *   n3 = (qlo.z[0..3], qlo.z[4..7], qhi.x[0..3], qhi.x[4..7])
  *   n4 = (qhi.y[0..3], qhi.y[4..7], qhi.z[0..3], qhi.z[4..7])
  *   child box = p + q * 2^(e-127) per axis (q: 8-bit, rounded outward)
- *   meta[i] = 0: empty slot; 0x80 | r: internal child, node child_base + r;
+ *   meta[i] = 0: empty slot (its box inverted: qlo 255, qhi 0);
+ *             0x80 | r: internal child, node child_base + r;
  *             (count << 5) | off (count 1..3): leaf, prims prim_base + off ..
  */
 #ifndef PT_TYPES_H

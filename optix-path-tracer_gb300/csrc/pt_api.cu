@@ -228,6 +228,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_env_marg.release();
   ctx->d_env_cond.release();
   ctx->d_env_rows.release();
+  ctx->d_env_pre.release();
   ctx->d_env_valid.release();
   ctx->d_slot_f4.release();
   ctx->d_slot_u4.release();
@@ -714,9 +715,10 @@ PT_API int pt_commit(pt_context* ctx) {
     CK(ctx->d_env_marg.ensure((size_t)h + 1));
     CK(ctx->d_env_cond.ensure((size_t)h * (w + 1)));
     CK(ctx->d_env_rows.ensure((size_t)h));
+    CK(ctx->d_env_pre.ensure((size_t)w * h));
     CK(ctx->d_env_valid.ensure(1));
     pt::launch_env_cdf(ctx->d_env.p, w, h, ctx->d_env_marg.p, ctx->d_env_cond.p,
-                       ctx->d_env_rows.p, ctx->d_env_valid.p, st);
+                       ctx->d_env_rows.p, ctx->d_env_pre.p, ctx->d_env_valid.p, st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&ctx->env_valid, ctx->d_env_valid.p, sizeof(int), cudaMemcpyDeviceToHost,
                        st));

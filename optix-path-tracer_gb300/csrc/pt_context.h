@@ -105,6 +105,7 @@ struct pt_context {
   DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
   DevBuf<float> d_env_marg, d_env_cond;  // environment sampling CDFs
   DevBuf<double> d_env_rows;
+  DevBuf<double> d_env_pre;   // per texel: weights, then row prefix sums
   DevBuf<int> d_env_valid;
   int env_valid = 0;
   DevScene scene{};

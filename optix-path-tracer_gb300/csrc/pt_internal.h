@@ -196,7 +196,7 @@ void launch_relocate(uint4* nodes, size_t n_nodes, uint32_t node_off, uint32_t p
                      uint32_t mat_off, uint32_t* leaf_of_id, uint4* tri_attr, uint32_t attr_off,
                      cudaStream_t st);
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,
-                    int* valid, cudaStream_t st);
+                    double* pre, int* valid, cudaStream_t st);
 void launch_accumulate(const float4* results, float4* acc, int w, int h, int frames,
                        cudaStream_t st);
 /* acc: 4 doubles per pixel (16-byte aligned) */

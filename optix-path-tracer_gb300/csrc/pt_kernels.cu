@@ -1626,69 +1626,51 @@ __global__ void k_resolve(const float4* __restrict__ acc, uchar4* out, int n, in
 // ------------------------------------------- environment sampling tables --
 // Weight of texel (r, c) = luminance x sin(theta_r).  Each row's prefix is
 // summed in double, sequentially, in the oracle's order, so the float CDFs
-// come out identical on both sides.  One warp owns 32 rows: it stages 32x32
-// weight tiles in shared memory (coalesced texel loads), lane t adds up row
-// t of each tile in column order, and the divisions and stores of a tile run
-// across the lanes.  The first pass gives each row's total, the second the
-// normalised prefixes.
-__global__ void __launch_bounds__(32) k_env_rows(const float4* __restrict__ env, int w, int h,
-                                                 float* cond, double* rows) {
-  __shared__ double tile[32][33];
-  __shared__ double sn[32], tot[32];
-  const int t = threadIdx.x;
-  const int r0 = blockIdx.x * 32;
-  {
-    const int r = r0 + t;
+// come out identical on both sides.  FP64 arithmetic is scarce on this GPU,
+// so the per-texel work (weights, then the normalising divisions) runs on
+// every SM, and only the dependent additions of a row stay in one thread:
+//   k_env_weights  pre[r][c] = weight (all texels)
+//   k_env_prefix   pre[r][c] = running sum of row r, rows[r] = its total
+//   k_env_cond     conditional CDFs (all entries)
+__global__ void k_env_weights(const float4* __restrict__ env, int w, int h, double* pre) {
+  const size_t n = (size_t)w * h;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / (size_t)w);
     float theta = PI_F * (((float)r + 0.5f) / (float)h);
-    sn[t] = r < h ? (double)pt_sinf(theta) : 0.0;
+    double sn = (double)pt_sinf(theta);
+    float4 t = env[i];
+    double lum = 0.2126 * (double)t.x + 0.7152 * (double)t.y + 0.0722 * (double)t.z;
+    if (!(lum > 0.0)) lum = 0.0;
+    pre[i] = lum * sn;
   }
-  __syncwarp();
+}
+
+__global__ void k_env_prefix(double* pre, int w, int h, double* rows) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= h) return;
+  double* p = pre + (size_t)r * w;
   double acc = 0.0;
-  for (int pass = 0; pass < 2; pass++) {
-    double run = 0.0;
-    for (int c0 = 0; c0 < w; c0 += 32) {
-      const int c = c0 + t;
-      for (int j = 0; j < 32; j++) {
-        const int r = r0 + j;
-        double v = 0.0;
-        if (r < h && c < w) {
-          float4 tx = env[(size_t)r * w + c];
-          double lum = 0.2126 * (double)tx.x + 0.7152 * (double)tx.y + 0.0722 * (double)tx.z;
-          if (!(lum > 0.0)) lum = 0.0;
-          v = lum * sn[j];
-        }
-        tile[j][t] = v;
-      }
-      __syncwarp();
-      const int kn = min(32, w - c0);
-      for (int k = 0; k < kn; k++) {
-        run = run + tile[t][k];
-        tile[t][k] = run;
-      }
-      __syncwarp();
-      if (pass == 1) {
-        for (int j = 0; j < 32; j++) {
-          const int r = r0 + j;
-          if (r < h && c < w) {
-            const double a = tot[j];
-            cond[(size_t)r * (w + 1) + c + 1] =
-                a > 0.0 ? (float)(tile[j][t] / a) : (float)((double)(c + 1) / (double)w);
-          }
-        }
-      }
-      __syncwarp();
-    }
-    if (pass == 0) {
-      tot[t] = run;
-      acc = run;
-    }
-    __syncwarp();
+  for (int c = 0; c < w; c++) {
+    acc = acc + p[c];
+    p[c] = acc;
   }
-  const int r = r0 + t;
-  if (r < h) {
-    rows[r] = acc;
-    cond[(size_t)r * (w + 1)] = 0.f;
-    cond[(size_t)r * (w + 1) + w] = 1.f;
+  rows[r] = acc;
+}
+
+__global__ void k_env_cond(const double* __restrict__ pre, const double* __restrict__ rows, int w,
+                           int h, float* cond) {
+  const size_t n = (size_t)(w + 1) * h;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / (size_t)(w + 1));
+    const int k = (int)(i - (size_t)r * (w + 1));
+    const double a = rows[r];
+    float v;
+    if (k == 0) v = 0.f;
+    else if (k == w) v = 1.f;
+    else v = a > 0.0 ? (float)(pre[(size_t)r * w + k - 1] / a) : (float)((double)k / (double)w);
+    cond[i] = v;
   }
 }
 
@@ -1914,8 +1896,11 @@ void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* pri
 }
 
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,
-                    int* valid, cudaStream_t st) {
-  k_env_rows<<<(h + 31) / 32, 32, 0, st>>>(env, w, h, cond, rows);
+                    double* pre, int* valid, cudaStream_t st) {
+  const int g = num_sms() * 8;
+  k_env_weights<<<g, 256, 0, st>>>(env, w, h, pre);
+  k_env_prefix<<<(h + 31) / 32, 32, 0, st>>>(pre, w, h, rows);
+  k_env_cond<<<g, 256, 0, st>>>(pre, rows, w, h, cond);
   k_env_marg<<<1, 256, 0, st>>>(rows, h, marg, valid);
 }
 

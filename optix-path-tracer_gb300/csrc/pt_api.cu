@@ -252,6 +252,8 @@ PT_API int pt_context_destroy(pt_context* ctx) {
     G.out.release();
     G.rows.release();
     G.rec.release();
+    G.coll_u.release();
+    G.coll_f.release();
   }
   ctx->d_tmp.release();
   ctx->d_tmpu.release();

@@ -67,6 +67,8 @@ struct GuideState {
   DevBuf<GuidePacked> out;   // per path slot: decoded guide
   DevBuf<uint32_t> rows;     // per path slot: positions selected for inference
   DevBuf<GuideSample> rec;   // training records of the current frame
+  DevBuf<uint32_t> coll_u;   // record collection scratch: per-block counts and offsets
+  DevBuf<float> coll_f;      //   and per-block weight sums
   uint32_t rec_stride = 1, rec_n = 0;
   float lr = 1e-2f;          // Adam learning rate of the online training
   int steps = 8;             // Adam steps per frame on the frame's samples

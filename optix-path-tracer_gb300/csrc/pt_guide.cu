@@ -658,48 +658,119 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(128));
 }
 
-// Completed training records with a positive weight, appended to the
-// training array (warp-aggregated atomics).
-__global__ void k_guide_collect(const GuideSample* __restrict__ rec, uint32_t n, GuideSample* out,
-                                uint32_t* count, float* wsum, uint32_t cap, float exponent) {
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t iters = (n + stride - 1) / stride;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (uint32_t it = 0; it < iters; it++, i += stride) {
+// Completed training records with a positive weight, copied to the
+// training array in record order (the first `cap` of them), with the sum of
+// their weights: a stable compaction over blocks of 1024 records, so the
+// training array, and with it the whole training, is the same on every run.
+//   k_guide_collect_count   takers per block
+//   k_guide_collect_scan    block offsets (one thread, in block order), count
+//   k_guide_collect_write   the copies; per-block weight sums (fixed order)
+//   k_guide_collect_sum     the weight sum (one thread, in block order)
+constexpr uint32_t kCollectPer = 1024;  // records per block: 4 chunks of 256
+
+__device__ __forceinline__ bool collect_take(const GuideSample& r) {
+  return r.pad[1] == 2.f && r.weight > 0.f;
+}
+
+__global__ void __launch_bounds__(256) k_guide_collect_count(const GuideSample* __restrict__ rec,
+                                                             uint32_t n, uint32_t* block_cnt) {
+  __shared__ uint32_t wc[8];
+  uint32_t c = 0;
+  for (int k = 0; k < 4; k++) {
+    const uint32_t i = blockIdx.x * kCollectPer + k * 256 + threadIdx.x;
+    if (i < n && collect_take(rec[i])) c++;
+  }
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) wc[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; w++) t += wc[w];
+    block_cnt[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_guide_collect_scan(const uint32_t* __restrict__ block_cnt, uint32_t nb,
+                                     uint32_t* offsets, uint32_t* count, uint32_t cap) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  uint32_t t = 0;
+  for (uint32_t b = 0; b < nb; b++) {
+    offsets[b] = t;
+    t += block_cnt[b];
+  }
+  *count = t < cap ? t : cap;
+}
+
+__global__ void __launch_bounds__(256) k_guide_collect_write(const GuideSample* __restrict__ rec,
+                                                             uint32_t n,
+                                                             const uint32_t* __restrict__ offsets,
+                                                             GuideSample* out, float* block_w,
+                                                             uint32_t cap, float exponent) {
+  __shared__ uint32_t wtot[8];
+  __shared__ float ws[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t run = offsets[blockIdx.x];
+  float wacc = 0.f;
+  for (int k = 0; k < 4; k++) {
+    const uint32_t i = blockIdx.x * kCollectPer + k * 256 + threadIdx.x;
     GuideSample r;
     bool take = false;
     if (i < n) {
       r = rec[i];
-      take = r.pad[1] == 2.f && r.weight > 0.f;
+      take = collect_take(r);
       if (take && exponent != 1.f) r.weight = powf(r.weight, exponent);
     }
-    uint32_t mask = __ballot_sync(0xffffffffu, take);
-    uint32_t base = 0;
-    int lane = threadIdx.x & 31;
-    if (mask) {
-      int leader = __ffs(mask) - 1;
-      if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
-      base = __shfl_sync(0xffffffffu, base, leader);
+    const uint32_t m = __ballot_sync(0xffffffffu, take);
+    if (lane == 0) wtot[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    uint32_t before = 0, chunk = 0;
+    for (int w = 0; w < 8; w++) {
+      if (w < warp) before += wtot[w];
+      chunk += wtot[w];
     }
     if (take) {
-      uint32_t k = base + __popc(mask & ((1u << lane) - 1u));
-      if (k < cap) {
-        out[k] = r;
-        atomicAdd(wsum, r.weight);
+      const uint32_t dst = run + before + (uint32_t)__popc(m & ((1u << lane) - 1u));
+      if (dst < cap) {
+        out[dst] = r;
+        wacc += r.weight;
       }
     }
+    run += chunk;
+    __syncthreads();
   }
+  for (int o = 16; o > 0; o >>= 1) wacc += __shfl_down_sync(0xffffffffu, wacc, o);
+  if (lane == 0) ws[warp] = wacc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < 8; w++) t += ws[w];
+    block_w[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_guide_collect_sum(const float* __restrict__ block_w, uint32_t nb, float* wsum) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  float t = 0.f;
+  for (uint32_t b = 0; b < nb; b++) t += block_w[b];
+  *wsum = t;
 }
 
 // ------------------------------------------------------------ launchers ----
 namespace pt {
 
+uint32_t guide_collect_blocks(uint32_t n) { return (n + kCollectPer - 1) / kCollectPer; }
+
 void launch_guide_collect(const GuideSample* rec, uint32_t n, GuideSample* out, uint32_t* count,
-                          float* wsum, uint32_t cap, float exponent, cudaStream_t st) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_guide_collect<<<sms * 4, 256, 0, st>>>(rec, n, out, count, wsum, cap, exponent);
+                          float* wsum, uint32_t cap, float exponent, uint32_t* scratch_u,
+                          float* scratch_f, cudaStream_t st) {
+  const uint32_t nb = guide_collect_blocks(n);
+  if (nb == 0) return;  // the caller zeroed count and wsum
+  uint32_t* block_cnt = scratch_u;
+  uint32_t* offsets = scratch_u + nb;
+  k_guide_collect_count<<<nb, 256, 0, st>>>(rec, n, block_cnt);
+  k_guide_collect_scan<<<1, 32, 0, st>>>(block_cnt, nb, offsets, count, cap);
+  k_guide_collect_write<<<nb, 256, 0, st>>>(rec, n, offsets, out, scratch_f, cap, exponent);
+  k_guide_collect_sum<<<1, 32, 0, st>>>(scratch_f, nb, wsum);
 }
 
 size_t guide_train_smem() { return (size_t)kWeights + 5 * kTileT + 2 * (kTileG + kGuard); }

@@ -128,8 +128,11 @@ void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ct
                         const GuideInferArgs& a, int grid, cudaStream_t st);
 /* Appends the completed records with a positive weight to out (at most cap;
  * count and wsum accumulate on the device). */
+// scratch: 2 x guide_collect_blocks(n) uint32 and guide_collect_blocks(n) floats
+uint32_t guide_collect_blocks(uint32_t n);
 void launch_guide_collect(const GuideSample* rec, uint32_t n, GuideSample* out, uint32_t* count,
-                          float* wsum, uint32_t cap, float exponent, cudaStream_t st);
+                          float* wsum, uint32_t cap, float exponent, uint32_t* scratch_u,
+                          float* scratch_f, cudaStream_t st);
 }  // namespace pt
 #endif
 

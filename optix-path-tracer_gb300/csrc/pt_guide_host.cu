@@ -118,6 +118,8 @@ int pth::guide_frame_begin(pt_context* ctx, int w, int h) {
   G.rec_stride = (uint32_t)std::max<size_t>(1, (wh + target - 1) / target);
   G.rec_n = (uint32_t)(2 * ((wh + G.rec_stride - 1) / G.rec_stride));
   GK(G.rec.ensure(G.rec_n));
+  GK(G.coll_u.ensure(2 * (size_t)pt::guide_collect_blocks(G.rec_n) + 1));
+  GK(G.coll_f.ensure((size_t)pt::guide_collect_blocks(G.rec_n) + 1));
   GK(G.samples.ensure((size_t)1 << 18));
   GK(cudaMemsetAsync(G.rec.p, 0, (size_t)G.rec_n * sizeof(GuideSample), ctx->stream));
   return PT_OK;
@@ -130,7 +132,7 @@ int pth::guide_frame_train(pt_context* ctx) {
   GK(cudaMemsetAsync(G.counters.p, 0, 4, st));  // the failure flags stay
   GK(cudaMemsetAsync(G.scalars.p, 0, 8, st));
   pt::launch_guide_collect(G.rec.p, G.rec_n, G.samples.p, G.counters.p, G.scalars.p + 1, cap,
-                           G.exponent, st);
+                           G.exponent, G.coll_u.p, G.coll_f.p, st);
   GuideTrainArgs a;
   memset(&a, 0, sizeof(a));
   a.w = (const __nv_bfloat16*)G.wbf.p;

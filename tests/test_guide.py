@@ -218,6 +218,21 @@ def test_guide_lowers_error_at_equal_samples(ptgb_mod):
     g.close()
 
 
+def test_guided_render_is_deterministic(ptgb_mod):
+    """Online training collects its samples in record order and sums in a
+    fixed order, so two guided renders from the same initial network give
+    the same image bit for bit."""
+    P = ptgb_mod.GpuRenderer.params
+    s = _box(ptgb_mod, 32)
+    out = []
+    for _ in range(2):
+        g = ptgb_mod.GpuRenderer(s)
+        g.guide_init(5)
+        out.append(g.render64(P(32, 32, 12, mode=1, guide=1)))
+        g.close()
+    assert np.array_equal(out[0], out[1])
+
+
 def test_guide_argument_checks(ptgb_mod):
     P = ptgb_mod.GpuRenderer.params
     g = ptgb_mod.GpuRenderer(_box(ptgb_mod, 16))

@@ -39,3 +39,24 @@ def test_python_signatures_cover_header(ptgb_mod):
 def test_version_string(ptgb_mod):
     lib = ptgb_mod.load_library()
     assert b"sm_103a" in lib.pt_version()
+
+
+def test_context_options_checked_without_gpu(ptgb_mod):
+    """pt_context_create rejects out-of-range options before it touches the
+    device (pt.h: bvh_width 2..8, shade_order 0..2, refetch_lanes 0..32)."""
+    lib = ptgb_mod.load_library()
+    for field, value in (("refetch_lanes", 33), ("refetch_lanes", -1), ("bvh_width", 9),
+                         ("bvh_width", 1), ("shade_order", 3)):
+        opt = ptgb_mod.Options()
+        setattr(opt, field, value)
+        ctx = ctypes.c_void_p()
+        rc = lib.pt_context_create(ctypes.byref(opt), ctypes.byref(ctx))
+        assert rc == -1 and not ctx.value, (field, value, rc)
+
+
+def test_batch_options_checked_without_gpu(ptgb_mod):
+    lib = ptgb_mod.load_library()
+    opt = ptgb_mod.Options()
+    opt.refetch_lanes = 40
+    b = ctypes.c_void_p()
+    assert lib.pt_batch_create(ctypes.byref(opt), ctypes.byref(b)) == -1 and not b.value

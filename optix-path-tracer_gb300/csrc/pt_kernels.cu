@@ -14,6 +14,10 @@
  *   k_trace_t<SHADOW> shadow rays (programs/hit.cu:16-24, closest-hit rule)
  *   k_finish        rest of Direct_Light (MIS), BSDF continuation
  *   k_advance       counter bookkeeping (one thread)
+ * The consistent mode (NEE over lights and the environment with MIS) uses
+ * k_shade_c, k_trace_t<OCCLUDED> (any hit before the light ends the ray) and
+ * k_finish_c in the same places.  Trace warps take rays from a per-launch
+ * counter (ray_next), so no warp sits idle while others still have rays.
  * Path state is kept in queue order: paths that continue are appended,
  * compacted with warp-aggregated atomics (ballot + popc prefix), to the other
  * buffer of a ping-pong pair, so every kernel streams its arrays

@@ -155,6 +155,42 @@ PT_API int pt_add_mesh(pt_context* ctx, const float* verts, size_t nv, const uin
                        const float* normals, const float* uvs, const float xform[12],
                        uint32_t* first_prim_id);
 
+/* ---- file formats (host side, no device work) ----------------------------
+ * Wavefront OBJ/MTL, as the reference's Mesh(file, folder[, BRDF*]) reads it
+ * through tinyobjloader (mesh.hpp:49-204, lib/tiny_obj_loader.h): v / vt /
+ * vn / f (any of v, v/vt, v//vn, v/vt/vn; negative indices count back),
+ * polygons ear-clipped as that loader does, usemtl / mtllib (newmtl, Ka,
+ * Kd, map_Kd).  Triangles are de-indexed: three corners each, in file order
+ * (mesh.hpp:123-138).  Normals / uvs are kept when every corner has one. */
+typedef struct pt_obj pt_obj;
+#define PT_OBJ_NO_MATERIAL 0xffffffffu /* mat_per_tri of a face without usemtl */
+#define PT_OBJ_MTL 0xfffffffeu         /* pt_add_obj: materials from the MTL file */
+PT_API int pt_obj_load(const char* path, pt_obj** out);
+PT_API int pt_obj_free(pt_obj* mesh);
+PT_API int pt_obj_info(const pt_obj* mesh, size_t* n_tris, size_t* n_materials,
+                       int* has_normals, int* has_uvs);
+/* verts 9 floats per triangle, normals 9, uvs 6, mat_per_tri 1 (any may be NULL) */
+PT_API int pt_obj_get(const pt_obj* mesh, float* verts, float* normals, float* uvs,
+                      uint32_t* mat_per_tri);
+PT_API int pt_obj_material(const pt_obj* mesh, size_t k, char* name, size_t name_cap,
+                           float ka[3], float kd[3], char* map_kd, size_t map_cap);
+/* Mesh::getGeometryInstance (mesh.hpp:49-204): the mesh into the scene with
+ * `material` on every face, or, with PT_OBJ_MTL, one Lambertian per MTL
+ * material coloured by its ambient term Ka (mesh.hpp:78-96; map_Kd image
+ * textures are not supported and fall back to Ka). */
+PT_API int pt_add_obj(pt_context* ctx, const pt_obj* mesh, uint32_t material,
+                      const float xform[12], uint32_t* first_prim_id);
+/* Radiance HDR in (lib/HDRloader.cpp): rgba NULL returns the size only;
+ * else w*h*4 floats, first scanline first, (r,g,b)/256 * 2^(e-128), a = 1.
+ * Only the "-Y h +X w" orientation, as the reference reads. */
+PT_API int pt_hdr_load(const char* path, int* w, int* h, float* rgba);
+/* Save_HDR (image_save.hpp:40-73): sum/spp, Reinhard c/(1+c), RGBE. */
+PT_API int pt_hdr_save(const char* path, int w, int h, const float* accum_rgba, int spp);
+/* Save_PNG (image_save.hpp:7-37): sqrt(sum/spp) clamped, x255.99, 8-bit RGB. */
+PT_API int pt_png_save(const char* path, int w, int h, const float* accum_rgba, int spp);
+/* message of the last failed file-format call of this thread */
+PT_API const char* pt_io_last_error(void);
+
 /* ---- lights (host_includes/pdfs.hpp + Light_Sampler, host_common.hpp:65-68) */
 /* Rectangle_PDF(a0,a1,b0,b1,k,axis) + emission  pdfs.hpp:17-80 */
 PT_API int pt_add_light_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k,

@@ -93,6 +93,17 @@ SIGNATURES = {
     "pt_add_box": [_P, _F3, _F3, ctypes.c_uint32, _P, _U32P],
     "pt_add_mesh": [_P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, ctypes.c_uint32, _P, _P,
                     _P, _U32P],
+    "pt_obj_load": [ctypes.c_char_p, ctypes.POINTER(_P)],
+    "pt_obj_free": [_P],
+    "pt_obj_info": [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t),
+                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    "pt_obj_get": [_P, _P, _P, _P, _P],
+    "pt_obj_material": [_P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t, _P, _P,
+                        ctypes.c_char_p, ctypes.c_size_t],
+    "pt_add_obj": [_P, _P, ctypes.c_uint32, _P, _U32P],
+    "pt_hdr_load": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _P],
+    "pt_hdr_save": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int],
+    "pt_png_save": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int],
     "pt_add_light_rect": [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                           ctypes.c_float, ctypes.c_int, _F3],
     "pt_add_light_sphere": [_P, _F3, ctypes.c_float, _F3],
@@ -148,12 +159,89 @@ def load_library(path=LIB_PATH):
     lib.pt_version.restype = ctypes.c_char_p
     lib.pt_batch_last_error.argtypes = [_P]
     lib.pt_batch_last_error.restype = ctypes.c_char_p
+    lib.pt_io_last_error.argtypes = []
+    lib.pt_io_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 
 
 def f3(v):
     return _F3(*[float(x) for x in v])
+
+
+# ----------------------------------------------------------- file formats
+PT_OBJ_NO_MATERIAL = 0xFFFFFFFF
+PT_OBJ_MTL = 0xFFFFFFFE
+
+
+def _io_check(lib, rc):
+    if rc != 0:
+        raise PtError(rc, lib.pt_io_last_error().decode())
+
+
+class ObjMesh:
+    """A Wavefront OBJ file read by pt_obj_load (de-indexed triangles)."""
+
+    def __init__(self, path):
+        self.lib = load_library()
+        h = _P()
+        _io_check(self.lib, self.lib.pt_obj_load(str(path).encode(), ctypes.byref(h)))
+        self.h = h
+        nt, nm = ctypes.c_size_t(), ctypes.c_size_t()
+        hn, hu = ctypes.c_int(), ctypes.c_int()
+        _io_check(self.lib, self.lib.pt_obj_info(h, ctypes.byref(nt), ctypes.byref(nm),
+                                                 ctypes.byref(hn), ctypes.byref(hu)))
+        self.n_tris, self.n_materials = nt.value, nm.value
+        self.verts = np.zeros((self.n_tris, 3, 3), np.float32)
+        self.normals = np.zeros((self.n_tris, 3, 3), np.float32) if hn.value else None
+        self.uvs = np.zeros((self.n_tris, 3, 2), np.float32) if hu.value else None
+        self.mat = np.zeros(self.n_tris, np.uint32)
+        _io_check(self.lib, self.lib.pt_obj_get(h, _ptr(self.verts), _ptr(self.normals),
+                                                _ptr(self.uvs), _ptr(self.mat)))
+
+    def material(self, k):
+        name = ctypes.create_string_buffer(256)
+        tex = ctypes.create_string_buffer(256)
+        ka = np.zeros(3, np.float32)
+        kd = np.zeros(3, np.float32)
+        _io_check(self.lib, self.lib.pt_obj_material(self.h, k, name, 256, _ptr(ka), _ptr(kd),
+                                                     tex, 256))
+        return {"name": name.value.decode(), "Ka": ka, "Kd": kd, "map_Kd": tex.value.decode()}
+
+    def close(self):
+        if self.h:
+            self.lib.pt_obj_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def hdr_load(path):
+    """A Radiance HDR file as an HxWx4 float32 array (pt_hdr_load)."""
+    lib = load_library()
+    w, h = ctypes.c_int(), ctypes.c_int()
+    _io_check(lib, lib.pt_hdr_load(str(path).encode(), ctypes.byref(w), ctypes.byref(h), None))
+    out = np.zeros((h.value, w.value, 4), np.float32)
+    _io_check(lib, lib.pt_hdr_load(str(path).encode(), ctypes.byref(w), ctypes.byref(h), _ptr(out)))
+    return out
+
+
+def hdr_save(path, accum, spp):
+    """Save_HDR of an HxWx4 float32 accumulation (pt_hdr_save)."""
+    lib = load_library()
+    a = np.ascontiguousarray(accum, np.float32)
+    _io_check(lib, lib.pt_hdr_save(str(path).encode(), a.shape[1], a.shape[0], _ptr(a), int(spp)))
+
+
+def png_save(path, accum, spp):
+    """Save_PNG of an HxWx4 float32 accumulation (pt_png_save)."""
+    lib = load_library()
+    a = np.ascontiguousarray(accum, np.float32)
+    _io_check(lib, lib.pt_png_save(str(path).encode(), a.shape[1], a.shape[0], _ptr(a), int(spp)))
 
 
 def _ptr(a):
@@ -212,6 +300,7 @@ class Scene:
     def __init__(self):
         self.materials = []   # (kind, c0, c1, p0, p1)
         self.items = []       # ("sphere"|"rect"|"box"|"mesh", args...)
+        self.add_obj = {}     # item index -> (ObjMesh, material or None): load with pt_add_obj
         self.lights = []      # ("rect"|"sphere", args..., emission)
         self.miss = ("constant", (0.0, 0.0, 0.0))
         self.camera = None
@@ -276,6 +365,30 @@ class Scene:
         self.items.append(("mesh", verts, idx, mat, mat_per_tri, normals, uvs, xform))
         first = self.n_prims
         self.n_prims += len(idx)
+        return first
+
+    def obj(self, mesh, material=None, xform=None, via_add_obj=False):
+        """An ObjMesh as the reference's Mesh adds it: `material` on every
+        face, or (None) one Lambertian per MTL material coloured by Ka, faces
+        without usemtl on the first (a grey Lambertian without an MTL file).
+        via_add_obj: the GPU renderer loads it through pt_add_obj instead of
+        pt_add_mesh (the oracle always sees the triangle arrays)."""
+        nt = mesh.n_tris
+        per = None
+        mat = material
+        if material is None:
+            ids = [self.lambertian(tuple(mesh.material(k)["Ka"])) for k in range(mesh.n_materials)]
+            if not ids:
+                ids = [self.lambertian((0.5, 0.5, 0.5))]
+            table = np.array(ids, np.uint32)
+            per = np.where(mesh.mat == PT_OBJ_NO_MATERIAL, table[0],
+                           table[np.minimum(mesh.mat, len(ids) - 1)]).astype(np.uint32)
+            mat = ids[0]
+        first = self.mesh(mesh.verts.reshape(-1, 3), np.arange(3 * nt, dtype=np.uint32).reshape(-1, 3),
+                          mat, per, None if mesh.normals is None else mesh.normals.reshape(-1, 3),
+                          None if mesh.uvs is None else mesh.uvs.reshape(-1, 2), xform)
+        if via_add_obj:
+            self.add_obj[len(self.items) - 1] = (mesh, material)
         return first
 
     # lights (host_includes/pdfs.hpp)
@@ -358,9 +471,15 @@ class GpuRenderer:
                 self._c(L.pt_material_ashikhmin_shirley(c, f3(c0), f3(c1), p0, p1,
                                                         ctypes.byref(mid)))
             mids.append(mid.value)
-        for it in scene.items:
+        add_obj = getattr(scene, "add_obj", {})
+        for k, it in enumerate(scene.items):
             pid = ctypes.c_uint32()
-            if it[0] == "sphere":
+            if k in add_obj:
+                mesh, m = add_obj[k]
+                xf = it[7]
+                self._c(L.pt_add_obj(c, mesh.h, PT_OBJ_MTL if m is None else mids[m], _ptr(xf),
+                                     ctypes.byref(pid)))
+            elif it[0] == "sphere":
                 _, cen, r, m, xf = it
                 self._c(L.pt_add_sphere(c, f3(cen), r, mids[m], _ptr(xf), ctypes.byref(pid)))
             elif it[0] == "rect":

@@ -293,6 +293,15 @@ PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame,
                                  int max_bounces);
 PT_API int pt_guide_get_params(pt_context* ctx, float* params);
 PT_API int pt_guide_set_params(pt_context* ctx, const float* params);
+/* Checkpoint of the online training: FP32 weights, Adam first and second
+ * moments (PT_GUIDE_STATE_FLOATS floats) and the Adam step count.  Training
+ * is deterministic, so a guided render resumed from a checkpoint continues
+ * bit for bit as the uninterrupted one (with the same pt_guide_set_training
+ * options).  The reference keeps only its in-memory accumulation
+ * (raygen.cu:153-154). */
+#define PT_GUIDE_STATE_FLOATS (3 * PT_GUIDE_PARAMS)
+PT_API int pt_guide_get_state(pt_context* ctx, float* state, int64_t* step);
+PT_API int pt_guide_set_state(pt_context* ctx, const float* state, int64_t step);
 /* Scene box of the position encoding: x01 = (p - bmin) * binv. */
 PT_API int pt_guide_bounds(pt_context* ctx, float bmin[3], float binv[3]);
 /* Raw network outputs (PT_GUIDE_OUTPUTS per sample) of n samples. */

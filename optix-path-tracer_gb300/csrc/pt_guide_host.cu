@@ -313,6 +313,42 @@ PT_API int pt_guide_set_params(pt_context* ctx, const float* params) {
   return upload_params(ctx, w);
 }
 
+PT_API int pt_guide_get_state(pt_context* ctx, float* state, int64_t* step) {
+  if (!ctx || !state || !step) return PT_EINVAL;
+  if (!ctx->guide.ready) return gfail(ctx, PT_ESTATE, "guide not initialised (pt_guide_init)");
+  GK(cudaSetDevice(ctx->device));
+  GuideState& G = ctx->guide;
+  GK(cudaStreamSynchronize(ctx->stream));
+  GK(cudaMemcpy(state, G.w32.p, PTG_PARAMS * 4, cudaMemcpyDeviceToHost));
+  GK(cudaMemcpy(state + PTG_PARAMS, G.m.p, PTG_PARAMS * 4, cudaMemcpyDeviceToHost));
+  GK(cudaMemcpy(state + 2 * PTG_PARAMS, G.v.p, PTG_PARAMS * 4, cudaMemcpyDeviceToHost));
+  *step = G.step;
+  return PT_OK;
+}
+
+PT_API int pt_guide_set_state(pt_context* ctx, const float* state, int64_t step) {
+  if (!ctx || !state || step < 0 || step > 0x7fffffff) return PT_EINVAL;
+  GK(cudaSetDevice(ctx->device));
+  int rc = guide_prepare(ctx);
+  if (rc) return rc;
+  for (int p = 0; p < 3 * PTG_PARAMS; p++)
+    if (!std::isfinite(state[p]) || (p >= 2 * PTG_PARAMS && state[p] < 0.f))
+      return gfail(ctx, PT_EINVAL, "guide state: finite values, second moments >= 0");
+  std::vector<float> w(state, state + PTG_PARAMS);
+  for (int p = 0; p < PTG_PARAMS; p++)
+    if (!param_used(p)) w[p] = 0.f;
+  rc = upload_params(ctx, w);  // weights and their BF16 copy; moments zeroed
+  if (rc) return rc;
+  GuideState& G = ctx->guide;
+  GK(cudaMemcpyAsync(G.m.p, state + PTG_PARAMS, PTG_PARAMS * 4, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  GK(cudaMemcpyAsync(G.v.p, state + 2 * PTG_PARAMS, PTG_PARAMS * 4, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  GK(cudaStreamSynchronize(ctx->stream));
+  G.step = (int)step;
+  return PT_OK;
+}
+
 PT_API int pt_guide_bounds(pt_context* ctx, float bmin[3], float binv[3]) {
   if (!ctx || !bmin || !binv) return PT_EINVAL;
   GK(cudaSetDevice(ctx->device));

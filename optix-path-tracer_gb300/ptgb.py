@@ -124,6 +124,8 @@ SIGNATURES = {
     "pt_guide_set_training": [_P, ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int],
     "pt_guide_get_params": [_P, _P],
     "pt_guide_set_params": [_P, _P],
+    "pt_guide_get_state": [_P, _P, ctypes.POINTER(ctypes.c_int64)],
+    "pt_guide_set_state": [_P, _P, ctypes.c_int64],
     "pt_guide_bounds": [_P, _P, _P],
     "pt_guide_eval": [_P, _P, ctypes.c_int, _P],
     "pt_guide_gradient": [_P, _P, ctypes.c_int, _P, _P],
@@ -554,6 +556,17 @@ class GpuRenderer:
     def guide_set_params(self, w):
         w = np.ascontiguousarray(w, dtype=np.float32)
         self._c(self.lib.pt_guide_set_params(self.ctx, _ptr(w)))
+
+    def guide_state(self):
+        """(weights + Adam moments as 3 x GUIDE_PARAMS floats, Adam step)"""
+        out = np.zeros(3 * self.GUIDE_PARAMS, np.float32)
+        step = ctypes.c_int64()
+        self._c(self.lib.pt_guide_get_state(self.ctx, _ptr(out), ctypes.byref(step)))
+        return out, step.value
+
+    def guide_set_state(self, state, step):
+        s = np.ascontiguousarray(state, dtype=np.float32)
+        self._c(self.lib.pt_guide_set_state(self.ctx, _ptr(s), int(step)))
 
     def guide_bounds(self):
         bmin = np.zeros(3, np.float32)

@@ -233,6 +233,30 @@ def test_guided_render_is_deterministic(ptgb_mod):
     assert np.array_equal(out[0], out[1])
 
 
+def test_guide_checkpoint_resume(ptgb_mod):
+    """A guided render checkpointed after 3 frames (weights, Adam moments,
+    step) and resumed in a fresh context renders frames 3..5 exactly as the
+    uninterrupted render does."""
+    P = ptgb_mod.GpuRenderer.params
+    s = _box(ptgb_mod, 32)
+    full = ptgb_mod.GpuRenderer(s)
+    full.guide_init(9)
+    frames = [full.render64(P(32, 32, 1, frame0=f, mode=1, guide=1)) for f in range(6)]
+    full.close()
+    first = ptgb_mod.GpuRenderer(s)
+    first.guide_init(9)
+    for f in range(3):
+        first.render64(P(32, 32, 1, frame0=f, mode=1, guide=1))
+    state, step = first.guide_state()
+    first.close()
+    assert step == 3 * 8  # eight Adam steps per frame
+    resumed = ptgb_mod.GpuRenderer(s)
+    resumed.guide_set_state(state, step)
+    for f in range(3, 6):
+        assert np.array_equal(resumed.render64(P(32, 32, 1, frame0=f, mode=1, guide=1)), frames[f])
+    resumed.close()
+
+
 def test_guide_argument_checks(ptgb_mod):
     P = ptgb_mod.GpuRenderer.params
     g = ptgb_mod.GpuRenderer(_box(ptgb_mod, 16))

@@ -372,9 +372,30 @@ class Mesh : public Hitable {
        std::vector<BRDF*> tri_materials = {})
       : Hitable(m), verts(std::move(verts)), idx(std::move(idx)), normals(std::move(normals)),
         uvs(std::move(uvs)), tri_materials(std::move(tri_materials)) {}
+  // Mesh(fileName[, assetsFolder][, givenMaterial], RTX) (mesh.hpp:22-45): an
+  // OBJ file read by pt_obj_load; without a material, one Lambertian per MTL
+  // material (its ambient colour).  The RTX flag has no meaning here.
+  Mesh(std::string fileName, bool /*RTX*/ = false) : Hitable(nullptr), file(std::move(fileName)) {}
+  Mesh(std::string fileName, std::string assetsFolder, bool /*RTX*/ = false)
+      : Hitable(nullptr), file(std::move(fileName)), folder(std::move(assetsFolder)) {}
+  Mesh(std::string fileName, BRDF* givenMaterial, bool /*RTX*/ = false)
+      : Hitable(givenMaterial), file(std::move(fileName)) {}
+  Mesh(std::string fileName, std::string assetsFolder, BRDF* givenMaterial, bool /*RTX*/ = false)
+      : Hitable(givenMaterial), file(std::move(fileName)), folder(std::move(assetsFolder)) {}
   void add(Context& ctx, const std::vector<TransformParameter>& ts) override {
     float x[12];
     bool has = compose(ts, x);
+    if (!file.empty()) {
+      pt_obj* obj = nullptr;
+      if (pt_obj_load((folder + file).c_str(), &obj) != PT_OK)
+        throw Error(PT_EINVAL, std::string("Mesh: ") + pt_io_last_error());
+      uint32_t mid = material ? material->assignTo(ctx) : PT_OBJ_MTL;
+      int rc = pt_add_obj(ctx.get(), obj, mid, has ? x : nullptr, nullptr);
+      pt_obj_free(obj);
+      ctx->check(rc, "Mesh");
+      ctx->dirty = true;
+      return;
+    }
     std::vector<uint32_t> mpt;
     for (BRDF* b : tri_materials) mpt.push_back(b->assignTo(ctx));
     uint32_t mid = material ? material->assignTo(ctx) : 0;
@@ -389,6 +410,7 @@ class Mesh : public Hitable {
   std::vector<uint32_t> idx;
   std::vector<float> normals, uvs;
   std::vector<BRDF*> tri_materials;
+  std::string file, folder;
 };
 
 class Hitable_List {  // host_includes/hitables.hpp:455-528
@@ -534,6 +556,22 @@ inline std::vector<uint8_t> resolveDisplay(Context& ctx, const float* acc, int W
   ctx->check(pt_resolve_display(ctx.get(), acc, W, H, frame, out.data(), nullptr),
              "resolveDisplay");
   return out;
+}
+
+// Save_PNG / Save_HDR (image_save.hpp:7-73) of an accumulation buffer of
+// w*h RGBA float sums over spp frames; ".png" / ".hdr" is appended to the
+// name as the reference does.
+inline void Save_PNG(const std::string& fileName, int w, int h, const std::vector<float>& acc,
+                     int spp) {
+  if (acc.size() < (size_t)w * h * 4) throw Error(PT_EINVAL, "Save_PNG: buffer too small");
+  if (pt_png_save((fileName + ".png").c_str(), w, h, acc.data(), spp) != PT_OK)
+    throw Error(PT_EINVAL, std::string("Save_PNG: ") + pt_io_last_error());
+}
+inline void Save_HDR(const std::string& fileName, int w, int h, const std::vector<float>& acc,
+                     int spp) {
+  if (acc.size() < (size_t)w * h * 4) throw Error(PT_EINVAL, "Save_HDR: buffer too small");
+  if (pt_hdr_save((fileName + ".hdr").c_str(), w, h, acc.data(), spp) != PT_OK)
+    throw Error(PT_EINVAL, std::string("Save_HDR: ") + pt_io_last_error());
 }
 
 }  // namespace pt

@@ -66,3 +66,28 @@ def test_cornell_example_matches_harness(ptgb_mod, tmp_path):
     ref = acc[..., :3]
     err = np.abs(img - ref) / np.maximum(np.maximum(np.abs(img), np.abs(ref)), 1e-3)
     assert err.max() <= 1e-4
+
+
+def test_facade_save_png_hdr(ptgb_mod, tmp_path):
+    """Save_PNG / Save_HDR of the facade write the same files as the ABI calls
+    (no device work: runs without a GPU)."""
+    src = tmp_path / "s.cpp"
+    src.write_text(r'''
+#include "pt_scene.hpp"
+int main(int argc, char** argv) {
+  int w = 5, h = 3;
+  std::vector<float> acc(w * h * 4);
+  for (size_t i = 0; i < acc.size(); i++) acc[i] = 0.37f * (float)(i % 11);
+  pt::Save_PNG(argv[1], w, h, acc, 4);
+  pt::Save_HDR(argv[1], w, h, acc, 4);
+  return 0;
+}''')
+    exe = tmp_path / "s"
+    subprocess.run(["g++", "-std=c++14", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe), "-L", PKG, "-lpt", "-Wl,-rpath," + PKG], check=True)
+    subprocess.run([str(exe), str(tmp_path / "cpp")], check=True)
+    acc = (np.float32(0.37) * (np.arange(5 * 3 * 4) % 11).astype(np.float32)).reshape(3, 5, 4)
+    ptgb_mod.png_save(tmp_path / "py.png", acc, 4)
+    ptgb_mod.hdr_save(tmp_path / "py.hdr", acc, 4)
+    assert (tmp_path / "cpp.png").read_bytes() == (tmp_path / "py.png").read_bytes()
+    assert (tmp_path / "cpp.hdr").read_bytes() == (tmp_path / "py.hdr").read_bytes()

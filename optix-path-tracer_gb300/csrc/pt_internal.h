@@ -9,7 +9,9 @@
 #include <stdint.h>
 #include "pt_types.h"
 
+#ifndef PT_TRACE_BLOCK
 #define PT_TRACE_BLOCK 128       /* default threads per trace block */
+#endif
 #define PT_TRACE_MAXTHREADS 256  /* largest trace block the kernels are compiled for */
 #ifndef PT_TRACE_MINBLOCKS
 #define PT_TRACE_MINBLOCKS 3     /* of 256 threads: <= 80 registers per thread, no spills */

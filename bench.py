@@ -75,6 +75,27 @@ def dist_env():
     return rank, world, local
 
 
+def rank_frame0(rank, frames_per_rank):
+    """Replicas: rank r renders frames [r*F, (r+1)*F) of every image (weak
+    scaling, no data-path collective)."""
+    return rank * frames_per_rank
+
+
+def reduce_over_ranks(dev_s, wall, paths, rays, device):
+    """(slowest rank's device time, slowest wall time, all ranks' paths,
+    all ranks' rays) over the process group; the inputs when it has one rank."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized() or dist.get_world_size() == 1:
+        return dev_s, wall, float(paths), float(rays)
+    t = torch.tensor([dev_s, wall, float(paths), float(rays)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(mx[1]), float(sm[2]), float(sm[3])
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -222,7 +243,7 @@ def run_ours(args, wl):
     gen, w, h, spp, kw, desc = wl
     scene = getattr(ptgb, gen)(w, h)
     # per-rank frames: rank r renders frames [r*spp, (r+1)*spp): weak scaling
-    frame0 = rank * spp
+    frame0 = rank_frame0(rank, spp)
     rend = ptgb.GpuRenderer(scene, device=local, timing=True)
     prm = ptgb.GpuRenderer.params(w, h, spp, frame0=frame0, **kw)
     acc = torch.zeros((h, w, 4), dtype=torch.float32, device=f"cuda:{local}")
@@ -258,16 +279,8 @@ def run_ours(args, wl):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     dev_s = dev_ms / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s, wall, float(paths), float(ext + shadow)], device=f"cuda:{local}")
-        mx = t.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        sm = t.clone()
-        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
-        dev_s, wall = float(mx[0]), float(mx[1])
-        tot_paths, tot_rays = float(sm[2]), float(sm[3])
-    else:
-        tot_paths, tot_rays = float(paths), float(ext + shadow)
+    dev_s, wall, tot_paths, tot_rays = reduce_over_ranks(dev_s, wall, paths, ext + shadow,
+                                                         f"cuda:{local}")
     value = tot_paths / dev_s
 
     # ---- end to end through the C ABI with host buffers: upload + BVH build
@@ -372,7 +385,7 @@ def run_batch(args):
     kw = BATCH_KW
     rends = [ptgb.GpuRenderer(sc, device=local) for sc, *_ in items]
     # replicas: rank r renders frames [r*spp, (r+1)*spp) of every scene
-    params = [ptgb.GpuRenderer.params(res, res, spp, frame0=rank * spp, **kw)
+    params = [ptgb.GpuRenderer.params(res, res, spp, frame0=rank_frame0(rank, spp), **kw)
               for _, res, spp, _ in items]
     npix = [res * res for _, res, _, _ in items]
     acc = torch.zeros((sum(npix), 4), dtype=torch.float32, device=f"cuda:{local}")
@@ -411,16 +424,8 @@ def run_batch(args):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     dev_s = dev_ms / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s, wall, float(paths), float(rays)], device=f"cuda:{local}")
-        mx = t.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        sm = t.clone()
-        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
-        dev_s, wall = float(mx[0]), float(mx[1])
-        tot_paths, tot_rays = float(sm[2]), float(sm[3])
-    else:
-        tot_paths, tot_rays = float(paths), float(rays)
+    dev_s, wall, tot_paths, tot_rays = reduce_over_ranks(dev_s, wall, paths, rays,
+                                                         f"cuda:{local}")
     value = tot_paths / dev_s
 
     # ---- the same scenes one at a time (same batch object and tune)

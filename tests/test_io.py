@@ -185,3 +185,30 @@ def test_png_large_image_spans_blocks(ptgb_mod, tmp_path):
     ptgb_mod.png_save(tmp_path / "big.png", acc, 1)
     px = png_pixels((tmp_path / "big.png").read_bytes())
     assert px.shape == (200, 150, 3) and np.all(px == int(255.99 * 0.5))
+
+
+def test_hdr_old_style_repeats(ptgb_mod, tmp_path):
+    # flat pixels with (1, 1, 1, n) markers repeating the previous pixel
+    # (consecutive markers shift the count by 8 bits)
+    a = [10, 20, 30, 130]
+    b = [200, 100, 50, 127]
+    body = bytes(a) + bytes([1, 1, 1, 3]) + bytes(b) + bytes([1, 1, 1, 1]) + bytes([1, 1, 1, 0])
+    # row of 1 + 3 + 1 + (1 + (0 << 8)) = 6 pixels
+    (tmp_path / "o.hdr").write_bytes(hdr_header(6, 1) + body)
+    img = ptgb_mod.hdr_load(tmp_path / "o.hdr")
+    q = np.array([a, a, a, a, b, b], np.uint8)[None]
+    assert np.array_equal(img[..., :3], rgbe_decode(q).astype(np.float32))
+
+
+def test_obj_crlf_and_convex_fan(ptgb_mod, tmp_path):
+    # CRLF line ends, a convex pentagon: ear clipping gives the fan from vertex 0
+    ang = np.linspace(0, 2 * np.pi, 6)[:5]
+    text = "".join(f"v {np.cos(t):.6f} {np.sin(t):.6f} 0\r\n" for t in ang) + "f 1 2 3 4 5\r\n"
+    m = ptgb_mod.ObjMesh(write(tmp_path / "p.obj", text))
+    assert m.n_tris == 3
+    v = m.verts
+    first = v[:, 0, :]
+    assert np.allclose(first, first[0])  # every triangle starts at vertex 0
+    assert np.allclose(v[0, 1:], [[np.cos(ang[1]), np.sin(ang[1]), 0], [np.cos(ang[2]), np.sin(ang[2]), 0]],
+                       atol=1e-6)
+    m.close()

@@ -7,7 +7,7 @@
  * RGBE encoding, the PNG specification with stored deflate blocks).
  */
 #include <algorithm>
-#include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -54,11 +54,15 @@ std::vector<std::string> split_ws(const std::string& line) {
   return t;
 }
 
+// Locale-independent decimal parse (the host program's locale may use a
+// decimal comma): read as double, rounded once to float.
 bool to_float(const std::string& s, float& v) {
-  char* end = nullptr;
-  errno = 0;
-  double d = strtod(s.c_str(), &end);
-  if (end == s.c_str()) return false;
+  const char* b = s.c_str();
+  const char* e = b + s.size();
+  if (b != e && *b == '+') b++;
+  double d = 0.0;
+  auto r = std::from_chars(b, e, d);
+  if (r.ec != std::errc() || r.ptr == b) return false;
   v = (float)d;
   return true;
 }
@@ -203,7 +207,7 @@ bool load_mtl(const std::string& path, std::vector<Mtl>& mats, std::map<std::str
   std::string text;
   if (!read_file(path.c_str(), text)) return false;
   size_t pos = 0;
-  Mtl* cur = nullptr;
+  int cur = -1;  // index of the material being read
   while (pos < text.size()) {
     size_t e = text.find('\n', pos);
     if (e == std::string::npos) e = text.size();
@@ -216,19 +220,19 @@ bool load_mtl(const std::string& path, std::vector<Mtl>& mats, std::map<std::str
     if (t[0] == "newmtl" && t.size() >= 2) {
       auto it = index.find(t[1]);
       if (it == index.end()) {
-        index[t[1]] = (int)mats.size();
+        cur = (int)mats.size();
+        index[t[1]] = cur;
         mats.push_back(Mtl());
         mats.back().name = t[1];
-        cur = &mats.back();
       } else {
-        cur = &mats[it->second];
+        cur = it->second;
       }
-    } else if (cur && (t[0] == "Ka" || t[0] == "Kd") && t.size() >= 4) {
-      float* d = t[0] == "Ka" ? cur->ka : cur->kd;
+    } else if (cur >= 0 && (t[0] == "Ka" || t[0] == "Kd") && t.size() >= 4) {
+      float* d = t[0] == "Ka" ? mats[cur].ka : mats[cur].kd;
       for (int a = 0; a < 3; a++)
         if (!to_float(t[1 + a], d[a])) d[a] = 0.f;
-    } else if (cur && t[0] == "map_Kd" && t.size() >= 2) {
-      cur->map_kd = t.back();
+    } else if (cur >= 0 && t[0] == "map_Kd" && t.size() >= 2) {
+      mats[cur].map_kd = t.back();
     }
   }
   return true;

@@ -1,9 +1,14 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 path tracer on the random-spheres workload (the
-second benchmark configuration: 1920x1080, 128 spp, 488 spheres, max depth
-50, Russian roulette after depth 10, seeded synthetic scene).
+"""Benchmark of the GB300 path tracer.  The default workload is the
+2,097,152-triangle heightfield (the third benchmark configuration, the one
+the 1.5 G rays/s target is stated on): 1920x1080, 256 spp, fBm terrain with
+Torrance-Sparrow / Ashikhmin-Shirley / Oren-Nayar tiles, a 2048x1024 HDR sky
+importance-sampled through its 2D CDF, consistent mode (NEE + MIS), max depth
+50, Russian roulette after depth 10, seeded synthetic scene.
+`--workload spheres` is the random-spheres configuration (1920x1080, 128 spp,
+488 spheres, reference mode).
 
-One step = one full render of the workload (all 128 frames) through the C
+One step = one full render of the workload (all frames) through the C
 ABI.  Prints one JSON line (rank 0).  `--impl reference` times the CPU
 restatement of the reference's device programs (the reference itself needs
 the OptiX 6 SDK and an OpenGL window, neither of which exists here) on a
@@ -157,6 +162,29 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+SMS, SCHEDULERS_PER_SM = 152, 4
+
+
+def issue_fraction(tr, ext, shadow, trace_ms, sm_mhz):
+    """The trace kernels are bound by instruction issue, not by HBM (their
+    BVH and records are served from L1/L2).  Warp instructions per ray come
+    from a committed ncu capture (smsp__inst_executed.sum / rays of the
+    captured launches, extension and occlusion separately); the rate is the
+    warp instructions this run's trace launches must have issued over their
+    device time, against 152 SMs x 4 schedulers x one instruction per clock
+    at the sampled SM clock (the maximum clock when no sample exists)."""
+    i_ext, i_occ = tr.get("warp_inst_per_ext_ray"), tr.get("warp_inst_per_shadow_ray")
+    if not i_ext or not i_occ:
+        return None
+    mhz = sm_mhz or 2070.0
+    inst = ext * i_ext + shadow * i_occ
+    achieved = inst / (trace_ms / 1e3)
+    peak = SMS * SCHEDULERS_PER_SM * mhz * 1e6
+    return {"warp_inst_per_s": achieved, "peak_warp_inst_per_s": peak, "frac": achieved / peak,
+            "sm_mhz": mhz, "warp_inst_per_ext_ray": i_ext, "warp_inst_per_shadow_ray": i_occ,
+            "source": tr.get("_inst_source", "committed ncu capture (profiles/)")}
 
 
 def cpu_sample(scene, w, h, spp, kw, target_s, threads, max_stride=None):
@@ -314,14 +342,18 @@ def run_ours(args, wl):
     trace_launches = 2 * iters
     achieved = (ext + shadow) * b_ray / (trace_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = None
+    traffic, issue = None, None
     try:
         with open(PROFILE_TRAFFIC) as f:
             tr = json.load(f).get(args.workload)
         if tr:
             traffic = tr["dram_bytes_per_ray"] * (ext + shadow) / trace_launches
+            issue = issue_fraction(tr, ext, shadow, trace_ms, None)
     except (OSError, ValueError, KeyError):
         pass
+
+    if issue is not None and clk:
+        issue = issue_fraction(tr, ext, shadow, trace_ms, clk.get("sm_mhz"))
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -357,7 +389,8 @@ def run_ours(args, wl):
                          "bytes_per_ray": b_ray, "nodes_per_ray": n_node,
                          "prims_per_ray": n_prim,
                          "avg_launch_ms": trace_ms / trace_launches,
-                         "rays_per_launch": (ext + shadow) / trace_launches},
+                         "rays_per_launch": (ext + shadow) / trace_launches,
+                         "issue": issue},
             "stage_ms_per_step": {k: v / args.steps for k, v in
                                   zip(["generate", "trace", "shade", "shadow_trace", "finish"],
                                       stage)},
@@ -659,7 +692,7 @@ def main():
                     help="timed steps (default 5; 2 for the batch workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spheres", choices=sorted(WORKLOADS) + ["batch", "guide"])
+    ap.add_argument("--workload", default="heightfield", choices=sorted(WORKLOADS) + ["batch", "guide"])
     ap.add_argument("--ref-spp", type=int, default=4096,
                     help="guide workload: spp of the FP64 plain reference")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

@@ -988,3 +988,46 @@ def material_zoo(width=128, height=96, cells=12):
     s.rect(-3, 3, 0, 2, -2.0, False, PT_Z_AXIS, on)
     s.set_camera((0.0, 1.6, 4.5), (0.0, 0.3, 0.0), (0, 1, 0), 45.0, width / height, 0.05, 4.5)
     return s
+
+
+# ------------------------------------------------------------ headless CLI
+SCENES = {"cornell": cornell_c1, "cornell_reference": cornell_reference,
+          "spheres": random_spheres, "heightfield": heightfield_scene,
+          "guide_box": guide_box_scene, "zoo": material_zoo}
+
+
+def main(argv=None):
+    """Headless render (the reference's GUI launch loop, main.cpp:174-354,
+    without a window): builds one of the synthetic scenes, renders `spp`
+    frames through the C ABI, prints the render statistics as one JSON line
+    and optionally writes the image (Save_PNG / Save_HDR conventions)."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--scene", default="cornell", choices=sorted(SCENES))
+    ap.add_argument("--width", type=int, default=512)
+    ap.add_argument("--height", type=int, default=512)
+    ap.add_argument("--spp", type=int, default=16)
+    ap.add_argument("--frame0", type=int, default=0)
+    ap.add_argument("--mode", type=int, default=0, help="0 reference, 1 consistent (NEE + MIS)")
+    ap.add_argument("--max-depth", type=int, default=50)
+    ap.add_argument("--rr-depth", type=int, default=10)
+    ap.add_argument("--builder", type=int, default=0, help="0 auto, 1 host SAH, 2 GPU LBVH")
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--out", default="", help="image path (.png or .hdr)")
+    a = ap.parse_args(argv)
+    scene = SCENES[a.scene](a.width, a.height)
+    r = GpuRenderer(scene, device=a.device, builder=a.builder)
+    prm = GpuRenderer.params(a.width, a.height, a.spp, frame0=a.frame0, max_depth=a.max_depth,
+                             rr_depth=a.rr_depth, mode=a.mode)
+    acc = r.render(prm)
+    st = r.stats()
+    st.update(scene=a.scene, width=a.width, height=a.height, spp=a.spp, mode=a.mode)
+    if a.out:
+        (hdr_save if a.out.lower().endswith(".hdr") else png_save)(a.out, acc, a.spp)
+    r.close()
+    print(json.dumps(st))
+
+
+if __name__ == "__main__":
+    main()

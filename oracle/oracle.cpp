@@ -39,10 +39,17 @@
  *   - shadow rays report the closest hit in (1e-3, tmax); the point is
  *     unoccluded iff that hit is a diffuse light and dot(N, Wi) > 0;
  *   - a HitRecord is computed from the object-space ray and mapped to world
- *     space once (the reference maps its world-space hit point again);
+ *     space once, as the reference's HitRecord programs do with the ray
+ *     OptiX gives them; Wo is taken from the world-space ray (the
+ *     reference's comes from the object-space one);
  *   - a pdf the reference leaves uninitialised starts at 0.
  * Arithmetic: compiled with -ffp-contract=off, elementary functions from
  * ptmath.h, so every float operation rounds exactly as on the GPU.
+ *
+ * Pinned: oracle/refhost compiles the reference's programs/ unmodified over
+ * an OptiX stand-in (oracle/_ref/libref.so), and tests/test_ref_pin.py finds
+ * this restatement bit-identical to them, function by function and path by
+ * path.
  */
 #include <stdint.h>
 #include <stdlib.h>
@@ -2137,4 +2144,129 @@ extern "C" void or_bsdf_c_batch(int type, const float* c0, const float* c1, floa
     f[3 * k + 2] = r.z;
     pdf[k] = bsdf_pdf_c(m, a, b);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Function-level entry points for the pins against the reference's own
+// programs (oracle/refhost, tests/test_ref_pin.py).  Reference mode.
+extern "C" void or_lcg_stream(uint32_t seed, int n, uint32_t* out) {
+  for (int i = 0; i < n; i++) out[i] = lcg(seed);
+}
+
+// kind 0 random_in_unit_disk, 1 random_in_unit_sphere, 2 random_on_unit_sphere
+extern "C" void or_sampling(int kind, uint32_t seed, int n, float* out) {
+  for (int i = 0; i < n; i++) {
+    V3 v = kind == 0 ? random_in_unit_disk(seed)
+                     : (kind == 1 ? random_in_unit_sphere(seed) : random_on_unit_sphere(seed));
+    out[3 * i] = v.x;
+    out[3 * i + 1] = v.y;
+    out[3 * i + 2] = v.z;
+  }
+}
+
+extern "C" void or_brdf_sample(int type, const float* c0, const float* c1, float p0, float p1,
+                               int n, const float* Wo, const float* N, uint32_t* seeds,
+                               float* Wi) {
+  Scene tmp;
+  const Material m = tmp.mats[or_add_material(&tmp, type, c0, c1, p0, p1)];
+  for (int i = 0; i < n; i++) {
+    V3 w = brdf_sample(m, v3(Wo[3 * i], Wo[3 * i + 1], Wo[3 * i + 2]),
+                       v3(N[3 * i], N[3 * i + 1], N[3 * i + 2]), seeds[i]);
+    Wi[3 * i] = w.x;
+    Wi[3 * i + 1] = w.y;
+    Wi[3 * i + 2] = w.z;
+  }
+}
+
+extern "C" void or_brdf_eval(int type, const float* c0, const float* c1, float p0, float p1,
+                             int n, const float* Wo, const float* Wi, const float* N, float* f,
+                             float* pdf) {
+  Scene tmp;
+  const Material m = tmp.mats[or_add_material(&tmp, type, c0, c1, p0, p1)];
+  for (int i = 0; i < n; i++) {
+    float pd = 0.f;
+    V3 v = brdf_eval(m, v3(Wo[3 * i], Wo[3 * i + 1], Wo[3 * i + 2]),
+                     v3(Wi[3 * i], Wi[3 * i + 1], Wi[3 * i + 2]),
+                     v3(N[3 * i], N[3 * i + 1], N[3 * i + 2]), pd);
+    f[3 * i] = v.x;
+    f[3 * i + 1] = v.y;
+    f[3 * i + 2] = v.z;
+    pdf[i] = pd;
+  }
+}
+
+// The same helper cases as the reference harness's ref_helper: inputs of 8
+// floats, outputs of 4, per case.
+extern "C" void or_helper(int fn, int n, const float* in, float* out) {
+  for (int i = 0; i < n; i++) {
+    const float* a = in + 8 * i;
+    float* o = out + 4 * i;
+    V3 A = v3(a[0], a[1], a[2]), B = v3(a[3], a[4], a[5]);
+    switch (fn) {
+      case 0: o[0] = schlick(a[0], a[1]); break;
+      case 1: {
+        V3 r = v3(0.f);
+        bool ok = Refract(A, B, a[6], r);
+        o[0] = r.x; o[1] = r.y; o[2] = r.z;
+        o[3] = ok ? 1.f : 0.f;
+        break;
+      }
+      case 2: {
+        V3 h = GGX_Sample(A, a[3], a[4], a[5], a[6]);
+        o[0] = h.x; o[1] = h.y; o[2] = h.z;
+        break;
+      }
+      case 3:
+        o[0] = GGX_D(A, a[6], a[7]);
+        o[1] = GGX_G(A, B, a[6], a[7]);
+        o[2] = GGX_PDF(A, a[6], a[7]);
+        break;
+      case 4: {
+        float phi, theta;
+        Sample_Quadrant(a[0], a[1], a[2], a[3], phi, theta);
+        o[0] = phi;
+        o[1] = theta;
+        break;
+      }
+      case 5:
+        o[0] = AbsCosTheta(A);
+        o[1] = SinTheta(A);
+        o[2] = CosPhi(A);
+        o[3] = SinPhi(A);
+        break;
+    }
+  }
+}
+
+// Light k of a committed scene: n samples from (P, N, seed) and the pdf of
+// each sampled direction.
+extern "C" void or_light(void* sp, int k, int n, const float* P, uint32_t* seeds, float* Wi,
+                         float* pdf) {
+  Scene& s = *(Scene*)sp;
+  const Light& L = s.lights[k];
+  for (int i = 0; i < n; i++) {
+    V3 p = v3(P[3 * i], P[3 * i + 1], P[3 * i + 2]);
+    V3 w = light_sample(L, p, seeds[i]);
+    Wi[3 * i] = w.x;
+    Wi[3 * i + 1] = w.y;
+    Wi[3 * i + 2] = w.z;
+    pdf[i] = light_pdf(L, p, w);
+  }
+}
+
+// One ray: closest primitive (-1 if none), t and its HitRecord as P, shading
+// normal, u, v, geometric normal, Wo, material (17 floats).
+extern "C" int or_probe(void* sp, const float* o, const float* d, float tmin, float* t,
+                        float* rec) {
+  Scene& s = *(Scene*)sp;
+  Ray r{v3(o[0], o[1], o[2]), v3(d[0], d[1], d[2]), tmin, RAY_TMAX};
+  Hit h = trace(s, r, nullptr);
+  *t = h.prim >= 0 ? h.t : 0.f;
+  if (h.prim < 0 || !rec) return h.prim;
+  HitRecord e = hit_record(s, s.prims[h.prim], r, h.t, h.u, h.v);
+  float v[17] = {e.P.x, e.P.y, e.P.z, e.shading_normal.x, e.shading_normal.y,
+                 e.shading_normal.z, e.u, e.v, e.geometric_normal.x, e.geometric_normal.y,
+                 e.geometric_normal.z, e.Wo.x, e.Wo.y, e.Wo.z, (float)e.index, 0.f, 0.f};
+  memcpy(rec, v, sizeof(v));
+  return h.prim;
 }

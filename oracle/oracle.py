@@ -61,6 +61,15 @@ def load():
     L.or_env_sample.argtypes = [_P, _P, ctypes.c_int, _P, _P]
     L.or_bsdf_c_batch.argtypes = [ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float, _P,
                                   ctypes.c_int, _P, _P, _P]
+    L.or_lcg_stream.argtypes = [ctypes.c_uint32, ctypes.c_int, _P]
+    L.or_sampling.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_int, _P]
+    L.or_brdf_sample.argtypes = [ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_int, _P, _P, _P, _P]
+    L.or_brdf_eval.argtypes = [ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_float,
+                               ctypes.c_int, _P, _P, _P, _P, _P]
+    L.or_helper.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P]
+    L.or_light.argtypes = [_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P]
+    L.or_probe.argtypes = [_P, _P, _P, ctypes.c_float, _P, _P]
     _lib = L
     return L
 
@@ -71,6 +80,51 @@ def _f(v):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(_P)
+
+
+def replay(L, prefix, h, s):
+    """Replays a ptgb.Scene (materials, primitives, meshes, lights, miss
+    program, camera, in call order) into a scene of the CPU oracle
+    (prefix "or_") or of the reference-program harness (prefix "rh_"): both
+    libraries take the same calls."""
+    fn = lambda name: getattr(L, prefix + name)
+    for kind, c0, c1, p0, p1 in s.materials:
+        c0a = _f(c0)
+        c1a = _f(c1) if c1 is not None else None
+        fn("add_material")(h, kind, _p(c0a), _p(c1a), p0, p1)
+    for it in s.items:
+        if it[0] == "sphere":
+            _, cen, r, m, xf = it
+            fn("add_prim")(h, 1, _p(_f(list(cen) + [r])), 0, 0, m, _p(xf))
+        elif it[0] == "rect":
+            _, v5, flip, axis, m, xf = it
+            fn("add_prim")(h, 2, _p(_f(v5)), axis, flip, m, _p(xf))
+        elif it[0] == "box":
+            _, p0, p1, m, xf = it
+            fn("add_prim")(h, 3, _p(_f(list(p0) + list(p1))), 0, 0, m, _p(xf))
+        else:
+            _, v, idx, m, mpt, nrm, uv, xf = it
+            mpt_i = None if mpt is None else np.ascontiguousarray(mpt, dtype=np.int32)
+            fn("add_mesh")(h, _p(v), len(v), _p(idx), len(idx), _p(mpt_i),
+                           m if m is not None else 0, _p(nrm), _p(uv), _p(xf))
+    for lt in s.lights:
+        if lt[0] == "rect":
+            _, v5, axis, e = lt
+            fn("add_light")(h, 0, _p(_f(v5)), axis, _p(_f(e)))
+        else:
+            _, cen, r, e = lt
+            fn("add_light")(h, 1, _p(_f(list(cen) + [r])), 0, _p(_f(e)))
+    ms = s.miss
+    if ms[0] == "gradient":
+        fn("set_miss")(h, 0, _p(_f(ms[1])), _p(_f(ms[2])), None, 0, 0, 1)
+    elif ms[0] == "constant":
+        fn("set_miss")(h, 1, _p(_f(ms[1])), None, None, 0, 0, 1)
+    else:
+        rgba = ms[1]
+        fn("set_miss")(h, ms[3], None, None, _p(rgba), rgba.shape[1], rgba.shape[0], ms[2])
+    cf, ca, cu, vfov, aspect, ap, fd, t0, t1 = s.camera
+    fn("set_camera")(h, _p(_f(cf)), _p(_f(ca)), _p(_f(cu)), vfov, aspect, ap, fd, t0, t1)
+    fn("commit")(h)
 
 
 class Oracle:
@@ -89,47 +143,7 @@ class Oracle:
             pass
 
     def load(self, s):
-        L, h = self.L, self.h
-        for kind, c0, c1, p0, p1 in s.materials:
-            c0a = _f(c0)
-            c1a = _f(c1) if c1 is not None else None
-            L.or_add_material(h, kind, _p(c0a), _p(c1a), p0, p1)
-        for it in s.items:
-            if it[0] == "sphere":
-                _, cen, r, m, xf = it
-                f = _f(list(cen) + [r])
-                L.or_add_prim(h, 1, _p(f), 0, 0, m, _p(xf))
-            elif it[0] == "rect":
-                _, v5, flip, axis, m, xf = it
-                f = _f(v5)
-                L.or_add_prim(h, 2, _p(f), axis, flip, m, _p(xf))
-            elif it[0] == "box":
-                _, p0, p1, m, xf = it
-                f = _f(list(p0) + list(p1))
-                L.or_add_prim(h, 3, _p(f), 0, 0, m, _p(xf))
-            else:
-                _, v, idx, m, mpt, nrm, uv, xf = it
-                mpt_i = None if mpt is None else np.ascontiguousarray(mpt, dtype=np.int32)
-                L.or_add_mesh(h, _p(v), len(v), _p(idx), len(idx), _p(mpt_i),
-                              m if m is not None else 0, _p(nrm), _p(uv), _p(xf))
-        for lt in s.lights:
-            if lt[0] == "rect":
-                _, v5, axis, e = lt
-                L.or_add_light(h, 0, _p(_f(v5)), axis, _p(_f(e)))
-            else:
-                _, cen, r, e = lt
-                L.or_add_light(h, 1, _p(_f(list(cen) + [r])), 0, _p(_f(e)))
-        ms = s.miss
-        if ms[0] == "gradient":
-            L.or_set_miss(h, 0, _p(_f(ms[1])), _p(_f(ms[2])), None, 0, 0, 1)
-        elif ms[0] == "constant":
-            L.or_set_miss(h, 1, _p(_f(ms[1])), None, None, 0, 0, 1)
-        else:
-            rgba = ms[1]
-            L.or_set_miss(h, ms[3], None, None, _p(rgba), rgba.shape[1], rgba.shape[0], ms[2])
-        cf, ca, cu, vfov, aspect, ap, fd, t0, t1 = s.camera
-        L.or_set_camera(h, _p(_f(cf)), _p(_f(ca)), _p(_f(cu)), vfov, aspect, ap, fd, t0, t1)
-        L.or_commit(h)
+        replay(self.L, "or_", self.h, s)
 
     def env_sample(self, u):
         u = np.ascontiguousarray(u, dtype=np.float32)

@@ -1,0 +1,16 @@
+// Wrapper of programs/materials/lambertian.cu (test infrastructure, see rtshim.h).
+#include "rtemu.h"
+#include "materials/lambertian.cu"
+#include "ref_common.h"
+
+REF_BIND_LIGHTS()
+
+extern "C" void ref_lambertian_hit(void* p_prd, const Ray* r, float t, int gi, float2 b,
+                             const int* tex, const float* p) {
+  (void)p;
+  bind_hitrecord(Get_HitRecord);
+  bind_texture(sample_texture, tex[0]);
+  bind_lights();
+
+  REF_RUN_CLOSEST_HIT(p_prd, r, t, gi, b);
+}

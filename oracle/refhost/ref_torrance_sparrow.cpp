@@ -1,0 +1,17 @@
+// Wrapper of programs/materials/torrance_sparrow.cu (test infrastructure, see rtshim.h).
+#include "rtemu.h"
+#include "materials/torrance_sparrow.cu"
+#include "ref_common.h"
+
+REF_BIND_LIGHTS()
+
+extern "C" void ref_torrance_sparrow_hit(void* p_prd, const Ray* r, float t, int gi, float2 b,
+                             const int* tex, const float* p) {
+  (void)p;
+  bind_hitrecord(Get_HitRecord);
+  bind_texture(sample_texture, tex[0]);
+  bind_lights();
+  nu = p[0];
+  nv = p[1];
+  REF_RUN_CLOSEST_HIT(p_prd, r, t, gi, b);
+}

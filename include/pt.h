@@ -291,6 +291,14 @@ PT_API int pt_guide_init(pt_context* ctx, uint64_t seed);
  * 4 bounces. */
 PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent,
                                  int max_bounces);
+/* Bound on each wait of the guide kernels for their tensor-core results, in
+ * mbarrier try_wait attempts (default PT_GUIDE_WAIT_DEFAULT = 2^24).  A wait
+ * that runs out makes the kernel stop, let its MMAs in flight finish, free
+ * its tensor memory and report PT_ETIMEOUT; the context stays usable.  0
+ * makes every wait run out at once: it exists to exercise that path (a
+ * working kernel never needs a small bound). */
+#define PT_GUIDE_WAIT_DEFAULT (1u << 24)
+PT_API int pt_guide_set_wait_limit(pt_context* ctx, uint32_t try_waits);
 PT_API int pt_guide_get_params(pt_context* ctx, float* params);
 PT_API int pt_guide_set_params(pt_context* ctx, const float* params);
 /* Checkpoint of the online training: FP32 weights, Adam first and second

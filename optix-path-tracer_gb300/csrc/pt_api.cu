@@ -7,6 +7,7 @@
  * builds the BVH8 at pt_commit and drives the wavefront kernels in
  * pt_render (the per-sample Context::launch of main.cpp:26-39,264).
  */
+#include <atomic>
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cfloat>
@@ -47,6 +48,9 @@ static int fail(pt_context* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
   return code;
 }
+
+static const char* const kOtherDevice =
+    "buffer is device memory of another GPU than the context's (pt_options.device)";
 
 static int cuda_fail(pt_context* ctx, cudaError_t e, const char* where) {
   return fail(ctx, PT_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
@@ -106,13 +110,15 @@ static bool finite3(const float* v) {
   return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
 }
 
-bool pth::is_device_ptr(const void* p) {
+int pth::device_ptr_kind(const void* p, int device) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return 0;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return 1;
+  if (a.type == cudaMemoryTypeDevice) return a.device == device ? 1 : -1;
+  return 0;
 }
 
 // World-space AABB of a primitive, padded so that rounding in the primitive
@@ -1015,7 +1021,9 @@ PT_API int pt_render(pt_context* ctx, const pt_render_params* params, float* acc
   CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
   reset_render_stats(ctx);
   size_t WH = (size_t)params->width * params->height;
-  bool dev = is_device_ptr(accum_rgba);
+  int kind = device_ptr_kind(accum_rgba, ctx->device);
+  if (kind < 0) return fail(ctx, PT_EINVAL, kOtherDevice);
+  bool dev = kind > 0;
   float4* d_acc = (float4*)accum_rgba;
   if (!dev) {
     CK(ctx->d_acc.ensure(WH));
@@ -1049,7 +1057,9 @@ PT_API int pt_render_accum64(pt_context* ctx, const pt_render_params* params,
   CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
   reset_render_stats(ctx);
   size_t WH = (size_t)params->width * params->height;
-  bool dev = is_device_ptr(accum_rgba);
+  int kind = device_ptr_kind(accum_rgba, ctx->device);
+  if (kind < 0) return fail(ctx, PT_EINVAL, kOtherDevice);
+  bool dev = kind > 0;
   double* d_acc = accum_rgba;
   if (!dev) {
     CK(ctx->d_acc64.ensure(4 * WH));
@@ -1091,7 +1101,9 @@ PT_API int pt_render_paths(pt_context* ctx, const pt_render_params* params, floa
   p.frame0 = params->frame0;
   rc = run_chunk(ctx, &p, p.frame0, 1);
   if (rc) return rc;
-  bool dev = is_device_ptr(out_rgb);
+  int kind = device_ptr_kind(out_rgb, ctx->device);
+  if (kind < 0) return fail(ctx, PT_EINVAL, kOtherDevice);
+  bool dev = kind > 0;
   float* d_out = out_rgb;
   if (!dev) {
     CK(ctx->d_tmp.ensure(3 * WH));
@@ -1142,7 +1154,9 @@ PT_API int pt_resolve_display(pt_context* ctx, const float* accum_rgba, int widt
   CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
   size_t WH = (size_t)width * height;
   const float4* d_acc = (const float4*)accum_rgba;
-  if (!is_device_ptr(accum_rgba)) {
+  int kind = device_ptr_kind(accum_rgba, ctx->device);
+  if (kind < 0) return fail(ctx, PT_EINVAL, kOtherDevice);
+  if (kind == 0) {
     CK(ctx->d_acc.ensure(WH));
     CK(cudaMemcpyAsync(ctx->d_acc.p, accum_rgba, WH * 16, cudaMemcpyHostToDevice, st));
     d_acc = ctx->d_acc.p;
@@ -1192,19 +1206,22 @@ constexpr size_t kNoAllocBytes =
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
-static void* g_noalloc_ptr[kMaxDevices];  // device address of the array, per device
+// device address of the array, per device; atomic because two host threads
+// may make their first call on one device at the same time (both resolve
+// the same address)
+static std::atomic<void*> g_noalloc_ptr[kMaxDevices];
 
 // Once per device, with that device current: the host-side name of the
 // array is a stand-in, not a device address, so kernels get this pointer.
 static int noalloc_setup(pt_context* ctx, unsigned char** out) {
   if (ctx->device < 0 || ctx->device >= kMaxDevices) return fail(ctx, PT_EINVAL, "device ordinal");
-  if (!g_noalloc_ptr[ctx->device]) {
-    void* p = nullptr;
+  void* p = g_noalloc_ptr[ctx->device].load(std::memory_order_acquire);
+  if (!p) {
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return cuda_fail(ctx, e, "cudaGetSymbolAddress(noalloc scratch)");
-    g_noalloc_ptr[ctx->device] = p;
+    g_noalloc_ptr[ctx->device].store(p, std::memory_order_release);
   }
-  *out = (unsigned char*)g_noalloc_ptr[ctx->device];
+  *out = (unsigned char*)p;
   return PT_OK;
 }
 
@@ -1236,8 +1253,9 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
     return fail(ctx, PT_EINVAL,
                 "pt_render_noalloc: image has " + std::to_string(WH) + " pixels, its static "
                 "scratch holds at most " + std::to_string(kNoAllocMaxPixels) + "; use pt_render");
-  if (!accum_rgba || !is_device_ptr(accum_rgba))
-    return fail(ctx, PT_EINVAL, "pt_render_noalloc needs a device accumulator");
+  if (!accum_rgba || device_ptr_kind(accum_rgba, ctx->device) <= 0)
+    return fail(ctx, PT_EINVAL, "pt_render_noalloc needs a device accumulator on the "
+                                "context's GPU");
   CK(cudaSetDevice(ctx->device));
   unsigned char* base = nullptr;
   rc = noalloc_setup(ctx, &base);
@@ -1247,6 +1265,7 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
   cudaStream_t st = ctx->stream;
   CK(cudaEventRecord(ctx->ev0, (cudaStream_t)stream));
   CK(cudaStreamWaitEvent(st, ctx->ev0, 0));
+  CK(cudaEventRecord(ctx->ev0, st));  // start of the device time (render_ms)
   reset_render_stats(ctx);
   float4* acc = (float4*)accum_rgba;
   if (p->frame0 == 0) CK(cudaMemsetAsync(acc, 0, WH * sizeof(float4), st));
@@ -1295,6 +1314,9 @@ extern "C" PT_API int pt_render_noalloc(pt_context* ctx, const pt_render_params*
   CK(cudaEventRecord(ctx->ev1, st));
   CK(cudaStreamWaitEvent((cudaStream_t)stream, ctx->ev1, 0));
   CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->stats.render_ms = ms;
   return PT_OK;
 }
 

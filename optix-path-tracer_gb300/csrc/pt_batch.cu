@@ -431,7 +431,10 @@ static int batch_render(pt_batch* b, const pt_batch_item* items, int n, float4* 
     max_wh = std::max(max_wh, wh);
     if (acc_override) {
       acc[i] = acc_override[i];
-    } else if (is_device_ptr(items[i].accum_rgba)) {
+    } else if (int kind = device_ptr_kind(items[i].accum_rgba, b->device)) {
+      if (kind < 0)
+        return bfail(b, PT_EINVAL, "batch item " + std::to_string(i) +
+                                       ": accumulator is device memory of another GPU");
       acc[i] = (float4*)items[i].accum_rgba;
     } else {
       stage_off[i] = stage;

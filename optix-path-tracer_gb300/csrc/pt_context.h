@@ -74,6 +74,7 @@ struct GuideState {
   int steps = 8;             // Adam steps per frame on the frame's samples
   float exponent = 1.f;      // training weight = (F/q)^exponent (1: the KL target)
   int max_bounces = 4;       // guided bounces per path (0: all)
+  uint32_t wait_limit = 1u << 24;  // try_waits per tensor-core completion wait
   float bmin[3] = {0, 0, 0}, binv[3] = {1, 1, 1};
   int step = 0;
   int grid = 0;
@@ -151,7 +152,9 @@ int build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<float4>
 /* Carves the wavefront arrays of `slots` paths out of one float4 block
  * (PT_SLOT_F4 per slot) and one uint4 block (PT_SLOT_U4 per slot). */
 void carve_wave(WaveState& W, float4* f, uint4* u, size_t slots);
-bool is_device_ptr(const void* p);
+/* 1: device memory of `device` (or managed memory), usable by its kernels;
+ * 0: host memory (pageable or pinned); -1: device memory of another GPU. */
+int device_ptr_kind(const void* p, int device);
 /* Whether shading in material-sorted tiles pays for this scene: it does when
  * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
  * is present, whose code paths diverge most in a mixed warp. */

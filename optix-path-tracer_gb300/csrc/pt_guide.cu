@@ -64,10 +64,16 @@ __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
                : "memory");
 }
 
-// Bounded wait for an mbarrier phase; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+// Bounded wait for an mbarrier phase: at most `limit` try_waits; false when
+// the limit ran out.  The kernels' waits take the limit from their arguments
+// (pt_guide_set_wait_limit: 2^24 by default, 0 runs out at once); after a
+// wait ran out, the wait for the MMAs still in flight always uses
+// kDrainLimit, so no kernel reads or frees TMEM under a running MMA.
+constexpr uint32_t kDrainLimit = 1u << 24;
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t limit) {
   uint32_t done = 0;
-  for (int it = 0; it < (1 << 24) && !done; it++) {
+  for (uint32_t it = 0; it < limit && !done; it++) {
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         "selp.u32 %0, 1, 0, p;\n}\n"
@@ -231,7 +237,7 @@ struct TmemGuard {
 // T[l+1] (training keeps every activation), with nT == 2 it ping-pongs.
 // Returns false, in every thread alike, when a wait ran out.
 __device__ bool forward_tile(uint32_t tmem, TmemGuard& g, uint32_t& phase, unsigned char* W,
-                             unsigned char* const* T, int nT, float* out) {
+                             unsigned char* const* T, int nT, float* out, uint32_t limit) {
   const int row = threadIdx.x;
   const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
   for (int l = 0; l < 5; l++) {
@@ -244,7 +250,7 @@ __device__ bool forward_tile(uint32_t tmem, TmemGuard& g, uint32_t& phase, unsig
       issue_forward(tmem, in, W, l);
       mma_commit(&g.mbar);
     }
-    bool ok = mbar_wait(&g.mbar, phase);
+    bool ok = mbar_wait(&g.mbar, phase, limit);
     phase ^= 1u;
     fence_after();
     if (!__syncthreads_and(ok)) return false;
@@ -362,7 +368,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
     if (valid) smp = A.samples[s];
     write_features_vec(T[0], tid, smp.P, smp.N, smp.Wo, A.bmin, A.binv, valid);
     float o[PTG_NOUT];
-    if (!forward_tile(tmem, g, phase, W, T, 5, o)) {
+    if (!forward_tile(tmem, g, phase, W, T, 5, o, A.wait_limit)) {
       failed = true;
       break;
     }
@@ -405,7 +411,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
         }
         mma_commit(&g.mbar);
       }
-      bool ok = mbar_wait(&g.mbar, phase);
+      bool ok = mbar_wait(&g.mbar, phase, A.wait_limit);
       phase ^= 1u;
       fence_after();
       if (!__syncthreads_and(ok)) {
@@ -431,6 +437,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
     if (failed) break;
     first = false;
   }
+  // after a wait that ran out, the MMAs in flight (phase was flipped past
+  // it) finish before TMEM is read or freed; this wait is bounded too
+  if (failed) mbar_wait(&g.mbar, phase ^ 1u, kDrainLimit);
   // ---- per-CTA partial gradients (rows of dW live in lanes 0..rows-1)
   fence_before();
   __syncthreads();
@@ -450,11 +459,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_grad(GuideTrainArgs A) {
     }
   }
   if (loss_acc != 0.f && A.loss) atomicAdd(A.loss, loss_acc);
-  if (failed) {
-    if (tid == 0) atomicOr(A.fail, 1u);
-    // give MMAs still in flight a second bounded wait before freeing TMEM
-    mbar_wait(&g.mbar, phase);
-  }
+  if (failed && tid == 0) atomicOr(A.fail, 1u);
   fence_before();
   __syncthreads();
   if (warp == 0)
@@ -616,7 +621,7 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
         issue_forward(tmem, T, Wt, l);
         mma_commit(&mbar[grp]);
       }
-      bool ok = mbar_wait(&mbar[grp], phase);
+      bool ok = mbar_wait(&mbar[grp], phase, A.wait_limit);
       phase ^= 1u;
       fence_after();
       if (!group_and(ok, bar_id)) {
@@ -650,7 +655,7 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
   }
   if (failed) {
     if (row == 0) atomicOr(A.fail, 1u);
-    mbar_wait(&mbar[grp], phase);
+    mbar_wait(&mbar[grp], phase ^ 1u, kDrainLimit);  // the MMAs in flight finish first
   }
   fence_before();
   __syncthreads();

@@ -84,6 +84,7 @@ struct GuideInferArgs {
   uint32_t* rows;           // positions that need a guide this iteration (k_guide_select)
   float bmin[3], binv[3];   // scene box for the position encoding
   uint32_t* fail;
+  uint32_t wait_limit;      // try_waits per tensor-core completion wait
 };
 
 // Training / evaluation on explicit samples.
@@ -99,6 +100,7 @@ struct GuideTrainArgs {
   int train;                // 1: backward + partial gradients
   uint32_t max_count;       // use at most this many samples (0: all)
   uint32_t* fail;
+  uint32_t wait_limit;      // try_waits per tensor-core completion wait
 };
 
 struct GuideAdamArgs {

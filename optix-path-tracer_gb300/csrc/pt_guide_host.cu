@@ -108,6 +108,7 @@ GuideInferArgs pth::guide_infer_args(pt_context* ctx) {
   memcpy(a.bmin, G.bmin, sizeof(a.bmin));
   memcpy(a.binv, G.binv, sizeof(a.binv));
   a.fail = G.counters.p + 2;  // read back at the end of a guided render
+  a.wait_limit = G.wait_limit;
   return a;
 }
 
@@ -146,6 +147,7 @@ int pth::guide_frame_train(pt_context* ctx) {
   a.train = 1;
   a.max_count = cap;
   a.fail = G.counters.p + 1;
+  a.wait_limit = G.wait_limit;
   for (int k = 0; k < G.steps; k++) {
     pt::launch_guide_grad(a, G.grid, st);
     GuideAdamArgs d;
@@ -208,6 +210,7 @@ static int guide_step(pt_context* ctx, int n, bool update, float lr, float* loss
   memcpy(a.binv, G.binv, sizeof(a.binv));
   a.train = 1;
   a.fail = G.counters.p + 1;
+  a.wait_limit = G.wait_limit;
   GK(cudaMemsetAsync(G.scalars.p, 0, 4, st));
   pt::launch_guide_grad(a, G.grid, st);
   GK(cudaGetLastError());
@@ -276,6 +279,12 @@ PT_API int pt_guide_init(pt_context* ctx, uint64_t seed) {
         w[PTG_LAYER_OFF(l) + i * PTG_K + c] = (2.f * r.uniform() - 1.f) * lim;
   }
   return upload_params(ctx, w);
+}
+
+PT_API int pt_guide_set_wait_limit(pt_context* ctx, uint32_t try_waits) {
+  if (!ctx) return PT_EINVAL;
+  ctx->guide.wait_limit = try_waits;
+  return PT_OK;
 }
 
 PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent,
@@ -380,6 +389,7 @@ PT_API int pt_guide_eval(pt_context* ctx, const float* samples, int n, float* ou
   memcpy(a.binv, G.binv, sizeof(a.binv));
   a.train = 0;
   a.fail = G.counters.p + 1;
+  a.wait_limit = G.wait_limit;
   pt::launch_guide_grad(a, G.grid, ctx->stream);
   GK(cudaGetLastError());
   uint32_t h_cnt[2];

@@ -122,6 +122,7 @@ SIGNATURES = {
     "pt_render_noalloc": [_P, ctypes.POINTER(RenderParams), _P, _P],
     "pt_guide_init": [_P, ctypes.c_uint64],
     "pt_guide_set_training": [_P, ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int],
+    "pt_guide_set_wait_limit": [_P, ctypes.c_uint32],
     "pt_guide_get_params": [_P, _P],
     "pt_guide_set_params": [_P, _P],
     "pt_guide_get_state": [_P, _P, ctypes.POINTER(ctypes.c_int64)],

@@ -267,3 +267,28 @@ def test_guide_argument_checks(ptgb_mod):
     with pytest.raises(ptgb_mod.PtError):
         g.render(P(16, 16, 1, mode=1, guide=2))
     g.close()
+
+
+def test_wait_limit_times_out_cleanly(ptgb_mod):
+    """A tensor-core wait that runs out (here: a bound of zero attempts)
+    stops the guide kernel, lets its MMAs in flight finish, frees its tensor
+    memory and reports PT_ETIMEOUT; with the default bound restored the same
+    context evaluates and differentiates the network exactly as before."""
+    g = ptgb_mod.GpuRenderer(ptgb_mod.material_zoo(32, 24))
+    g.guide_init(11)
+    bmin, binv = g.guide_bounds()
+    s = random_samples(np.random.default_rng(4), 700, bmin, binv)
+    out0 = g.guide_eval(s)
+    grad0, loss0 = g.guide_gradient(s)
+    L = g.lib
+    assert L.pt_guide_set_wait_limit(g.ctx, 0) == 0
+    for call in (lambda: g.guide_eval(s), lambda: g.guide_gradient(s)):
+        with pytest.raises(ptgb_mod.PtError) as e:
+            call()
+        assert e.value.code == -4 and "ran out" in str(e.value)
+    assert L.pt_guide_set_wait_limit(g.ctx, 1 << 24) == 0
+    assert np.array_equal(g.guide_eval(s), out0)
+    grad1, loss1 = g.guide_gradient(s)
+    assert np.array_equal(grad1, grad0)          # per-CTA partials summed in a fixed order
+    assert abs(loss1 - loss0) <= 1e-6 * abs(loss0)  # per-CTA losses added atomically
+    g.close()

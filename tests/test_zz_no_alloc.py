@@ -70,3 +70,28 @@ def test_noalloc_progressive_and_limits(ptgb_mod):
     rc = L.pt_render_noalloc(g.ctx, ctypes.byref(p1), host.ctypes.data_as(ctypes.c_void_p), None)
     assert rc == -1
     g.close()
+
+
+def test_noalloc_consistent_mode_with_environment(ptgb_mod):
+    """Consistent mode (NEE + MIS, shadow rays through the occlusion
+    traversal, the environment map importance-sampled) through the static
+    scratch: two calls in a row equal pt_render, and the device time is
+    reported."""
+    torch = pytest.importorskip("torch")
+    w, h = 96, 54
+    g = ptgb_mod.GpuRenderer(ptgb_mod.heightfield_scene(w, h, cells=48, env_w=256, env_h=128))
+    L = g.lib
+    prm = ptgb_mod.GpuRenderer.params(w, h, 4, mode=1)
+    ref = g.render(prm)
+    acc = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        acc.fill_(-7.0)
+        rc = L.pt_render_noalloc(g.ctx, ctypes.byref(prm), ctypes.c_void_p(acc.data_ptr()), None)
+        assert rc == 0, L.pt_last_error(g.ctx)
+        torch.cuda.synchronize()
+        out = acc.cpu().numpy()
+        assert np.array_equal(out[..., 3], ref[..., 3])
+        assert rel_err(out[..., :3], ref[..., :3]).max() <= REL_TOL
+        st = g.stats()
+        assert st["shadow_rays"] > 0 and st["render_ms"] > 0
+    g.close()

@@ -2270,3 +2270,256 @@ extern "C" int or_probe(void* sp, const float* o, const float* d, float tmin, fl
   memcpy(rec, v, sizeof(v));
   return h.prim;
 }
+
+// ===================================================== FP64 hit distances ==
+// A double-precision ray-primitive oracle against which the FP32 hit
+// distances (oracle and kernels alike) are stated.  The primitives are the
+// same float data (an instance transform is the float matrix, inverted here
+// in double without rounding); the tests run in double: sphere roots by the
+// cancellation-free quadratic, rect planes, box slabs, triangles by the
+// Moller-Trumbore test (exact enough in double).  Traversal reuses the float
+// BVH, whose boxes are padded conservatively, with the slab test in double.
+namespace {
+
+struct D3 {
+  double x, y, z;
+};
+inline D3 dd(V3 v) { return D3{v.x, v.y, v.z}; }
+inline D3 dsub(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 dcross(D3 a, D3 b) {
+  return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double dget(D3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+void inverse64(const float* m, double* out) {
+  double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9],
+         i = m[10];
+  double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+  double inv_det = 1.0 / (a * A + b * B + c * C);
+  double r[9] = {A * inv_det, -(b * i - c * h) * inv_det, (b * f - c * e) * inv_det,
+                 B * inv_det, (a * i - c * g) * inv_det, -(a * f - c * d) * inv_det,
+                 C * inv_det, -(a * h - b * g) * inv_det, (a * e - b * d) * inv_det};
+  for (int row = 0; row < 3; row++) {
+    out[row * 4 + 0] = r[row * 3 + 0];
+    out[row * 4 + 1] = r[row * 3 + 1];
+    out[row * 4 + 2] = r[row * 3 + 2];
+    out[row * 4 + 3] = -(r[row * 3 + 0] * m[3] + r[row * 3 + 1] * m[7] + r[row * 3 + 2] * m[11]);
+  }
+}
+
+// Candidate of one primitive for a world ray (o, d) in double.  Returns true
+// on a hit with t > tmin; t is then the hit distance, else the distance to
+// the primitive's surface where the ray passes nearest (plane t for
+// triangles and rects, the closest approach for spheres, the slab entry for
+// boxes).  The FP32 error statement uses three more numbers:
+//   margin  how far inside the primitive's outline the ray passes, relative
+//           to its size (triangles: the smallest barycentric; rects: the
+//           nearest edge distance / extent; spheres: (r - h) / r with h the
+//           ray's distance to the centre; boxes: slab overlap / box size);
+//           negative on a miss;
+//   mslack  the size of the rounding error of an FP32 evaluation of margin,
+//           in units of epsilon (position magnitude / primitive size; for
+//           spheres (|o - c|^2 + r^2) / r^2, from c = |o - c|^2 - r^2);
+//   tslack  the size of the rounding error of an FP32 t, as a distance in
+//           units of epsilon: |o| + t|d| (for spheres plus
+//           (|o - c|^2 + r^2) / L, L the half chord: the discriminant's
+//           cancellation).
+struct Cand64 {
+  double t, margin, mslack, tslack;
+};
+
+bool cand64(const Scene& s, const Prim& p, D3 o, D3 d, double tmin, Cand64& c64) {
+  D3 wo = o, wd = d;
+  if (p.xform >= 0) {
+    double inv[12];
+    inverse64(s.xforms[p.xform].m, inv);
+    D3 oo{inv[0] * o.x + inv[1] * o.y + inv[2] * o.z + inv[3],
+          inv[4] * o.x + inv[5] * o.y + inv[6] * o.z + inv[7],
+          inv[8] * o.x + inv[9] * o.y + inv[10] * o.z + inv[11]};
+    D3 od{inv[0] * d.x + inv[1] * d.y + inv[2] * d.z, inv[4] * d.x + inv[5] * d.y + inv[6] * d.z,
+          inv[8] * d.x + inv[9] * d.y + inv[10] * d.z};
+    o = oo;
+    d = od;
+  }
+  const float* f = p.f;
+  const double on = sqrt(ddot(wo, wo)), dn = sqrt(ddot(wd, wd));
+  double& t = c64.t;
+  c64.margin = -1.0;
+  c64.mslack = 1.0;
+  bool hit = false;
+  if (p.type == PRIM_SPHERE) {
+    double r = f[3];
+    D3 oc = dsub(o, D3{f[0], f[1], f[2]});
+    double a = ddot(d, d), b = ddot(oc, d), occ = ddot(oc, oc), c = occ - r * r;
+    double disc = b * b - a * c;
+    double h2 = std::max(0.0, occ - b * b / a);
+    c64.margin = (r - sqrt(h2)) / r;
+    c64.mslack = (occ + r * r) / (r * r);
+    double L = disc > 0.0 ? sqrt(disc / a) : 0.0;
+    if (disc < 0.0) {
+      t = -b / a;
+    } else {
+      double sq = sqrt(disc);
+      double q = b > 0.0 ? -(b + sq) : -(b - sq);
+      double t0 = q / a, t1 = c / q;
+      if (t0 > t1) std::swap(t0, t1);
+      if (t0 > tmin) { t = t0; hit = true; }
+      else if (t1 > tmin) { t = t1; hit = true; }
+      else { t = t1; c64.margin = -1.0; }
+    }
+    c64.tslack = on + fabs(t) * dn + (occ + r * r) / std::max(L, 1e-300);
+    return hit;
+  }
+  if (p.type == PRIM_RECT) {
+    int ax = p.axis, ia = ax == 0 ? 1 : 0, ib = ax == 2 ? 1 : 2;
+    t = ((double)f[4] - dget(o, ax)) / dget(d, ax);
+    double a = dget(o, ia) + t * dget(d, ia), b = dget(o, ib) + t * dget(d, ib);
+    double ea = (double)f[1] - f[0], eb = (double)f[3] - f[2];
+    double ext = std::max(std::min(ea, eb), 1e-30);
+    c64.margin = std::min(std::min(a - f[0], f[1] - a), std::min(b - f[2], f[3] - b)) / ext;
+    c64.tslack = on + fabs(t) * dn;
+    c64.mslack = c64.tslack / ext + 1.0;
+    return c64.margin >= 0.0 && t > tmin;
+  }
+  if (p.type == PRIM_BOX) {
+    double tn = -INFINITY, tf = INFINITY, size = INFINITY;
+    for (int k = 0; k < 3; k++) {
+      double t0 = ((double)f[k] - dget(o, k)) / dget(d, k);
+      double t1 = ((double)f[3 + k] - dget(o, k)) / dget(d, k);
+      tn = std::max(tn, std::min(t0, t1));
+      tf = std::min(tf, std::max(t0, t1));
+      size = std::min(size, (double)f[3 + k] - f[k]);
+    }
+    size = std::max(size, 1e-30);
+    c64.margin = (tf - tn) * sqrt(ddot(d, d)) / size;
+    if (tn <= tf) {
+      if (tn > tmin) { t = tn; hit = true; }
+      else if (tf > tmin) { t = tf; hit = true; }
+      else t = tf;
+    } else {
+      t = tn;
+    }
+    c64.tslack = on + fabs(t) * dn;
+    c64.mslack = c64.tslack / size + 1.0;
+    return hit;
+  }
+  D3 v0{f[0], f[1], f[2]}, v1{f[3], f[4], f[5]}, v2{f[6], f[7], f[8]};
+  D3 e1 = dsub(v1, v0), e2 = dsub(v2, v0);
+  D3 P = dcross(d, e2);
+  double det = ddot(P, e1);
+  D3 R = dsub(o, v0);
+  D3 Q = dcross(R, e1);
+  if (det == 0.0) {
+    t = INFINITY;
+    c64.tslack = INFINITY;
+    return false;
+  }
+  double u = ddot(P, R) / det, v = ddot(Q, d) / det;
+  t = ddot(Q, e2) / det;
+  c64.margin = std::min(std::min(u, v), 1.0 - u - v);
+  D3 e3 = dsub(v2, v1);
+  double area2 = sqrt(ddot(dcross(e1, e2), dcross(e1, e2)));
+  double maxe = sqrt(std::max(std::max(ddot(e1, e1), ddot(e2, e2)), ddot(e3, e3)));
+  double alt = std::max(area2 / maxe, 1e-30);
+  c64.tslack = on + fabs(t) * dn;
+  c64.mslack = c64.tslack / alt + 1.0;
+  return c64.margin >= 0.0 && t > tmin;
+}
+
+struct Hit64 {
+  int prim = -1;
+  double t = INFINITY;
+  Cand64 c{};
+};
+
+Hit64 trace64(const Scene& s, D3 o, D3 d, double tmin) {
+  Hit64 best;
+  if (s.nodes.empty()) return best;
+  D3 inv{1.0 / d.x, 1.0 / d.y, 1.0 / d.z};
+  auto slab = [&](const AABB& b, double& tn) {
+    double lo = tmin, hi = best.t;
+    for (int k = 0; k < 3; k++) {
+      double t0 = (dget(dd(b.lo), k) - dget(o, k)) * dget(inv, k);
+      double t1 = (dget(dd(b.hi), k) - dget(o, k)) * dget(inv, k);
+      if (t0 > t1) std::swap(t0, t1);
+      if (t0 == t0) lo = std::max(lo, t0);  // a NaN bound (0 * inf) constrains nothing
+      if (t1 == t1) hi = std::min(hi, t1);
+    }
+    tn = lo;
+    return lo <= hi;
+  };
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const BNode& n = s.nodes[stack[--sp]];
+    double tn;
+    if (!slab(n.box, tn)) continue;
+    if (n.count) {
+      for (int k = n.left; k < n.left + n.count; k++) {
+        int pid = s.order[k];
+        Cand64 c;
+        if (!cand64(s, s.prims[pid], o, d, tmin, c)) continue;
+        if (c.t < best.t || (c.t == best.t && pid < best.prim)) {
+          best.prim = pid;
+          best.t = c.t;
+          best.c = c;
+        }
+      }
+    } else {
+      stack[sp++] = n.right;
+      stack[sp++] = n.left;
+    }
+  }
+  return best;
+}
+
+}  // namespace
+
+// Camera rays of frame `frame` (float, as the float path generates them):
+// origins and directions, 3 floats each per pixel.
+extern "C" void or_camera_rays(void* sp, int W, int H, int frame, float* o, float* d) {
+  Scene& s = *(Scene*)sp;
+  Tracer tr{s, nullptr};
+  for (int p = 0; p < W * H; p++) {
+    uint32_t x = p % W, y = p / W;
+    uint32_t seed = tea64((uint32_t)W * y + x, (uint32_t)frame);
+    Ray r = tr.camera_ray(x, y, W, H, seed);
+    o[3 * p] = r.o.x; o[3 * p + 1] = r.o.y; o[3 * p + 2] = r.o.z;
+    d[3 * p] = r.d.x; d[3 * p + 1] = r.d.y; d[3 * p + 2] = r.d.z;
+  }
+}
+
+// Closest hit in double of n rays (float origins and directions, tmin as
+// the float path's): primitive (-1), and per ray 4 doubles: t, margin,
+// mslack, tslack (see Cand64).
+extern "C" void or_trace64(void* sp, int n, const float* o, const float* d, float tmin,
+                           int32_t* prim, double* out, int threads) {
+  Scene& s = *(Scene*)sp;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+  for (int i = 0; i < n; i++) {
+    Hit64 h = trace64(s, D3{o[3 * i], o[3 * i + 1], o[3 * i + 2]},
+                      D3{d[3 * i], d[3 * i + 1], d[3 * i + 2]}, (double)tmin);
+    prim[i] = h.prim;
+    double* q = out + 4 * i;
+    q[0] = h.prim >= 0 ? h.c.t : 0.0;
+    q[1] = h.c.margin;
+    q[2] = h.c.mslack;
+    q[3] = h.c.tslack;
+  }
+}
+
+// One primitive in double for one ray: 1 on a hit; out = t, margin, mslack,
+// tslack.
+extern "C" int or_prim64(void* sp, int prim, const float* o, const float* d, float tmin,
+                         double* out) {
+  Scene& s = *(Scene*)sp;
+  Cand64 c;
+  bool hit = cand64(s, s.prims[prim], D3{o[0], o[1], o[2]}, D3{d[0], d[1], d[2]}, (double)tmin, c);
+  out[0] = c.t;
+  out[1] = c.margin;
+  out[2] = c.mslack;
+  out[3] = c.tslack;
+  return hit ? 1 : 0;
+}

@@ -70,6 +70,9 @@ def load():
     L.or_helper.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P]
     L.or_light.argtypes = [_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P]
     L.or_probe.argtypes = [_P, _P, _P, ctypes.c_float, _P, _P]
+    L.or_camera_rays.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]
+    L.or_trace64.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_float, _P, _P, ctypes.c_int]
+    L.or_prim64.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_float, _P]
     _lib = L
     return L
 
@@ -152,6 +155,30 @@ class Oracle:
         pdf = np.zeros(n, dtype=np.float32)
         ok = self.L.or_env_sample(self.h, _p(u), n, _p(dirs), _p(pdf))
         return (dirs, pdf) if ok else (None, None)
+
+    def camera_rays(self, width, height, frame):
+        """Camera rays of `frame` as the float path generates them."""
+        o = np.zeros((width * height, 3), np.float32)
+        d = np.zeros((width * height, 3), np.float32)
+        self.L.or_camera_rays(self.h, width, height, frame, _p(o), _p(d))
+        return o, d
+
+    def trace64(self, o, d, tmin=1e-6, threads=0):
+        """Closest hits in double precision: primitive (-1) and, per ray, t,
+        margin, mslack, tslack (the FP32 error scales; see or_trace64)."""
+        o, d = _f(o), _f(d)
+        n = len(o)
+        prim = np.zeros(n, np.int32)
+        out = np.zeros((n, 4), np.float64)
+        self.L.or_trace64(self.h, n, _p(o), _p(d), tmin, _p(prim), _p(out),
+                          threads or os.cpu_count())
+        return prim, out
+
+    def prim64(self, prim, o, d, tmin=1e-6):
+        """(hit, [t, margin, mslack, tslack]) of one primitive in double."""
+        out = np.zeros(4, np.float64)
+        hit = self.L.or_prim64(self.h, int(prim), _p(_f(o)), _p(_f(d)), tmin, _p(out))
+        return bool(hit), out
 
     def first_hits(self, width, height, frame, threads=0):
         prim = np.zeros(width * height, dtype=np.int32)

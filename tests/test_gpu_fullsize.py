@@ -94,3 +94,16 @@ def test_large_mesh_batch_items_equal_plain_renders(ptgb_mod):
         assert np.array_equal(a, ref), f"item {k} ({2 * cells[k] ** 2} triangles) differs"
     for r in rends:
         r.close()
+
+
+def test_fullsize_gpu_hit_distances_against_fp64(fullsize, oracle_mod):
+    """The GPU's FP32 first-hit distances on the 2.1M-triangle scene, stated
+    against the double-precision ray-primitive oracle with the bounds of
+    tests/test_fp64_hits.py (|t32 - t64| |d| <= 16 eps tslack; ids differ
+    only within 4 eps of an outline)."""
+    from test_fp64_hits import check_against_fp64
+    scene, _, rends = fullsize
+    for builder in (1, 2):
+        gp, _, gt = rends[builder].first_hits(FH_W, FH_H, 2)
+        kmax, ndis = check_against_fp64(oracle_mod, scene, FH_W, FH_H, 2, gp, gt)
+        assert ndis <= 5

@@ -131,8 +131,14 @@ def test_forward_matches_reference(guide):
     ref, _, _ = reference(torch, g.guide_params(), s, bmin, binv, train=False)
     err = np.abs(out[:, :41] - ref)
     scale = np.abs(ref).max()
-    assert np.median(err) <= 2e-3 * scale
-    assert err.max() <= 5e-2 * scale, err.max() / scale
+    # Both sides round the stored activations to BF16 at the same points;
+    # FP32 tensor-core sums and float64 sums can land on opposite sides of a
+    # BF16 rounding boundary (one step: 2^-8 relative), which the next
+    # layers carry on.  Bound: two such steps of the output scale
+    # (measured: max 0.0034-0.0039, 99th percentile < 0.001, median 0).
+    assert np.median(err) <= 1e-4 * scale
+    assert np.quantile(err, 0.99) <= 2.0 ** -9 * scale
+    assert err.max() <= 2.0 ** -7 * scale, err.max() / scale
     assert np.all(out[:, 41:] == 0)
 
 

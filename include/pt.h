@@ -135,6 +135,50 @@ PT_API int pt_material_ashikhmin_shirley(pt_context* ctx, const float diffuse[3]
                                          const float specular[3], float nu, float nv,
                                          uint32_t* id);
 
+/* ---- textures (host_includes/textures.hpp, the programs of programs/textures/)
+ * A texture maps a hit's (u, v, P, texture index) to a colour; a material
+ * slot that names one uses it in place of its constant colour.  Each call
+ * returns the texture id in *id; checker and vector textures name textures
+ * made before them.  Texture coordinates are the primitives' (sphere.cu:84-87,
+ * aarect.cu:71-115, triangle uvs); the texture index is 0 on analytic shapes
+ * and the face's index on meshes (pt_mesh_set_texture_index, the
+ * material_buffer of mesh.hpp:140-150). */
+#define PT_NO_TEXTURE 0xffffffffu
+/* Constant_Texture(float3)                     textures.hpp:19-37 */
+PT_API int pt_texture_constant(pt_context* ctx, const float rgb[3], uint32_t* id);
+/* Checker_Texture(odd, even): odd where sin(10x) sin(10y) sin(10z) < 0,
+ * checkered_texture.cu:8-15, textures.hpp:39-54 */
+PT_API int pt_texture_checker(pt_context* ctx, uint32_t odd, uint32_t even, uint32_t* id);
+/* Noise_Texture(scale, axis): Perlin turbulence, noise_texture.cu:12-76,
+ * textures.hpp:56-112.  ranvec: 256 x 3 floats, perm: perm_x, perm_y, perm_z
+ * (3 x 256 ints, values 0..255); null tables are made as the host class makes
+ * them (std::mt19937 seeded 0, uniform floats).  As in noise_texture.cu:66-73,
+ * whose switch has no breaks, every axis evaluates the Z-axis formula. */
+PT_API int pt_texture_noise(pt_context* ctx, float scale, int axis, const float* ranvec,
+                            const int32_t* perm, uint32_t* id);
+/* The default tables of pt_texture_noise (host only, no device work). */
+PT_API int pt_noise_tables(float* ranvec, int32_t* perm);
+/* Image_Texture / HDR_Texture: w x h RGBA float texels, row 0 at v = 0
+ * (the loaders flip the file's rows, textures.hpp:140-151), bilinear with
+ * repeat wrap; image_texture.cu:3-7, textures.hpp:114-230 */
+PT_API int pt_texture_image(pt_context* ctx, const float* rgba, int w, int h, uint32_t* id);
+/* Gradient_Texture(A, B, C): |n.x| A + |n.y| B + |n.z| C with n = P / |P|,
+ * gradient_texture.cu:7-14, textures.hpp:233-251 */
+PT_API int pt_texture_gradient(pt_context* ctx, const float a[3], const float b[3],
+                               const float c[3], uint32_t* id);
+/* Vector_Texture(textures): entry `texture index` (black outside 0..n-1),
+ * vector.cu:7-12, textures.hpp:253-271 */
+PT_API int pt_texture_vector(pt_context* ctx, const uint32_t* textures, int n, uint32_t* id);
+/* Material colour from a texture: slot 0 is the colour / albedo / diffuse /
+ * base / emission, slot 1 the Ashikhmin-Shirley specular or the dielectric
+ * extinction; PT_NO_TEXTURE restores the constant colour. */
+PT_API int pt_material_set_texture(pt_context* ctx, uint32_t material, int slot,
+                                   uint32_t texture);
+/* Texture index of n consecutive triangles from first_prim (their faces'
+ * entries of a vector texture; 0 by default), mesh.hpp:140-150 */
+PT_API int pt_mesh_set_texture_index(pt_context* ctx, uint32_t first_prim, size_t n,
+                                     const uint32_t* index);
+
 /* ---- geometry (host_includes/hitables.hpp, mesh.hpp) ---------------------
  * Primitive ids are assigned in call order (a mesh takes nt consecutive ids);
  * equal hit distances resolve to the lower id. */

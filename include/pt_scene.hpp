@@ -4,7 +4,8 @@
  *
  * Class and function names follow joaovbs96/OptiX-Path-Tracer's
  * host_includes/ so that scene code written against them (scenes.hpp) ports
- * by changing includes: Constant_Texture, HDR_Texture (textures.hpp),
+ * by changing includes: Constant_Texture, Checker_Texture, Noise_Texture,
+ * Image_Texture / HDR_Texture, Gradient_Texture, Vector_Texture (textures.hpp),
  * Lambertian, Metal, Dielectric, Diffuse_Light, Oren_Nayar, Torrance_Sparrow,
  * Ashikhmin_Shirley (materials.hpp), Sphere, AARect, Box, Mesh, Hitable_List
  * (hitables.hpp, mesh.hpp), Camera (camera.hpp), Rectangle_PDF, Sphere_PDF,
@@ -21,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -94,24 +96,153 @@ class Context {
 struct Group {};  // the top-level OptiX Group; here all primitives share one BVH8
 
 // ----------------------------------------------------------------- textures
+// host_includes/host_common.hpp:59-63: the host's random numbers (scene
+// generators and the Perlin tables draw from this one stream).
+inline float rnd() {
+  static std::mt19937 gen(0);
+  static std::uniform_real_distribution<float> dis(0.f, 1.f);
+  return dis(gen);
+}
+
+// host_includes/textures.hpp: a texture registers itself in a context once
+// (assignTo returns its texture id there, as the reference's returns its
+// callable program).
 struct Texture {
   virtual ~Texture() = default;
-  virtual float3v color() const = 0;
+  uint32_t assignTo(Context& ctx) const {
+    if (ctx_ != ctx.get()) {
+      id_ = create(ctx);
+      ctx_ = ctx.get();
+      ctx->dirty = true;
+    }
+    return id_;
+  }
+  // the colour of a constant texture (a material then needs no texture)
+  virtual bool constant(float3v* c) const {
+    (void)c;
+    return false;
+  }
+
+ protected:
+  virtual uint32_t create(Context& ctx) const = 0;
+  static const float* f3(const float3v& v) { return &v.x; }
+  mutable pt_context* ctx_ = nullptr;
+  mutable uint32_t id_ = 0;
 };
 
-struct Constant_Texture : public Texture {
+struct Constant_Texture : public Texture {  // textures.hpp:19-37
   explicit Constant_Texture(const float3v& c) : c_(c) {}
   explicit Constant_Texture(float rgb) : c_(make_float3(rgb)) {}
   Constant_Texture(float r, float g, float b) : c_(make_float3(r, g, b)) {}
-  float3v color() const override { return c_; }
+  bool constant(float3v* c) const override {
+    *c = c_;
+    return true;
+  }
   float3v c_;
+
+ protected:
+  uint32_t create(Context& c) const override {
+    uint32_t id;
+    c->check(pt_texture_constant(c.get(), f3(c_), &id), "Constant_Texture");
+    return id;
+  }
 };
 
-// HDR_Texture(file) after loading: RGBA float texels, row 0 at v = 0.
-struct HDR_Texture {
+struct Checker_Texture : public Texture {  // textures.hpp:39-54
+  Checker_Texture(const Texture* o, const Texture* e) : odd(o), even(e) {}
+  const Texture *odd, *even;
+
+ protected:
+  uint32_t create(Context& c) const override {
+    uint32_t o = odd->assignTo(c), e = even->assignTo(c), id;
+    c->check(pt_texture_checker(c.get(), o, e, &id), "Checker_Texture");
+    return id;
+  }
+};
+
+struct Noise_Texture : public Texture {  // textures.hpp:56-112
+  Noise_Texture(float s, AXIS ax = X_AXIS) : scale(s), ax(ax) {}
+  const float scale;
+  const AXIS ax;
+
+ protected:
+  static float3v unit_float3(float x, float y, float z) {
+    float l = std::sqrt(x * x + y * y + z * z);
+    return make_float3(x / l, y / l, z / l);
+  }
+  static void permute(int32_t* p) {
+    for (int i = 256 - 1; i > 0; i--) {
+      int target = int(rnd() * (i + 1));
+      int32_t tmp = p[i];
+      p[i] = p[target];
+      p[target] = tmp;
+    }
+  }
+  // the tables as the host class makes them, from the shared rnd() stream
+  uint32_t create(Context& c) const override {
+    std::vector<float> ranvec(768);
+    std::vector<int32_t> perm(768);
+    for (int i = 0; i < 256; ++i) {
+      float3v v = unit_float3(-1 + 2 * rnd(), -1 + 2 * rnd(), -1 + 2 * rnd());
+      ranvec[3 * i] = v.x;
+      ranvec[3 * i + 1] = v.y;
+      ranvec[3 * i + 2] = v.z;
+    }
+    for (int a = 0; a < 3; a++) {
+      for (int i = 0; i < 256; i++) perm[256 * a + i] = i;
+      permute(perm.data() + 256 * a);
+    }
+    uint32_t id;
+    c->check(pt_texture_noise(c.get(), scale, (int)ax, ranvec.data(), perm.data(), &id),
+             "Noise_Texture");
+    return id;
+  }
+};
+
+// Image_Texture / HDR_Texture after loading: RGBA float texels, row 0 at
+// v = 0 (textures.hpp:114-230; the loaders flip the file's rows and
+// normalise 8-bit texels to [0, 1]).  HDR_Texture also serves as the
+// environment map of setMissProgram.
+struct HDR_Texture : public Texture {
   HDR_Texture(const float* rgba, int w, int h) : rgba(rgba, rgba + (size_t)w * h * 4), w(w), h(h) {}
   std::vector<float> rgba;
   int w, h;
+
+ protected:
+  uint32_t create(Context& c) const override {
+    uint32_t id;
+    c->check(pt_texture_image(c.get(), rgba.data(), w, h, &id), "Image_Texture");
+    return id;
+  }
+};
+typedef HDR_Texture Image_Texture;
+
+struct Gradient_Texture : public Texture {  // textures.hpp:233-251
+  Gradient_Texture(const float3v& a, const float3v& b, const float3v& cc)
+      : colorA(a), colorB(b), colorC(cc) {}
+  const float3v colorA, colorB, colorC;
+
+ protected:
+  uint32_t create(Context& c) const override {
+    uint32_t id;
+    c->check(pt_texture_gradient(c.get(), f3(colorA), f3(colorB), f3(colorC), &id),
+             "Gradient_Texture");
+    return id;
+  }
+};
+
+struct Vector_Texture : public Texture {  // textures.hpp:253-271
+  explicit Vector_Texture(const std::vector<Texture*>& tv) : texture_vector(tv) {}
+  const std::vector<Texture*> texture_vector;
+
+ protected:
+  uint32_t create(Context& c) const override {
+    std::vector<uint32_t> ids;
+    for (const Texture* t : texture_vector) ids.push_back(t->assignTo(c));
+    uint32_t id;
+    c->check(pt_texture_vector(c.get(), ids.data(), (int)ids.size(), &id), "Vector_Texture");
+    return id;
+  }
 };
 
 // ---------------------------------------------------------------- materials
@@ -130,6 +261,18 @@ struct BRDF {
  protected:
   virtual uint32_t create(Context& ctx) const = 0;
   static const float* f3(const float3v& v) { return &v.x; }
+  // a texture's constant colour, or black where the material takes the
+  // texture itself (bind() then names it)
+  static float3v colour(const Texture* t) {
+    float3v c = make_float3(0.f);
+    t->constant(&c);
+    return c;
+  }
+  static void bind(Context& c, uint32_t id, int slot, const Texture* t) {
+    float3v unused;
+    if (!t->constant(&unused))
+      c->check(pt_material_set_texture(c.get(), id, slot, t->assignTo(c)), "texture");
+  }
   mutable pt_context* ctx_ = nullptr;
   mutable uint32_t id_ = 0;
 };
@@ -141,8 +284,8 @@ struct Lambertian : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v col = texture->color();
-    c->check(pt_material_lambertian(c.get(), f3(col), &id), "Lambertian");
+    c->check(pt_material_lambertian(c.get(), f3(colour(texture)), &id), "Lambertian");
+    bind(c, id, 0, texture);
     return id;
   }
 };
@@ -155,8 +298,8 @@ struct Metal : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v col = texture->color();
-    c->check(pt_material_metal(c.get(), f3(col), fuzz, &id), "Metal");
+    c->check(pt_material_metal(c.get(), f3(colour(texture)), fuzz, &id), "Metal");
+    bind(c, id, 0, texture);
     return id;
   }
 };
@@ -170,8 +313,11 @@ struct Dielectric : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v b = baseTex->color(), e = extTex->color();
-    c->check(pt_material_dielectric(c.get(), f3(b), f3(e), ref_idx, density, &id), "Dielectric");
+    c->check(pt_material_dielectric(c.get(), f3(colour(baseTex)), f3(colour(extTex)), ref_idx,
+                                    density, &id),
+             "Dielectric");
+    bind(c, id, 0, baseTex);
+    bind(c, id, 1, extTex);
     return id;
   }
 };
@@ -183,8 +329,8 @@ struct Diffuse_Light : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v col = texture->color();
-    c->check(pt_material_diffuse_light(c.get(), f3(col), &id), "Diffuse_Light");
+    c->check(pt_material_diffuse_light(c.get(), f3(colour(texture)), &id), "Diffuse_Light");
+    bind(c, id, 0, texture);
     return id;
   }
 };
@@ -197,8 +343,8 @@ struct Oren_Nayar : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v col = texture->color();
-    c->check(pt_material_oren_nayar(c.get(), f3(col), R, &id), "Oren_Nayar");
+    c->check(pt_material_oren_nayar(c.get(), f3(colour(texture)), R, &id), "Oren_Nayar");
+    bind(c, id, 0, texture);
     return id;
   }
 };
@@ -211,8 +357,9 @@ struct Torrance_Sparrow : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v col = texture->color();
-    c->check(pt_material_torrance_sparrow(c.get(), f3(col), nu, nv, &id), "Torrance_Sparrow");
+    c->check(pt_material_torrance_sparrow(c.get(), f3(colour(texture)), nu, nv, &id),
+             "Torrance_Sparrow");
+    bind(c, id, 0, texture);
     return id;
   }
 };
@@ -226,9 +373,11 @@ struct Ashikhmin_Shirley : public BRDF {
  protected:
   uint32_t create(Context& c) const override {
     uint32_t id;
-    float3v d = diffuse_tex->color(), s = specular_tex->color();
-    c->check(pt_material_ashikhmin_shirley(c.get(), f3(d), f3(s), nu, nv, &id),
+    c->check(pt_material_ashikhmin_shirley(c.get(), f3(colour(diffuse_tex)),
+                                           f3(colour(specular_tex)), nu, nv, &id),
              "Ashikhmin_Shirley");
+    bind(c, id, 0, diffuse_tex);
+    bind(c, id, 1, specular_tex);
     return id;
   }
 };

@@ -8,6 +8,7 @@
  * pt_render (the per-sample Context::launch of main.cpp:26-39,264).
  */
 #include <atomic>
+#include <random>
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cfloat>
@@ -108,6 +109,12 @@ static inline void xpoint_h(const float* m, const float* p, float* o) {
 
 static bool finite3(const float* v) {
   return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
+}
+
+bool pth::uses_textures(const pt_context* ctx) {
+  for (const GpuMaterial& m : ctx->mats)
+    if (m.tex0 >= 0 || m.tex1 >= 0) return true;
+  return false;
 }
 
 int pth::device_ptr_kind(const void* p, int device) {
@@ -291,9 +298,183 @@ static int add_material(pt_context* ctx, int type, const float* c0, const float*
   }
   m.p0 = p0;
   m.p1 = p1;
+  m.tex0 = m.tex1 = -1;
   ctx->mats.push_back(m);
   ctx->committed = false;
   *id = (uint32_t)ctx->mats.size() - 1;
+  return PT_OK;
+}
+
+// ----------------------------------------------------------------- textures
+// host_includes/textures.hpp: texture callables as records; a material slot
+// names a texture in place of its constant colour (pt_material_set_texture).
+static int add_texture(pt_context* ctx, GpuTexture t, uint32_t* id) {
+  if (!id) return fail(ctx, PT_EINVAL, "null argument");
+  ctx->textures.push_back(t);
+  ctx->committed = false;
+  *id = (uint32_t)ctx->textures.size() - 1;
+  return PT_OK;
+}
+
+static GpuTexture blank_texture(int kind) {
+  GpuTexture t;
+  memset(&t, 0, sizeof(t));
+  t.kind = kind;
+  return t;
+}
+
+PT_API int pt_texture_constant(pt_context* ctx, const float rgb[3], uint32_t* id) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(rgb)) return fail(ctx, PT_EINVAL, "texture colour must be finite");
+  GpuTexture t = blank_texture(PT_TEX_CONSTANT);
+  for (int k = 0; k < 3; k++) t.c[k] = rgb[k];
+  return add_texture(ctx, t, id);
+}
+
+PT_API int pt_texture_checker(pt_context* ctx, uint32_t odd, uint32_t even, uint32_t* id) {
+  if (!ctx) return PT_EINVAL;
+  if (odd >= ctx->textures.size() || even >= ctx->textures.size())
+    return fail(ctx, PT_EINVAL, "checker: unknown texture id");
+  GpuTexture t = blank_texture(PT_TEX_CHECKER);
+  t.a = (int)odd;
+  t.b = (int)even;
+  return add_texture(ctx, t, id);
+}
+
+// Perlin tables as Noise_Texture::assignTo makes them (textures.hpp:63-106):
+// 256 unit vectors of (-1 + 2 rnd()) components, then perm_x, perm_y,
+// perm_z, each a Fisher-Yates shuffle of 0..255 from the top; rnd() is the
+// host's std::mt19937 seeded 0 with a uniform float distribution
+// (host_common.hpp:59-63), drawn left to right.
+static void noise_tables(float* ranvec, int32_t* perm) {
+  std::mt19937 gen(0);
+  std::uniform_real_distribution<float> dis(0.f, 1.f);
+  for (int i = 0; i < 256; i++) {
+    float x = -1 + 2 * dis(gen);
+    float y = -1 + 2 * dis(gen);
+    float z = -1 + 2 * dis(gen);
+    float l = std::sqrt(x * x + y * y + z * z);
+    ranvec[3 * i] = x / l;
+    ranvec[3 * i + 1] = y / l;
+    ranvec[3 * i + 2] = z / l;
+  }
+  for (int a = 0; a < 3; a++) {
+    int32_t* p = perm + 256 * a;
+    for (int i = 0; i < 256; i++) p[i] = i;
+    for (int i = 256 - 1; i > 0; i--) {
+      int target = int(dis(gen) * (i + 1));
+      int tmp = p[i];
+      p[i] = p[target];
+      p[target] = tmp;
+    }
+  }
+}
+
+PT_API int pt_noise_tables(float* ranvec, int32_t* perm) {
+  if (!ranvec || !perm) return PT_EINVAL;
+  noise_tables(ranvec, perm);
+  return PT_OK;
+}
+
+PT_API int pt_texture_noise(pt_context* ctx, float scale, int axis, const float* ranvec,
+                            const int32_t* perm, uint32_t* id) {
+  if (!ctx) return PT_EINVAL;
+  if (!std::isfinite(scale)) return fail(ctx, PT_EINVAL, "noise scale must be finite");
+  if (axis < 0 || axis > 2) return fail(ctx, PT_EINVAL, "invalid axis");
+  float rv[768];
+  int32_t pm[768];
+  if (!ranvec || !perm) noise_tables(rv, pm);
+  if (ranvec) memcpy(rv, ranvec, sizeof(rv));
+  if (perm) memcpy(pm, perm, sizeof(pm));
+  for (int k = 0; k < 768; k++) {
+    if (!std::isfinite(rv[k])) return fail(ctx, PT_EINVAL, "noise vectors must be finite");
+    if (pm[k] < 0 || pm[k] > 255) return fail(ctx, PT_EINVAL, "noise permutations: 0..255");
+  }
+  GpuTexture t = blank_texture(PT_TEX_NOISE);
+  t.a = axis;
+  t.c[0] = scale;
+  t.data = (int)ctx->tex_data.size();
+  for (int i = 0; i < 256; i++)
+    ctx->tex_data.push_back(make_float4(rv[3 * i], rv[3 * i + 1], rv[3 * i + 2], 0.f));
+  for (int i = 0; i < 768; i += 4) {
+    float4 q;
+    memcpy(&q, pm + i, sizeof(q));
+    ctx->tex_data.push_back(q);
+  }
+  return add_texture(ctx, t, id);
+}
+
+PT_API int pt_texture_image(pt_context* ctx, const float* rgba, int w, int h, uint32_t* id) {
+  if (!ctx) return PT_EINVAL;
+  if (!rgba || w <= 0 || h <= 0 || (size_t)w * h > ((size_t)1 << 28))
+    return fail(ctx, PT_EINVAL, "image texture: texels and a size of 1 .. 2^28 texels");
+  GpuTexture t = blank_texture(PT_TEX_IMAGE);
+  t.a = w;
+  t.b = h;
+  t.data = (int)ctx->tex_data.size();
+  size_t n = (size_t)w * h;
+  for (size_t k = 0; k < 4 * n; k++)
+    if (!std::isfinite(rgba[k])) return fail(ctx, PT_EINVAL, "image texels must be finite");
+  size_t base = ctx->tex_data.size();
+  ctx->tex_data.resize(base + n);
+  memcpy(ctx->tex_data.data() + base, rgba, n * sizeof(float4));
+  return add_texture(ctx, t, id);
+}
+
+PT_API int pt_texture_gradient(pt_context* ctx, const float a[3], const float b[3],
+                               const float c[3], uint32_t* id) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(a) || !finite3(b) || !finite3(c))
+    return fail(ctx, PT_EINVAL, "gradient colours must be finite");
+  GpuTexture t = blank_texture(PT_TEX_GRADIENT);
+  for (int k = 0; k < 3; k++) {
+    t.c[k] = a[k];
+    t.c[3 + k] = b[k];
+    t.c[6 + k] = c[k];
+  }
+  return add_texture(ctx, t, id);
+}
+
+PT_API int pt_texture_vector(pt_context* ctx, const uint32_t* ids, int n, uint32_t* id) {
+  if (!ctx) return PT_EINVAL;
+  if (n < 0 || (n > 0 && !ids)) return fail(ctx, PT_EINVAL, "vector texture: n >= 0 ids");
+  for (int k = 0; k < n; k++)
+    if (ids[k] >= ctx->textures.size()) return fail(ctx, PT_EINVAL, "vector: unknown texture id");
+  GpuTexture t = blank_texture(PT_TEX_VECTOR);
+  t.a = (int)ctx->tex_list.size();
+  t.b = n;
+  for (int k = 0; k < n; k++) ctx->tex_list.push_back((int)ids[k]);
+  return add_texture(ctx, t, id);
+}
+
+PT_API int pt_material_set_texture(pt_context* ctx, uint32_t material, int slot,
+                                   uint32_t texture) {
+  if (!ctx) return PT_EINVAL;
+  if (material >= ctx->mats.size()) return fail(ctx, PT_EINVAL, "unknown material id");
+  if (slot < 0 || slot > 1) return fail(ctx, PT_EINVAL, "texture slot is 0 or 1");
+  if (texture >= ctx->textures.size() && texture != PT_NO_TEXTURE)
+    return fail(ctx, PT_EINVAL, "unknown texture id");
+  int t = texture == PT_NO_TEXTURE ? -1 : (int)texture;
+  (slot == 0 ? ctx->mats[material].tex0 : ctx->mats[material].tex1) = t;
+  ctx->committed = false;
+  return PT_OK;
+}
+
+PT_API int pt_mesh_set_texture_index(pt_context* ctx, uint32_t first_prim, size_t n,
+                                     const uint32_t* index) {
+  if (!ctx) return PT_EINVAL;
+  if (!index || (size_t)first_prim + n > ctx->prims.size())
+    return fail(ctx, PT_EINVAL, "texture index: primitive range out of bounds");
+  for (size_t k = 0; k < n; k++) {
+    if (ctx->prims[first_prim + k].type != PT_PRIM_TRIANGLE)
+      return fail(ctx, PT_EINVAL, "texture index: only triangles carry one");
+    if (index[k] >= (1u << 30)) return fail(ctx, PT_EINVAL, "texture index must be < 2^30");
+  }
+  for (size_t k = 0; k < n; k++) {
+    uint4& a = ctx->tri_attr[first_prim + k];
+    a.w = (a.w & 3u) | (index[k] << 2);
+  }
+  ctx->committed = false;
   return PT_OK;
 }
 
@@ -705,6 +886,15 @@ PT_API int pt_commit(pt_context* ctx) {
   std::vector<GpuLight> lights = ctx->lights;
   if (lights.empty()) lights.resize(1);
   CK(ctx->d_lights.upload(lights.data(), lights.size(), st));
+  std::vector<GpuTexture> texs = ctx->textures;
+  if (texs.empty()) texs.resize(1);
+  std::vector<float4> tdata = ctx->tex_data;
+  if (tdata.empty()) tdata.resize(1);
+  std::vector<int> tlist = ctx->tex_list;
+  if (tlist.empty()) tlist.resize(1);
+  CK(ctx->d_textures.upload(texs.data(), texs.size(), st));
+  CK(ctx->d_tex_data.upload(tdata.data(), tdata.size(), st));
+  CK(ctx->d_tex_list.upload(tlist.data(), tlist.size(), st));
   std::vector<uint4> ta = ctx->tri_attr;
   if (ta.empty()) ta.resize(1);
   CK(ctx->d_tri_attr.upload(ta.data(), ta.size(), st));
@@ -743,6 +933,9 @@ PT_API int pt_commit(pt_context* ctx) {
   S.normals = ctx->d_normals.p;
   S.uvs = ctx->d_uvs.p;
   S.leaf_of_id = ctx->d_leaf_of_id.p;
+  S.textures = ctx->d_textures.p;
+  S.tex_data = ctx->d_tex_data.p;
+  S.tex_list = ctx->d_tex_list.p;
   S.num_lights = (int)ctx->lights.size();
   S.num_prims = (int)n;
   S.miss = ctx->miss;
@@ -761,6 +954,7 @@ PT_API int pt_commit(pt_context* ctx) {
   ctx->lc = pt::default_launch(ctx->max_stack);
   ctx->lc.sort = ctx->opt.shade_order == 1 || (ctx->opt.shade_order == 0 && pth::sort_pays(ctx));
   ctx->lc.refetch = ctx->opt.refetch_lanes ? ctx->opt.refetch_lanes : pth::auto_refetch(n);
+  ctx->lc.tex = pth::uses_textures(ctx) ? 1 : 0;
   auto t1 = std::chrono::steady_clock::now();
   ctx->stats.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   ctx->stats.bvh_nodes = nn;

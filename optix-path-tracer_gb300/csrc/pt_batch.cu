@@ -415,6 +415,8 @@ static int batch_render(pt_batch* b, const pt_batch_item* items, int n, float4* 
   lc.sort = b->tune.shade_order == 1;
   if (b->tune.shade_order == 0)
     for (const ScenePart& p : b->parts) lc.sort = lc.sort || sort_pays(p.ctx);
+  lc.tex = 0;
+  for (const ScenePart& p : b->parts) lc.tex = lc.tex || uses_textures(p.ctx);
   lc.refetch = b->tune.refetch_lanes;
   if (lc.refetch == 0) {  // automatic: by the largest scene of the batch
     size_t most = 0;

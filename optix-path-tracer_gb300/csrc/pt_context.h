@@ -93,6 +93,9 @@ struct pt_context {
   std::vector<uint4> tri_attr;
   std::vector<float> normals, uvs;
   std::vector<GpuLight> lights;
+  std::vector<GpuTexture> textures;
+  std::vector<float4> tex_data;   // image texels and noise tables
+  std::vector<int> tex_list;      // vector-texture entries
   GpuMiss miss{};
   std::vector<float4> env;
   GpuCamera cam{};
@@ -102,6 +105,9 @@ struct pt_context {
   DevBuf<float4> d_prims, d_xforms, d_env;
   DevBuf<GpuMaterial> d_mats;
   DevBuf<GpuLight> d_lights;
+  DevBuf<GpuTexture> d_textures;
+  DevBuf<float4> d_tex_data;
+  DevBuf<int> d_tex_list;
   DevBuf<uint4> d_tri_attr;
   DevBuf<float> d_normals, d_uvs;
   DevBuf<uint32_t> d_leaf_of_id;
@@ -155,6 +161,8 @@ void carve_wave(WaveState& W, float4* f, uint4* u, size_t slots);
 /* 1: device memory of `device` (or managed memory), usable by its kernels;
  * 0: host memory (pageable or pinned); -1: device memory of another GPU. */
 int device_ptr_kind(const void* p, int device);
+/* Whether some material of the scene takes a texture. */
+bool uses_textures(const pt_context* ctx);
 /* Whether shading in material-sorted tiles pays for this scene: it does when
  * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
  * is present, whose code paths diverge most in a mixed warp. */

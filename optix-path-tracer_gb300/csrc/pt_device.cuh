@@ -304,6 +304,7 @@ PTD bool tri_candidate(const PrimRec& p, V3 o, const WtRay& w, float tmin, float
 // ------------------------------------------------------------ hit record --
 struct HitRecord {
   uint32_t index;  // material id
+  int tindex;      // texture index: the face's (mesh.hpp material_buffer), 0 for analytic shapes
   V3 P;
   float u, v;
   V3 geometric_normal, shading_normal, Wo;
@@ -312,8 +313,8 @@ struct HitRecord {
 // Get_HitRecord of each primitive: programs/hitables/{sphere,aarect,box,
 // triangle}.cu, from the object-space ray, mapped to world space once.
 // need_uv: texture coordinates are computed only when a texture reads them
-// (the materials here use constant colours, so the shading kernels pass
-// false; u, v feed nothing else).
+// (the shading kernels pass false and compute them out of line, in
+// textured_colours, for textured materials only; u, v feed nothing else).
 PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, float t_hit,
                          float bu, float bv, bool need_uv = true) {
   HitRecord rec;
@@ -327,6 +328,7 @@ PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, floa
     d = xvector(I, rd);
   }
   rec.index = prim_material(p);
+  rec.tindex = 0;
   int type = prim_type(p);
   if (type == PT_PRIM_SPHERE) {
     V3 center = v3(p.r0.x, p.r0.y, p.r0.z);
@@ -389,6 +391,7 @@ PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, floa
     Ng = normalize(normalize(Ng));
     rec.geometric_normal = Ng;
     uint4 at = __ldg(S.tri_attr + prim_id(p));
+    rec.tindex = (int)(at.w >> 2);
     if (!(at.w & 1u)) {
       rec.shading_normal = Ng;
     } else {
@@ -973,6 +976,119 @@ PTD V3 sphere_light_sample_c(const GpuLight& L, V3 P, uint32_t& seed) {
 }
 
 PTD float power_mis(float a, float b) { return (a * a) / (a * a + b * b); }
+
+
+// ------------------------------------------------------------ textures ----
+// Bilinear lookup with repeat wrap of float4 texels (row 0 at v = 0): the
+// software stand-in for OptiX's hardware texture filtering (environment and
+// image textures alike).
+PTD V3 bilinear_rgb(const float4* texels, int w, int h, float u, float v) {
+  if (!(u == u) || !(v == v) || fabsf(u) > 1e6f || fabsf(v) > 1e6f) return v3(0.f);
+  float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+  float fx = ptm_floor(x), fy = ptm_floor(y);
+  float ax = x - fx, ay = y - fy;
+  int ix0 = (int)fx % w; if (ix0 < 0) ix0 += w;
+  int iy0 = (int)fy % h; if (iy0 < 0) iy0 += h;
+  int ix1 = ix0 + 1 == w ? 0 : ix0 + 1;
+  int iy1 = iy0 + 1 == h ? 0 : iy0 + 1;
+  V3 c00 = f4xyz(texels[iy0 * w + ix0]), c10 = f4xyz(texels[iy0 * w + ix1]);
+  V3 c01 = f4xyz(texels[iy1 * w + ix0]), c11 = f4xyz(texels[iy1 * w + ix1]);
+  return (c00 * (1.f - ax) + c10 * ax) * (1.f - ay) + (c01 * (1.f - ax) + c11 * ax) * ay;
+}
+
+// programs/textures/noise_texture.cu:12-59: Perlin noise over the texture's
+// tables (ranvec: 256 vectors, then perm_x, perm_y, perm_z: 256 ints each).
+PTD float perlin_noise(const float4* D, V3 p) {
+  const int* perm = (const int*)(D + 256);
+  float u = p.x - ptm_floor(p.x);
+  float v = p.y - ptm_floor(p.y);
+  float w = p.z - ptm_floor(p.z);
+  int i = (int)ptm_floor(p.x);
+  int j = (int)ptm_floor(p.y);
+  int k = (int)ptm_floor(p.z);
+  float uu = u * u * (3 - 2 * u);
+  float vv = v * v * (3 - 2 * v);
+  float ww = w * w * (3 - 2 * w);
+  float accum = 0;
+  for (int di = 0; di < 2; di++)
+    for (int dj = 0; dj < 2; dj++)
+      for (int dk = 0; dk < 2; dk++) {
+        int r = perm[(i + di) & 255] ^ perm[256 + ((j + dj) & 255)] ^ perm[512 + ((k + dk) & 255)];
+        V3 c = f4xyz(D[r]);
+        V3 weight_v = v3(u - di, v - dj, w - dk);
+        accum += (di * uu + (1 - di) * (1 - uu)) * (dj * vv + (1 - dj) * (1 - vv)) *
+                 (dk * ww + (1 - dk) * (1 - ww)) * dot(c, weight_v);
+      }
+  return accum;
+}
+
+// noise_texture.cu:61-76: seven octaves of turbulence.
+PTD float perlin_turb(const float4* D, V3 p) {
+  float accum = 0;
+  V3 temp_p = p;
+  float weight = 1.0f;
+  for (int i = 0; i < 7; i++) {
+    accum += weight * perlin_noise(D, temp_p);
+    weight *= 0.5f;
+    temp_p *= 2.f;
+  }
+  return fabsf(accum);
+}
+
+// A texture's colour at (u, v, P) with texture index i (the callable
+// sample_texture(u, v, p, i) of programs/textures/*.cu).  Checker and vector
+// textures hand over to another texture (with index 0, as
+// checkered_texture.cu:11-14 and vector.cu:7-12 call it); the chain is
+// bounded (ids only decrease along it).
+PTD V3 texture_color(const DevScene& S, int id, float u, float v, V3 p, int i) {
+  for (int hop = 0; hop < 64; hop++) {
+    const GpuTexture& t = S.textures[id];
+    switch (t.kind) {
+      case PT_TEX_CONSTANT:  // constant_texture.cu:5-7
+        return v3(t.c[0], t.c[1], t.c[2]);
+      case PT_TEX_CHECKER: {  // checkered_texture.cu:8-15
+        float sines = pt_sinf(10 * p.x) * pt_sinf(10 * p.y) * pt_sinf(10 * p.z);
+        id = sines < 0 ? t.a : t.b;
+        i = 0;
+        break;
+      }
+      case PT_TEX_VECTOR:  // vector.cu:7-12
+        if (i >= t.b || i < 0) return v3(0.f);
+        id = S.tex_list[t.a + i];
+        i = 0;
+        break;
+      case PT_TEX_NOISE: {  // noise_texture.cu:61-76: the switch has no breaks, so
+                            // every axis ends in the Z case
+        float scale = t.c[0];
+        float sinValue = pt_sinf(scale * p.z + 5 * perlin_turb(S.tex_data + t.data, scale * p));
+        return v3(1.f) * 0.5f * (1 + sinValue);
+      }
+      case PT_TEX_IMAGE:  // image_texture.cu:3-7 (texels normalised to [0, 1])
+        return bilinear_rgb(S.tex_data + t.data, t.a, t.b, u, v);
+      default: {  // PT_TEX_GRADIENT, gradient_texture.cu:7-14
+        V3 unit_direction = normalize(p);
+        float x = fabsf(unit_direction.x), y = fabsf(unit_direction.y),
+              z = fabsf(unit_direction.z);
+        return x * v3(t.c[0], t.c[1], t.c[2]) + y * v3(t.c[3], t.c[4], t.c[5]) +
+               z * v3(t.c[6], t.c[7], t.c[8]);
+      }
+    }
+  }
+  return v3(0.f);
+}
+
+// The material's colours at a hit: Get_Parameters of the closest-hit
+// programs (e.g. lambertian.cu:29-38) with textures in place of constants.
+PTD void resolve_textures(const DevScene& S, GpuMaterial& m, float u, float v, V3 p, int i) {
+  if (m.tex0 >= 0) {
+    V3 c = texture_color(S, m.tex0, u, v, p, i);
+    m.c0x = c.x; m.c0y = c.y; m.c0z = c.z;
+  }
+  if (m.tex1 >= 0) {
+    V3 c = texture_color(S, m.tex1, u, v, p, i);
+    m.c1x = c.x; m.c1y = c.y; m.c1z = c.z;
+  }
+}
 
 }  // namespace ptd
 

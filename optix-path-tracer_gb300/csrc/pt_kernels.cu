@@ -199,24 +199,26 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
   bool started = false;
   uint32_t nn = 0, np = 0;
 
-  // per-lane ray state
-  V3 o = v3(0.f), d = v3(0.f);
-  float tmin = 0.f, tmax = 0.f, ix = 0.f, iy = 0.f, iz = 0.f, tbest = 0.f;
+  // per-lane ray state (the direction and tmax of a lane's ray live in the
+  // warp's shared copy, ws.rd[lane]: the node tests need only o, tmin and
+  // the reciprocal direction)
+  const uint32_t parity = MODE == TRACE_EXT ? c.parity : 0u;
+  V3 o = v3(0.f);
+  float tmin = 0.f, ix = 0.f, iy = 0.f, iz = 0.f, tbest = 0.f;
   bool negx = false, negy = false, negz = false;
-  uint32_t cur = 0, best_id = PT_NO_HIT, slot = 0;
+  uint32_t cur = 0, best_id = PT_NO_HIT;
   int sp = 0;
   bool active = false;
 
-  auto load_ray = [&]() {
+  // loads ray i into o, d, tmin, tmax
+  auto load_ray = [&](V3& d, float& tmax) {
     if (MODE == TRACE_EXT) {
-      slot = i;
-      float4 ro = W.path[c.parity].ray_o[i], rdv = W.path[c.parity].ray_d[i];
+      float4 ro = W.path[parity].ray_o[i], rdv = W.path[parity].ray_d[i];
       o = f4xyz(ro);
       d = f4xyz(rdv);
       tmin = ro.w;
       tmax = rdv.w;
     } else if (SHADOWRAY) {
-      slot = i;
       o = f4xyz(W.sh.P[i]);
       d = f4xyz(W.sh.Wi[i]);
       tmin = 1e-3f;
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     }
   };
 
-  auto finish = [&]() {
+  auto finish = [&](V3 d, float tmax) {
     if (MODE == TRACE_EXT) {
       float4 h = make_float4(tmax, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
       if (best_id != PT_NO_HIT) {
@@ -242,7 +244,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         if (prim_type(p) == PT_PRIM_TRIANGLE) tri_candidate(p, o, wt_setup(d), tmin, tmax, t, bu, bv);
         h = make_float4(tbest, bu, bv, __uint_as_float(leaf));
       }
-      W.hit[slot] = h;
+      W.hit[i] = h;
     } else if (SHADOWRAY) {
       bool occluded = true;
       if (consistent) {
@@ -250,9 +252,9 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       } else if (best_id != PT_NO_HIT) {
         PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
         bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
-        occluded = !(is_light && dot(f4xyz(W.sh.N[slot]), d) > 0.f);
+        occluded = !(is_light && dot(f4xyz(W.sh.N[i]), d) > 0.f);
       }
-      W.sh.Wi[slot].w = occluded ? 1.f : 0.f;
+      W.sh.Wi[i].w = occluded ? 1.f : 0.f;
     } else {
       if (best_id == PT_NO_HIT) {
         fo.prim[i] = PT_NO_HIT;
@@ -267,6 +269,11 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     }
   };
 
+  auto finish_traced = [&]() {
+    float4 rdv = ws.rd[lane];
+    finish(f4xyz(rdv), rdv.w);
+  };
+
   bool idle = true;  // wants a ray (finished one, or none taken yet)
   // loads ray i (< n) and sets up its traversal
   auto fetch = [&]() {
@@ -274,13 +281,15 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     // primitive test fails or yields a NaN distance, which never wins the
     // closest-hit minimum), and neither does any ray of an empty scene: both
     // end here, without a traversal (a NaN ray would pass every box test)
-    load_ray();
+    V3 d;
+    float tmax;
+    load_ray(d, tmax);
     bool nan = !(o.x == o.x && o.y == o.y && o.z == o.z && d.x == d.x && d.y == d.y &&
                  d.z == d.z);
     if (nan || S.num_prims == 0) {
       best_id = PT_NO_HIT;
       tbest = tmax;
-      finish();
+      finish(d, tmax);
       active = false;
       idle = true;
       return;
@@ -307,7 +316,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
     cur = S.root;
     if (BATCH) {
-      uint32_t z = MODE == TRACE_EXT ? W.path[c.parity].st[i].z : W.sh.st[i].z;
+      uint32_t z = MODE == TRACE_EXT ? W.path[parity].st[i].z : W.sh.st[i].z;
       cur = __ldg(br.roots + (z >> PT_ST_SCENE_SHIFT));
     }
     sp = 0;
@@ -422,6 +431,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       float4 w4 = ws.wt[lane];
       WtRay wt = wt_unpack(w4);
       unsigned long long bk = ws.best[lane];
+      const float4 rdv = ws.rd[lane];
       while (m) {
         int k = __ffs(m) - 1;
         m &= m - 1;
@@ -431,7 +441,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
           PrimRec p = load_prim(S.prims, first + q);
           if (COUNT) np++;
           float t, bu, bv;
-          if (prim_test(S, p, o, d, wt, tmin, tmax, t, bu, bv)) {
+          if (prim_test(S, p, o, f4xyz(rdv), wt, tmin, rdv.w, t, bu, bv)) {
             unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
             bk = min(bk, key);
           }
@@ -486,7 +496,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     // ---- consistent-mode shadow rays ask only whether anything lies before
     // tmax: the first confirmed hit ends the ray
     if (consistent && active && best_id != PT_NO_HIT) {
-      finish();
+      finish_traced();
       active = false;
       idle = true;
     }
@@ -501,7 +511,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
           if (sp >= max_stack) {
             atomicOr(&W.ctr->error, 1u);
             sp = 0;  // abandon this ray (the host reports the error)
-            finish();
+            finish_traced();
             active = false;
             idle = true;
           } else {
@@ -516,7 +526,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         if (e.y == 0) sp--;
         else stk[(sp - 1) * bd].y = e.y;
       } else {
-        finish();
+        finish_traced();
         active = false;
         idle = true;
       }
@@ -540,7 +550,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         if (sp >= max_stack) {
           atomicOr(MODE == TRACE_FIRST ? fo.err : &W.ctr->error, 1u);
           sp = 0;  // abandon this ray (the host reports the error)
-          finish();
+          finish_traced();
           active = false;
           idle = true;
         } else {
@@ -567,7 +577,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
           break;
         }
         if (!found) {
-          finish();
+          finish_traced();
           active = false;
           idle = true;
         }
@@ -838,6 +848,16 @@ __device__ __forceinline__ V3 env_lookup(const GpuMiss& ms, float u, float v) {
   return (c00 * (1.f - ax) + c10 * ax) * (1.f - ay) + (c01 * (1.f - ax) + c11 * ax) * ay;
 }
 
+// The colours of a textured material at a hit (Get_Parameters of the
+// closest-hit programs).  Compiled only into the shading kernels of scenes
+// with textures (the TEX variants): untextured shading never computes the
+// texture coordinates.
+__device__ __forceinline__ void apply_textures(const DevScene& S, GpuMaterial& m, const PrimRec& p,
+                                               V3 ro, V3 rd, float t, float bu, float bv) {
+  HitRecord rec = hit_record(S, p, ro, rd, t, bu, bv, true);
+  resolve_textures(S, m, rec.u, rec.v, rec.P, rec.tindex);
+}
+
 // programs/miss.cu:30-95; returns the multiplier applied to throughput.
 __device__ __forceinline__ V3 miss_color(const GpuMiss& ms, V3 d) {
   if (ms.type == 0) {
@@ -955,7 +975,7 @@ __device__ __forceinline__ void sort_tile(SortTile& t, const DevScene& S0,
 
 // One path of k_shade (position i of the current buffer; all lanes of the
 // warp call it together: the queue appends are warp-aggregated).
-template <bool BATCH>
+template <bool BATCH, bool TEX>
 __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& W,
                                          const WaveCounters& c, const WaveCtl& ctl,
                                          const BatchRefs& br, uint32_t i, bool active) {
@@ -971,6 +991,8 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
   float lightPDF = 0.f;
   int lindex = 0;
   uint32_t mid = 0;
+  bool textured = false;  // the material's colours come from textures
+  V3 tcol = v3(0.f);      // its colour at this hit (k_finish needs it for Direct_Light)
   if (active) st = pb.st[i];
   const DevScene& S = path_scene<BATCH>(S0, br, st.z);
   if (active) {
@@ -989,6 +1011,11 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
       HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, false);
       mid = rec.index;
       GpuMaterial m = S.mats[mid];
+      textured = TEX && (m.tex0 >= 0 || m.tex1 >= 0);
+      if (textured) {
+        apply_textures(S, m, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z);
+        tcol = v3(m.c0x, m.c0y, m.c0z);
+      }
       P = rec.P;
       Wo = rec.Wo;
       N = rec.shading_normal;
@@ -1076,6 +1103,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
     W.sh.N[spos] = make_float4(N.x, N.y, N.z, __int_as_float(lindex));
     W.sh.Wo[spos] = make_float4(Wo.x, Wo.y, Wo.z, __uint_as_float(mid));
     W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
+    if (textured) W.sh.C[spos] = make_float4(tcol.x, tcol.y, tcol.z, 0.f);
     W.sh.st[spos] = st;
     W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
     W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
@@ -1084,7 +1112,9 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
   path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, tail);
 }
 
-template <bool BATCH, bool SORT>
+// TEX: the scene has textured materials (their colours are evaluated at
+// the hit); the other variant carries no texture code at all.
+template <bool BATCH, bool SORT, bool TEX>
 __global__ void __launch_bounds__(PT_SHADE_BLOCK, PT_SHADE_MINBLOCKS) k_shade(DevScene S0, WaveState W,
                                                           const WaveCtl* __restrict__ ctlp,
                                                           BatchRefs br) {
@@ -1092,7 +1122,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK, PT_SHADE_MINBLOCKS) k_shade(De
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
-  SHADE_LOOP(shade_path<BATCH>(S0, W, c, ctl, br, i, i < n))
+  SHADE_LOOP((shade_path<BATCH, TEX>(S0, W, c, ctl, br, i, i < n)))
 }
 
 template <bool BATCH>
@@ -1119,6 +1149,12 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S0, WaveStat
       rad = f4xyz(W.sh.rad[i]);
       float4 P4 = W.sh.P[i], N4 = W.sh.N[i], Wo4 = W.sh.Wo[i], Wi4 = W.sh.Wi[i];
       GpuMaterial m = S.mats[__float_as_uint(Wo4.w)];
+      if (m.tex0 >= 0) {  // the colour its texture gave at the hit (k_shade): NEE materials
+        float4 c4 = W.sh.C[i];  // (Lambertian, Oren-Nayar, diffuse light) read only c0
+        m.c0x = c4.x;
+        m.c0y = c4.y;
+        m.c0z = c4.z;
+      }
       V3 P = f4xyz(P4), N = f4xyz(N4), Wo = f4xyz(Wo4);
       V3 direct = nee_end(S, m, st.x, P, Wo, N, f4xyz(Wi4), P4.w, __float_as_int(N4.w),
                           Wi4.w != 0.f);
@@ -1189,7 +1225,7 @@ __device__ __forceinline__ void guide_end(const WaveState& W, uint32_t pid, floa
 // (the guide of this position from k_guide_infer) and that mixture density is
 // the MIS partner of NEE and of emitter hits at the next vertex.  One path of
 // k_shade_c (see shade_path).
-template <bool BATCH, bool GUIDE>
+template <bool BATCH, bool GUIDE, bool TEX>
 __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState& W,
                                            const WaveCounters& c, const WaveCtl& ctl,
                                            const BatchRefs& br, uint32_t i, bool active) {
@@ -1225,6 +1261,8 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
       PrimRec p = load_prim(S.prims, leaf);
       HitRecord rec = hit_record(S, p, f4xyz(ro), d, hit.x, hit.y, hit.z, false);
       GpuMaterial m = S.mats[rec.index];
+      if (TEX && (m.tex0 >= 0 || m.tex1 >= 0))
+        apply_textures(S, m, p, f4xyz(ro), d, hit.x, hit.y, hit.z);
       P = rec.P;
       V3 Wo = rec.Wo, N = rec.shading_normal;
       if (m.type == PT_MAT_DIFFUSE_LIGHT) {
@@ -1388,7 +1426,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
   path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended, cw);
 }
 
-template <bool BATCH, bool SORT, bool GUIDE>
+template <bool BATCH, bool SORT, bool GUIDE, bool TEX>
 __global__ void __launch_bounds__(PT_SHADE_BLOCK, PT_SHADE_MINBLOCKS) k_shade_c(DevScene S0, WaveState W,
                                                             const WaveCtl* __restrict__ ctlp,
                                                             BatchRefs br) {
@@ -1396,7 +1434,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK, PT_SHADE_MINBLOCKS) k_shade_c(
   WaveCounters c = *W.ctr;
   WaveCtl ctl = *ctlp;
   uint32_t n = c.n_cur + gen_count(c, ctl, (uint32_t)W.slots);
-  SHADE_LOOP((shade_c_path<BATCH, GUIDE>(S0, W, c, ctl, br, i, i < n)))
+  SHADE_LOOP((shade_c_path<BATCH, GUIDE, TEX>(S0, W, c, ctl, br, i, i < n)))
 }
 
 __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveState W,
@@ -1727,7 +1765,7 @@ int wave_grid(int kind, int max_stack, int block) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace_t<TRACE_EXT, false, false>,
                                                       block, trace_smem(max_stack, block));
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false, true>, block, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false, true, false>, block, 0);
   if (e != cudaSuccess || blocks < 1) {
     cudaGetLastError();
     blocks = 1;
@@ -1741,6 +1779,7 @@ LaunchCfg default_launch(int max_stack) {
   lc.shade_block = PT_SHADE_BLOCK;
   lc.sort = 1;
   lc.refetch = 32;
+  lc.tex = 0;
   lc.trace_grid = wave_grid(0, max_stack, lc.trace_block);
   lc.shade_grid = wave_grid(1, max_stack, lc.shade_block);
   return lc;
@@ -1786,6 +1825,23 @@ cudaError_t set_trace_smem() {
   return cudaSuccess;
 }
 
+// The shading kernel of the integrator mode, guide, tile order and texture
+// variant.
+template <bool BATCH, bool TEX>
+static void launch_shade(const DevScene& S, const WaveState& W, const WaveCtl* ctl, BatchRefs br,
+                         int mode, bool guide, int sort, int tgs, int sg, int sb, cudaStream_t st) {
+  if (mode == 1 && guide) {
+    if (sort) k_shade_c<BATCH, true, true, TEX><<<tgs, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade_c<BATCH, false, true, TEX><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  } else if (mode == 1) {
+    if (sort) k_shade_c<BATCH, true, false, TEX><<<tgs, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade_c<BATCH, false, false, TEX><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  } else {
+    if (sort) k_shade<BATCH, true, TEX><<<tgs, sb, 0, st>>>(S, W, ctl, br);
+    else k_shade<BATCH, false, TEX><<<sg, sb, 0, st>>>(S, W, ctl, br);
+  }
+}
+
 template <bool BATCH>
 static void launch_iteration_t(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                                int max_stack, bool counters, const LaunchCfg& lc, cudaStream_t st,
@@ -1810,17 +1866,11 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
   else
     k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
-  if (mode == 1 && gi) {
-    launch_guide_infer(S, W, ctl, *gi, 2 * num_sms(), st);
-    if (lc.sort) k_shade_c<BATCH, true, true><<<tgs, sb, 0, st>>>(S, W, ctl, br);
-    else k_shade_c<BATCH, false, true><<<sg, sb, 0, st>>>(S, W, ctl, br);
-  } else if (mode == 1) {
-    if (lc.sort) k_shade_c<BATCH, true, false><<<tgs, sb, 0, st>>>(S, W, ctl, br);
-    else k_shade_c<BATCH, false, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
-  } else {
-    if (lc.sort) k_shade<BATCH, true><<<tgs, sb, 0, st>>>(S, W, ctl, br);
-    else k_shade<BATCH, false><<<sg, sb, 0, st>>>(S, W, ctl, br);
-  }
+  if (mode == 1 && gi) launch_guide_infer(S, W, ctl, *gi, 2 * num_sms(), st);
+  if (lc.tex)
+    launch_shade<BATCH, true>(S, W, ctl, br, mode, gi != nullptr, lc.sort, tgs, sg, sb, st);
+  else
+    launch_shade<BATCH, false>(S, W, ctl, br, mode, gi != nullptr, lc.sort, tgs, sg, sb, st);
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
   if (mode == 1 && counters)
     k_trace_t<TRACE_OCCLUDED, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);

@@ -53,6 +53,27 @@ struct GpuMaterial {
   float c0x, c0y, c0z;  /* colour / albedo / diffuse / base */
   float c1x, c1y, c1z;  /* specular / extinction */
   float p0, p1;         /* fuzz | ref_idx,density | rA,rB | nu,nv */
+  int tex0, tex1;       /* texture ids of c0 / c1, or -1 for the constant colour */
+  int pad;
+};
+
+/* Texture callables (programs/textures/, host_includes/textures.hpp): a
+ * texture maps (u, v, P, index) to a colour.  Checker and vector textures
+ * name other textures (ids below their own: the graph has no cycles). */
+#define PT_TEX_CONSTANT 0
+#define PT_TEX_CHECKER 1
+#define PT_TEX_NOISE 2
+#define PT_TEX_IMAGE 3
+#define PT_TEX_GRADIENT 4
+#define PT_TEX_VECTOR 5
+
+struct GpuTexture {
+  int kind;
+  int a, b;     /* checker: odd, even ids; vector: first list entry, size; image: w, h;
+                   noise: axis */
+  int data;     /* image: first texel in tex_data; noise: ranvec (256 float4) then
+                   perm_x, perm_y, perm_z (64 float4 each, 4 ints per float4) */
+  float c[9];   /* constant: c[0..2]; gradient: colorA, colorB, colorC; noise: scale */
   int pad[3];
 };
 
@@ -88,7 +109,8 @@ struct DevScene {
   const GpuMaterial* mats;
   const GpuLight* lights;
   const uint4* tri_attr;    /* per prim id: absolute attribute-vertex indices (x,y,z),
-                               .w bit0 = has normals, bit1 = has uvs */
+                               .w bit0 = has normals, bit1 = has uvs, bits 2-31 the
+                               face's texture index (mesh.hpp material_buffer) */
   const float* normals;     /* 3 floats per attribute vertex */
   const float* uvs;         /* 2 floats per attribute vertex */
   const uint32_t* leaf_of_id; /* primitive id -> position in the leaf-ordered records */
@@ -99,6 +121,9 @@ struct DevScene {
   int num_prims;
   uint32_t root;            /* BVH8 node where traversal starts (0 for one scene) */
   int pad;
+  const GpuTexture* textures;
+  const float4* tex_data;   /* image texels (rgba, row 0 at v = 0) and noise tables */
+  const int* tex_list;      /* entries of vector textures */
   GpuMiss miss;
   GpuCamera cam;
 };

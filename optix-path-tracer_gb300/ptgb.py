@@ -24,6 +24,7 @@ MISS_GRADIENT, MISS_CONSTANT, MISS_HDR, MISS_IMG = 0, 1, 2, 3
 MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_DIFFUSE_LIGHT = 0, 1, 2, 3
 MAT_OREN_NAYAR, MAT_TORRANCE_SPARROW, MAT_ASHIKHMIN_SHIRLEY = 4, 5, 6
 PRIM_TRIANGLE, PRIM_SPHERE, PRIM_RECT, PRIM_BOX = 0, 1, 2, 3
+TEX_CONSTANT, TEX_CHECKER, TEX_NOISE, TEX_IMAGE, TEX_GRADIENT, TEX_VECTOR = 0, 1, 2, 3, 4, 5
 NO_HIT = 0xFFFFFFFF
 
 STATUS = {0: "PT_OK", -1: "PT_EINVAL", -2: "PT_ENOMEM", -3: "PT_ECUDA", -4: "PT_ETIMEOUT",
@@ -87,6 +88,15 @@ SIGNATURES = {
     "pt_material_oren_nayar": [_P, _F3, ctypes.c_float, _U32P],
     "pt_material_torrance_sparrow": [_P, _F3, ctypes.c_float, ctypes.c_float, _U32P],
     "pt_material_ashikhmin_shirley": [_P, _F3, _F3, ctypes.c_float, ctypes.c_float, _U32P],
+    "pt_texture_constant": [_P, _F3, _U32P],
+    "pt_texture_checker": [_P, ctypes.c_uint32, ctypes.c_uint32, _U32P],
+    "pt_texture_noise": [_P, ctypes.c_float, ctypes.c_int, _P, _P, _U32P],
+    "pt_noise_tables": [_P, _P],
+    "pt_texture_image": [_P, _P, ctypes.c_int, ctypes.c_int, _U32P],
+    "pt_texture_gradient": [_P, _F3, _F3, _F3, _U32P],
+    "pt_texture_vector": [_P, _P, ctypes.c_int, _U32P],
+    "pt_material_set_texture": [_P, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint32],
+    "pt_mesh_set_texture_index": [_P, ctypes.c_uint32, ctypes.c_size_t, _P],
     "pt_add_sphere": [_P, _F3, ctypes.c_float, ctypes.c_uint32, _P, _U32P],
     "pt_add_rect": [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                     ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, _P, _U32P],
@@ -302,6 +312,9 @@ class Scene:
 
     def __init__(self):
         self.materials = []   # (kind, c0, c1, p0, p1)
+        self.textures = []    # (kind, a, b, c[9], data, perm, ids)
+        self.mat_textures = []  # (material, slot, texture) in call order
+        self.tex_index = {}   # mesh item index -> per-face texture index (uint32)
         self.items = []       # ("sphere"|"rect"|"box"|"mesh", args...)
         self.add_obj = {}     # item index -> (ObjMesh, material or None): load with pt_add_obj
         self.lights = []      # ("rect"|"sphere", args..., emission)
@@ -340,6 +353,45 @@ class Scene:
                                float(nv)))
         return len(self.materials) - 1
 
+    # textures (host_includes/textures.hpp)
+    def _texture(self, kind, a=0, b=0, c=(), data=None, perm=None, ids=None):
+        cc = np.zeros(9, np.float32)
+        cc[:len(c)] = c
+        self.textures.append((kind, int(a), int(b), cc, data, perm, ids))
+        return len(self.textures) - 1
+
+    def texture_constant(self, rgb):
+        return self._texture(TEX_CONSTANT, c=tuple(rgb))
+
+    def texture_checker(self, odd, even):
+        return self._texture(TEX_CHECKER, odd, even)
+
+    def texture_noise(self, scale, axis=PT_X_AXIS, ranvec=None, perm=None):
+        """Perlin noise; null tables are the library's defaults (those the
+        reference's host class makes with std::mt19937 seeded 0)."""
+        if ranvec is None or perm is None:
+            r0, p0 = noise_tables()
+            ranvec = r0 if ranvec is None else ranvec
+            perm = p0 if perm is None else perm
+        ranvec = np.ascontiguousarray(ranvec, np.float32).reshape(768)
+        perm = np.ascontiguousarray(perm, np.int32).reshape(768)
+        return self._texture(TEX_NOISE, axis, 0, (float(scale),), ranvec, perm)
+
+    def texture_image(self, rgba):
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        assert rgba.ndim == 3 and rgba.shape[2] == 4
+        return self._texture(TEX_IMAGE, rgba.shape[1], rgba.shape[0], data=rgba)
+
+    def texture_gradient(self, a, b, c):
+        return self._texture(TEX_GRADIENT, c=tuple(a) + tuple(b) + tuple(c))
+
+    def texture_vector(self, ids):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        return self._texture(TEX_VECTOR, 0, len(ids), ids=ids)
+
+    def set_texture(self, material, slot, texture):
+        self.mat_textures.append((int(material), int(slot), int(texture)))
+
     # geometry (host_includes/hitables.hpp, mesh.hpp)
     def sphere(self, center, radius, mat, xform=None):
         self.items.append(("sphere", tuple(center), float(radius), mat, xform))
@@ -356,7 +408,8 @@ class Scene:
         self.n_prims += 1
         return self.n_prims - 1
 
-    def mesh(self, verts, idx, mat, mat_per_tri=None, normals=None, uvs=None, xform=None):
+    def mesh(self, verts, idx, mat, mat_per_tri=None, normals=None, uvs=None, xform=None,
+             tex_index=None):
         verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
         if mat_per_tri is not None:
@@ -366,6 +419,8 @@ class Scene:
         if uvs is not None:
             uvs = np.ascontiguousarray(uvs, dtype=np.float32).reshape(-1, 2)
         self.items.append(("mesh", verts, idx, mat, mat_per_tri, normals, uvs, xform))
+        if tex_index is not None:
+            self.tex_index[len(self.items) - 1] = np.ascontiguousarray(tex_index, np.uint32)
         first = self.n_prims
         self.n_prims += len(idx)
         return first
@@ -418,6 +473,17 @@ class Scene:
                        float(aperture), float(focus), float(t0), float(t1))
 
 
+def noise_tables():
+    """The default Perlin tables of pt_texture_noise: ranvec (256, 3) float32,
+    perm (3, 256) int32."""
+    lib = load_library()
+    r = np.zeros((256, 3), np.float32)
+    p = np.zeros((3, 256), np.int32)
+    if lib.pt_noise_tables(_ptr(r), _ptr(p)) != 0:
+        raise PtError(-1, "pt_noise_tables failed")
+    return r, p
+
+
 def _check(lib, ctx, rc):
     if rc != 0:
         raise PtError(rc, lib.pt_last_error(ctx).decode())
@@ -455,6 +521,22 @@ class GpuRenderer:
 
     def load(self, scene):
         L, c = self.lib, self.ctx
+        for kind, a, b, cc, data, perm, ids in getattr(scene, "textures", []):
+            tid = ctypes.c_uint32()
+            if kind == TEX_CONSTANT:
+                self._c(L.pt_texture_constant(c, f3(cc[:3]), ctypes.byref(tid)))
+            elif kind == TEX_CHECKER:
+                self._c(L.pt_texture_checker(c, a, b, ctypes.byref(tid)))
+            elif kind == TEX_NOISE:
+                self._c(L.pt_texture_noise(c, float(cc[0]), a, _ptr(data), _ptr(perm),
+                                           ctypes.byref(tid)))
+            elif kind == TEX_IMAGE:
+                self._c(L.pt_texture_image(c, _ptr(data), a, b, ctypes.byref(tid)))
+            elif kind == TEX_GRADIENT:
+                self._c(L.pt_texture_gradient(c, f3(cc[0:3]), f3(cc[3:6]), f3(cc[6:9]),
+                                              ctypes.byref(tid)))
+            else:
+                self._c(L.pt_texture_vector(c, _ptr(ids), b, ctypes.byref(tid)))
         mids = []
         for kind, c0, c1, p0, p1 in scene.materials:
             mid = ctypes.c_uint32()
@@ -474,6 +556,9 @@ class GpuRenderer:
                 self._c(L.pt_material_ashikhmin_shirley(c, f3(c0), f3(c1), p0, p1,
                                                         ctypes.byref(mid)))
             mids.append(mid.value)
+        for m, slot, t in getattr(scene, "mat_textures", []):
+            self._c(L.pt_material_set_texture(c, mids[m], slot, t))
+        tex_index = getattr(scene, "tex_index", {})
         add_obj = getattr(scene, "add_obj", {})
         for k, it in enumerate(scene.items):
             pid = ctypes.c_uint32()
@@ -498,6 +583,9 @@ class GpuRenderer:
                 self._c(L.pt_add_mesh(c, _ptr(v), len(v), _ptr(idx), len(idx), _ptr(mpt),
                                       mids[m] if m is not None else 0, _ptr(nrm), _ptr(uv),
                                       _ptr(xf), ctypes.byref(pid)))
+                if k in tex_index:
+                    ti = tex_index[k]
+                    self._c(L.pt_mesh_set_texture_index(c, pid.value, len(ti), _ptr(ti)))
         for lt in scene.lights:
             if lt[0] == "rect":
                 _, (a0, a1, b0, b1, k), axis, e = lt
@@ -1032,3 +1120,64 @@ def main(argv=None):
 
 if __name__ == "__main__":
     main()
+
+
+def checker_image(w=64, h=32, seed=7):
+    """A small seeded RGBA float image (row 0 at v = 0) for image textures."""
+    rng = SplitMix64(seed)
+    img = np.zeros((h, w, 4), np.float32)
+    for y in range(h):
+        for x in range(w):
+            base = 0.8 if ((x // 8) + (y // 8)) % 2 else 0.2
+            img[y, x, :3] = (base * (0.5 + 0.5 * rng.uniform()), base * x / w, base * y / h)
+    img[..., 3] = 1.0
+    return img
+
+
+def texture_zoo(width=96, height=72):
+    """Every texture callable of the reference on every material it can
+    colour: checker (of a checker), Perlin noise, an image, a gradient, and a
+    vector texture indexed per face on a heightfield mesh with uvs; textured
+    Lambertian, Oren-Nayar, metal, dielectric, Torrance-Sparrow,
+    Ashikhmin-Shirley (both colours) and an emitter; a rect light and a
+    gradient sky."""
+    s = Scene()
+    red = s.texture_constant((0.8, 0.1, 0.1))
+    white = s.texture_constant((0.9, 0.9, 0.9))
+    fine = s.texture_checker(red, white)
+    blue = s.texture_constant((0.1, 0.2, 0.8))
+    check = s.texture_checker(fine, blue)
+    noise = s.texture_noise(4.0, PT_Y_AXIS)
+    image = s.texture_image(checker_image())
+    grad = s.texture_gradient((0.9, 0.2, 0.2), (0.2, 0.9, 0.2), (0.2, 0.2, 0.9))
+    vec = s.texture_vector([check, noise, image, grad])
+    lam = s.lambertian((0.5, 0.5, 0.5))
+    s.set_texture(lam, 0, vec)
+    mats = []
+    for k, (ctor, args) in enumerate([
+            (s.lambertian, ((0.5, 0.5, 0.5),)), (s.oren_nayar, ((0.6, 0.6, 0.6), 0.3)),
+            (s.metal, ((0.8, 0.8, 0.8), 0.1)),
+            (s.dielectric, ((1.0, 1.0, 1.0), (0.5, 0.5, 0.5), 1.5)),
+            (s.torrance_sparrow, ((0.9, 0.6, 0.3), 0.3, 0.3)),
+            (s.ashikhmin_shirley, ((0.5, 0.5, 0.7), (0.1, 0.1, 0.1), 50.0, 400.0))]):
+        m = ctor(*args)
+        s.set_texture(m, 0, (check, noise, image, grad, noise, check)[k])
+        mats.append(m)
+    s.set_texture(mats[5], 1, grad)
+    glow = s.diffuse_light((3.0, 3.0, 3.0))
+    s.set_texture(glow, 0, check)
+    verts, idx, nrm, uvs, tile = heightfield_mesh(8, 0.15, seed=9, extent=3.0)
+    s.mesh(verts, idx, lam, normals=nrm, uvs=uvs, tex_index=(tile % 5).astype(np.uint32))
+    for k, m in enumerate(mats):
+        s.sphere((-2.5 + k, 0.55, 0.3 * (k % 2)), 0.45, m)
+    s.box((-0.3, 0.0, -0.3), (0.3, 0.6, 0.3), mats[0],
+          compose([mat_translate((0.6, 0.1, -1.3)), mat_rotate(25.0, PT_Y_AXIS)]))
+    s.rect(-3, 3, 0, 2, -2.0, False, PT_Z_AXIS, mats[1])
+    s.rect(-0.8, 0.8, -0.8, 0.8, 2.6, True, PT_Y_AXIS, glow)
+    s.light_rect(-0.8, 0.8, -0.8, 0.8, 2.6, PT_Y_AXIS, (3.0, 3.0, 3.0))
+    s.miss_gradient((1.0, 1.0, 1.0), (0.5, 0.7, 1.0))
+    s.set_camera((0.0, 1.6, 4.5), (0.0, 0.3, 0.0), (0, 1, 0), 45.0, width / height, 0.05, 4.5)
+    return s
+
+
+SCENES["textures"] = texture_zoo

@@ -225,6 +225,18 @@ struct Material {
   int type;
   V3 c0, c1;    // colour (diffuse), second colour (specular / extinction)
   float p0, p1; // fuzz | ref_idx,density | rA,rB | nu,nv
+  int tex0 = -1, tex1 = -1;  // textures of c0 / c1 (-1: the constant colour)
+};
+
+// Texture callables of programs/textures/*.cu (host_includes/textures.hpp).
+enum { TEX_CONSTANT = 0, TEX_CHECKER, TEX_NOISE, TEX_IMAGE, TEX_GRADIENT, TEX_VECTOR };
+struct Texture {
+  int kind;
+  int a = 0, b = 0;          // checker: odd, even; vector: first entry, size; image: w, h;
+                             // noise: axis
+  float c[9] = {0};          // constant colour; gradient A, B, C; noise scale
+  std::vector<float> data;   // image: rgba texels; noise: ranvec (256 x 3)
+  std::vector<int> perm;     // noise: perm_x, perm_y, perm_z (3 x 256)
 };
 
 struct Xform {
@@ -239,6 +251,7 @@ struct Prim {
   // triangles: vertex indices into the mesh-wide attribute arrays
   int32_t vi[3];
   int mesh;
+  int tindex;  // texture index: 0, or the face's (mesh.hpp material_buffer)
 };
 
 struct Mesh {
@@ -291,6 +304,8 @@ struct EnvCdf {
 struct Scene {
   EnvCdf env_cdf;
   std::vector<Material> mats;
+  std::vector<Texture> textures;
+  std::vector<int> tex_list;  // vector-texture entries
   std::vector<Prim> prims;
   std::vector<Xform> xforms;
   std::vector<Mesh> meshes;
@@ -348,6 +363,7 @@ struct Ray {
 
 struct HitRecord {
   int index;
+  int tindex;  // texture index
   V3 P;
   float u, v;
   V3 geometric_normal, shading_normal, Wo;
@@ -477,6 +493,7 @@ HitRecord hit_record(const Scene& s, const Prim& p, const Ray& r, float t_hit, f
   const float* M = p.xform >= 0 ? s.xforms[p.xform].m : nullptr;
   const float* I = p.xform >= 0 ? s.xforms[p.xform].inv : nullptr;
   rec.index = p.material;
+  rec.tindex = p.type == PRIM_TRIANGLE ? p.tindex : 0;
   if (p.type == PRIM_SPHERE) {  // programs/hitables/sphere.cu:65-93
     V3 center = v3(p.f[0], p.f[1], p.f[2]);
     float radius = p.f[3];
@@ -550,6 +567,103 @@ HitRecord hit_record(const Scene& s, const Prim& p, const Ray& r, float t_hit, f
     }
   }
   return rec;
+}
+
+// -------------------------------------------------------------- textures --
+// programs/textures/noise_texture.cu:12-59 (ranvec: 256 x 3, perm: 3 x 256)
+float perlin_noise(const Texture& t, V3 p) {
+  float u = p.x - floorf(p.x);
+  float v = p.y - floorf(p.y);
+  float w = p.z - floorf(p.z);
+  int i = (int)floorf(p.x);
+  int j = (int)floorf(p.y);
+  int k = (int)floorf(p.z);
+  float uu = u * u * (3 - 2 * u);
+  float vv = v * v * (3 - 2 * v);
+  float ww = w * w * (3 - 2 * w);
+  float accum = 0;
+  for (int di = 0; di < 2; di++)
+    for (int dj = 0; dj < 2; dj++)
+      for (int dk = 0; dk < 2; dk++) {
+        int r = t.perm[(i + di) & 255] ^ t.perm[256 + ((j + dj) & 255)] ^
+                t.perm[512 + ((k + dk) & 255)];
+        V3 c = v3(t.data[3 * r], t.data[3 * r + 1], t.data[3 * r + 2]);
+        V3 weight_v = v3(u - di, v - dj, w - dk);
+        accum += (di * uu + (1 - di) * (1 - uu)) * (dj * vv + (1 - dj) * (1 - vv)) *
+                 (dk * ww + (1 - dk) * (1 - ww)) * dot(c, weight_v);
+      }
+  return accum;
+}
+
+// noise_texture.cu:61-76
+float perlin_turb(const Texture& t, V3 p) {
+  float accum = 0;
+  V3 temp_p = p;
+  float weight = 1.0f;
+  for (int i = 0; i < 7; i++) {
+    accum += weight * perlin_noise(t, temp_p);
+    weight *= 0.5f;
+    temp_p *= 2.f;
+  }
+  return fabsf(accum);
+}
+
+// sample_texture(u, v, p, i) of the texture callables.
+V3 texture_color(const Scene& s, int id, float u, float v, V3 p, int i) {
+  for (int hop = 0; hop < 64; hop++) {
+    const Texture& t = s.textures[id];
+    switch (t.kind) {
+      case TEX_CONSTANT:  // constant_texture.cu:5-7
+        return v3(t.c[0], t.c[1], t.c[2]);
+      case TEX_CHECKER: {  // checkered_texture.cu:8-15
+        float sines = pt_sinf(10 * p.x) * pt_sinf(10 * p.y) * pt_sinf(10 * p.z);
+        id = sines < 0 ? t.a : t.b;
+        i = 0;
+        break;
+      }
+      case TEX_VECTOR:  // vector.cu:7-12
+        if (i >= t.b || i < 0) return v3(0.f);
+        id = s.tex_list[t.a + i];
+        i = 0;
+        break;
+      case TEX_NOISE: {  // noise_texture.cu:61-76: every axis falls through to Z
+        float scale = t.c[0];
+        float sinValue = pt_sinf(scale * p.z + 5 * perlin_turb(t, scale * p));
+        return v3(1.f) * 0.5f * (1 + sinValue);
+      }
+      case TEX_IMAGE: {  // image_texture.cu:3-7: bilinear, repeat wrap
+        int W = t.a, H = t.b;
+        if (!(u == u) || !(v == v) || fabsf(u) > 1e6f || fabsf(v) > 1e6f) return v3(0.f);
+        float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+        float fx = ptm_floor(x), fy = ptm_floor(y);
+        float ax = x - fx, ay = y - fy;
+        int ix0 = (int)fx % W; if (ix0 < 0) ix0 += W;
+        int iy0 = (int)fy % H; if (iy0 < 0) iy0 += H;
+        int ix1 = ix0 + 1 == W ? 0 : ix0 + 1;
+        int iy1 = iy0 + 1 == H ? 0 : iy0 + 1;
+        auto tx = [&](int ix, int iy) {
+          const float* e = t.data.data() + ((size_t)iy * W + ix) * 4;
+          return v3(e[0], e[1], e[2]);
+        };
+        return (tx(ix0, iy0) * (1.f - ax) + tx(ix1, iy0) * ax) * (1.f - ay) +
+               (tx(ix0, iy1) * (1.f - ax) + tx(ix1, iy1) * ax) * ay;
+      }
+      default: {  // gradient_texture.cu:7-14
+        V3 unit_direction = normalize(p);
+        float x = fabsf(unit_direction.x), y = fabsf(unit_direction.y),
+              z = fabsf(unit_direction.z);
+        return x * v3(t.c[0], t.c[1], t.c[2]) + y * v3(t.c[3], t.c[4], t.c[5]) +
+               z * v3(t.c[6], t.c[7], t.c[8]);
+      }
+    }
+  }
+  return v3(0.f);
+}
+
+// Get_Parameters of the closest-hit programs: colours from the textures.
+inline void resolve_textures(const Scene& s, Material& m, const HitRecord& rec) {
+  if (m.tex0 >= 0) m.c0 = texture_color(s, m.tex0, rec.u, rec.v, rec.P, rec.tindex);
+  if (m.tex1 >= 0) m.c1 = texture_color(s, m.tex1, rec.u, rec.v, rec.P, rec.tindex);
 }
 
 // ------------------------------------------------------------------- BVH ---
@@ -1510,7 +1624,8 @@ struct Tracer {
   void closest_hit(PRD& prd, const Ray& ray, const Hit& h) {
     const Prim& p = s.prims[h.prim];
     HitRecord rec = hit_record(s, p, ray, h.t, h.u, h.v);
-    const Material& m = s.mats[rec.index];
+    Material m = s.mats[rec.index];
+    resolve_textures(s, m, rec);
     V3 P = rec.P, Wo = rec.Wo, N = rec.shading_normal;
     switch (m.type) {
       case MAT_LAMBERTIAN:     // programs/materials/lambertian.cu:49-73
@@ -1671,7 +1786,8 @@ struct Tracer {
       }
       const Prim& p = s.prims[h.prim];
       HitRecord rec = hit_record(s, p, ray, h.t, h.u, h.v);
-      const Material& m = s.mats[rec.index];
+      Material m = s.mats[rec.index];
+      resolve_textures(s, m, rec);
       V3 P = rec.P, Wo = rec.Wo, N = rec.shading_normal;
       if (m.type == MAT_DIFFUSE_LIGHT) {
         float w = 1.f;
@@ -1885,6 +2001,41 @@ int or_add_mesh(void* sp, const float* verts, int nv, const uint32_t* idx, int n
     s.prims.push_back(p);
   }
   return first;
+}
+
+// A texture (kind TEX_*): ints a, b as the kind uses them (checker: odd,
+// even; vector: -, size with `ids` its entries; image: w, h; noise: axis),
+// c[9] its colours / scale, data: image rgba (w*h*4) or noise ranvec
+// (768 floats), perm: noise permutations (768 ints).  Returns the id.
+int or_add_texture(void* sp, int kind, int a, int b, const float* c, const float* data,
+                   const int32_t* perm, const uint32_t* ids) {
+  Scene& s = *(Scene*)sp;
+  Texture t;
+  t.kind = kind;
+  t.a = a;
+  t.b = b;
+  if (c) memcpy(t.c, c, sizeof(t.c));
+  if (kind == TEX_IMAGE) t.data.assign(data, data + (size_t)a * b * 4);
+  if (kind == TEX_NOISE) {
+    t.data.assign(data, data + 768);
+    t.perm.assign(perm, perm + 768);
+  }
+  if (kind == TEX_VECTOR) {
+    t.a = (int)s.tex_list.size();
+    for (int k = 0; k < b; k++) s.tex_list.push_back((int)ids[k]);
+  }
+  s.textures.push_back(t);
+  return (int)s.textures.size() - 1;
+}
+
+void or_material_set_texture(void* sp, int material, int slot, int texture) {
+  Scene& s = *(Scene*)sp;
+  (slot == 0 ? s.mats[material].tex0 : s.mats[material].tex1) = texture;
+}
+
+void or_mesh_set_texture_index(void* sp, int first_prim, int n, const uint32_t* index) {
+  Scene& s = *(Scene*)sp;
+  for (int k = 0; k < n; k++) s.prims[first_prim + k].tindex = (int)index[k];
 }
 
 // type LIGHT_RECT: f = a0,a1,b0,b1,k (axis); LIGHT_SPHERE: cx,cy,cz,r.

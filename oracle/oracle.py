@@ -44,6 +44,9 @@ def load():
                               ctypes.c_int]
     L.or_set_camera.argtypes = [_P, _P, _P, _P] + [ctypes.c_float] * 6
     L.or_commit.argtypes = [_P]
+    L.or_add_texture.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P]
+    L.or_material_set_texture.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.or_mesh_set_texture_index.argtypes = [_P, ctypes.c_int, ctypes.c_int, _P]
     L.or_first_hits.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
                                 ctypes.c_int]
     L.or_render_paths.argtypes = [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int]
@@ -91,11 +94,16 @@ def replay(L, prefix, h, s):
     (prefix "or_") or of the reference-program harness (prefix "rh_"): both
     libraries take the same calls."""
     fn = lambda name: getattr(L, prefix + name)
+    for kind, a, b, cc, data, perm, ids in getattr(s, "textures", []):
+        fn("add_texture")(h, kind, a, b, _p(_f(cc)), _p(data), _p(perm), _p(ids))
     for kind, c0, c1, p0, p1 in s.materials:
         c0a = _f(c0)
         c1a = _f(c1) if c1 is not None else None
         fn("add_material")(h, kind, _p(c0a), _p(c1a), p0, p1)
-    for it in s.items:
+    for m, slot, t in getattr(s, "mat_textures", []):
+        fn("material_set_texture")(h, m, slot, t)
+    tex_index = getattr(s, "tex_index", {})
+    for k, it in enumerate(s.items):
         if it[0] == "sphere":
             _, cen, r, m, xf = it
             fn("add_prim")(h, 1, _p(_f(list(cen) + [r])), 0, 0, m, _p(xf))
@@ -108,8 +116,11 @@ def replay(L, prefix, h, s):
         else:
             _, v, idx, m, mpt, nrm, uv, xf = it
             mpt_i = None if mpt is None else np.ascontiguousarray(mpt, dtype=np.int32)
-            fn("add_mesh")(h, _p(v), len(v), _p(idx), len(idx), _p(mpt_i),
-                           m if m is not None else 0, _p(nrm), _p(uv), _p(xf))
+            first = fn("add_mesh")(h, _p(v), len(v), _p(idx), len(idx), _p(mpt_i),
+                                   m if m is not None else 0, _p(nrm), _p(uv), _p(xf))
+            if k in tex_index:
+                ti = tex_index[k]
+                fn("mesh_set_texture_index")(h, first, len(ti), _p(ti))
     for lt in s.lights:
         if lt[0] == "rect":
             _, v5, axis, e = lt

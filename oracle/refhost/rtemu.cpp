@@ -45,10 +45,23 @@ enum { TEX_CONSTANT = 0, TEX_IMAGE };
 enum { LIGHT_RECT = 0, LIGHT_SPHERE };
 enum { MISS_GRADIENT = 0, MISS_CONSTANT, MISS_HDR, MISS_IMAGE };
 
+// Textures the runtime makes for the materials' constant colours and the
+// miss programs (ids -1, -2, ... in the programs' callables), and the
+// scene's own textures (ids 0, 1, ... as the oracle and the library number
+// them).
 struct Texture {
   int kind;
   float c[3];
   int image;  // index into Scene::images
+};
+struct UserTexture {
+  int kind;   // the oracle's TEX_*
+  int a, b;   // checker: odd, even; vector: -, size; image: w, h; noise: axis
+  float c[9];
+  std::vector<float> texels;  // image rgba
+  std::vector<float3> ranvec; // noise
+  std::vector<int> perm;      // noise: perm_x, perm_y, perm_z
+  std::vector<int> ids;       // vector entries
 };
 struct Material {
   int type;
@@ -79,6 +92,7 @@ struct Image {
 };
 struct Scene {
   std::vector<Texture> tex;
+  std::vector<UserTexture> utex;
   std::vector<Material> mats;
   std::vector<Xform> xforms;
   std::vector<Prim> prims;
@@ -368,10 +382,21 @@ void rtemu_trace(const Ray& ray, void* payload) {
 
 // ------------------------------------------------- callables of the scene --
 float3 rtemu_texture(int tex, float u, float v, const float3& p, int i) {
-  const Texture& t = g->tex[tex];
-  if (t.kind == TEX_CONSTANT) return ref_constant_texture(t.c, u, v, &p, i);
-  const Image& im = g->images[t.image];
-  return ref_image_texture(im.texels.data(), im.w, im.h, u, v, &p, i);
+  if (tex < 0) {
+    const Texture& t = g->tex[-1 - tex];
+    if (t.kind == TEX_CONSTANT) return ref_constant_texture(t.c, u, v, &p, i);
+    const Image& im = g->images[t.image];
+    return ref_image_texture(im.texels.data(), im.w, im.h, u, v, &p, i);
+  }
+  const UserTexture& t = g->utex[tex];
+  switch (t.kind) {
+    case 0: return ref_constant_texture(t.c, u, v, &p, i);
+    case 1: return ref_checker_texture(t.a, t.b, u, v, &p, i);
+    case 2: return ref_noise_texture(t.c[0], t.a, t.ranvec.data(), t.perm.data(), u, v, &p, i);
+    case 3: return ref_image_texture(t.texels.data(), t.a, t.b, u, v, &p, i);
+    case 4: return ref_gradient_texture(t.c, u, v, &p, i);
+    default: return ref_vector_texture(tex, t.ids.data(), (int)t.ids.size(), u, v, &p, i);
+  }
 }
 
 void rtemu_hitrecord(int index, const Ray& ray, float t, float2 b, EmuRec* out) {
@@ -414,7 +439,7 @@ int add_texture(Scene& s, const float* c) {
   t.c[2] = c ? c[2] : 0.f;
   t.image = -1;
   s.tex.push_back(t);
-  return (int)s.tex.size() - 1;
+  return -(int)s.tex.size();
 }
 int add_xform(Scene& s, const float* x) {
   if (!x) return -1;
@@ -491,11 +516,9 @@ int rh_add_mesh(void* sp, const float* verts, int nv, const uint32_t* idx, int n
     for (int i = 0; i < nv; i++) mesh.uv[i] = make_float2(uvs[2 * i], uvs[2 * i + 1]);
   }
   mesh.idx.resize(nt);
-  mesh.texidx.resize(nt);
-  for (int t = 0; t < nt; t++) {
+  mesh.texidx.assign(nt, 0);  // the faces' texture indices (rh_mesh_set_texture_index)
+  for (int t = 0; t < nt; t++)
     mesh.idx[t] = make_int3((int)idx[3 * t], (int)idx[3 * t + 1], (int)idx[3 * t + 2]);
-    mesh.texidx[t] = mat_per_tri ? mat_per_tri[t] : material;
-  }
   s.meshes.push_back(std::move(mesh));
   int mid = (int)s.meshes.size() - 1;
   int first = (int)s.prims.size();
@@ -510,6 +533,41 @@ int rh_add_mesh(void* sp, const float* verts, int nv, const uint32_t* idx, int n
     s.prims.push_back(p);
   }
   return first;
+}
+
+// The scene's textures, as or_add_texture takes them (kind: 0 constant,
+// 1 checker, 2 noise, 3 image, 4 gradient, 5 vector).
+int rh_add_texture(void* sp, int kind, int a, int b, const float* c, const float* data,
+                   const int32_t* perm, const uint32_t* ids) {
+  Scene& s = *(Scene*)sp;
+  UserTexture t;
+  t.kind = kind;
+  t.a = a;
+  t.b = b;
+  for (int k = 0; k < 9; k++) t.c[k] = c ? c[k] : 0.f;
+  if (kind == 3) t.texels.assign(data, data + (size_t)a * b * 4);
+  if (kind == 2) {
+    t.ranvec.resize(256);
+    for (int k = 0; k < 256; k++)
+      t.ranvec[k] = make_float3(data[3 * k], data[3 * k + 1], data[3 * k + 2]);
+    t.perm.assign(perm, perm + 768);
+  }
+  if (kind == 5)
+    for (int k = 0; k < b; k++) t.ids.push_back((int)ids[k]);
+  s.utex.push_back(std::move(t));
+  return (int)s.utex.size() - 1;
+}
+
+void rh_material_set_texture(void* sp, int material, int slot, int texture) {
+  ((Scene*)sp)->mats[material].tex[slot] = texture;
+}
+
+void rh_mesh_set_texture_index(void* sp, int first_prim, int n, const uint32_t* index) {
+  Scene& s = *(Scene*)sp;
+  for (int k = 0; k < n; k++) {
+    const Prim& p = s.prims[first_prim + k];
+    s.meshes[p.mesh].texidx[p.local] = (int)index[k];
+  }
 }
 
 // type 0 rect: f = a0,a1,b0,b1,k (axis); 1 sphere: cx,cy,cz,r.
@@ -545,7 +603,7 @@ void rh_set_miss(void* sp, int type, const float* c1, const float* c2, const flo
     t.kind = TEX_IMAGE;
     t.image = (int)s.images.size() - 1;
     s.tex.push_back(t);
-    s.miss_tex[0] = (int)s.tex.size() - 1;
+    s.miss_tex[0] = -(int)s.tex.size();
   }
 }
 

@@ -92,10 +92,16 @@ float3 ref_sphere_light_sample(const float* f, const float3* P, const float3* Wo
 float ref_sphere_light_pdf(const float* f, const float3* P, const float3* Wo, const float3* Wi,
                            const float3* N);
 
-// programs/textures/{constant_texture,image_texture}.cu
+// programs/textures/*.cu texture callables
 float3 ref_constant_texture(const float* color, float u, float v, const float3* p, int i);
 float3 ref_image_texture(const float* texels, int w, int h, float u, float v, const float3* p,
                          int i);
+float3 ref_checker_texture(int odd_id, int even_id, float u, float v, const float3* p, int i);
+float3 ref_noise_texture(float scale, int axis, const float3* ranvec, const int* perm, float u,
+                         float v, const float3* p, int i);
+float3 ref_gradient_texture(const float* c, float u, float v, const float3* p, int i);
+float3 ref_vector_texture(int self, const int* ids, int n, float u, float v, const float3* p,
+                          int i);
 
 // programs/raygen.cu renderPixel: one launch index of one frame; acc and
 // display are W x H buffers (row y holds launch row H-1-y).

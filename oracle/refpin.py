@@ -67,6 +67,9 @@ def load():
     L.rh_set_miss.argtypes = [_P, i, _P, _P, _P, i, i, i]
     L.rh_set_camera.argtypes = [_P, _P, _P, _P] + [fl] * 6
     L.rh_commit.argtypes = [_P]
+    L.rh_add_texture.argtypes = [_P, i, i, i, _P, _P, _P, _P]
+    L.rh_material_set_texture.argtypes = [_P, i, i, i]
+    L.rh_mesh_set_texture_index.argtypes = [_P, i, i, _P]
     L.rh_render_paths.argtypes = [_P, _P, i, _P, i, _P]
     L.rh_first_hits.argtypes = [_P, i, i, i, _P, _P, _P]
     L.rh_probe.argtypes = [_P, _P, _P, fl, _P, _P]

@@ -13,7 +13,29 @@ PKG = os.path.join(ROOT, "optix-path-tracer_gb300")
 
 def test_facade_header_compiles(tmp_path):
     src = tmp_path / "t.cpp"
-    src.write_text('#include "pt_scene.hpp"\nint main(){ pt::Hitable_List l; (void)l; return 0; }\n')
+    src.write_text(r'''
+#include "pt_scene.hpp"
+using namespace pt;
+// every texture class, as the reference's scene code builds them (the
+// functions are compiled, not run: they need a GPU context)
+void build(Context& ctx) {
+  Constant_Texture red(0.8f, 0.1f, 0.1f), white(0.9f);
+  Checker_Texture check(&red, &white);
+  Noise_Texture noise(4.f), noiseZ(0.1f, Z_AXIS);
+  float texels[4 * 4] = {0};
+  Image_Texture image(texels, 2, 2);
+  Gradient_Texture grad(make_float3(1, 0, 0), make_float3(0, 1, 0), make_float3(0, 0, 1));
+  Vector_Texture vec(std::vector<Texture*>{&check, &noise, &image, &grad});
+  Lambertian lam(&vec);
+  Ashikhmin_Shirley as(&check, &grad, 10.f, 100.f);
+  Dielectric glass(&noise, &white, 1.5f);
+  lam.assignTo(ctx);
+  as.assignTo(ctx);
+  glass.assignTo(ctx);
+  (void)noiseZ;
+}
+int main(){ pt::Hitable_List l; (void)l; (void)&build; return 0; }
+''')
     r = subprocess.run(["g++", "-std=c++14", "-fsyntax-only", "-Wall", "-Werror",
                         "-I", os.path.join(ROOT, "include"), str(src)],
                        capture_output=True, text=True)

@@ -291,3 +291,47 @@ def test_env_mapping_variants(ptgb_mod, oracle_mod, variant, mode):
     assert np.mean(np.all(gpu == ref, axis=1)) > 0.999
     assert (op == 0xFFFFFFFF).any(), "the camera must see the background"
     g.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_textures_match_oracle(ptgb_mod, oracle_mod, mode):
+    """Every texture callable (checker of a checker, Perlin noise, image,
+    gradient, a vector texture indexed per mesh face) on every material it
+    can colour, including both Ashikhmin-Shirley colours and an emitter: the
+    oracle's paths, whose textures are in turn pinned to the reference's own
+    texture programs (tests/test_ref_pin.py)."""
+    w, h = 96, 72
+    s = ptgb_mod.texture_zoo(w, h)
+    g, o = ptgb_mod.GpuRenderer(s), oracle_mod.Oracle(s)
+    gp, gm, gt = g.first_hits(w, h, 0)
+    op, om, ot = o.first_hits(w, h, 0)
+    assert np.array_equal(gp, op) and np.array_equal(gm, om)
+    for frame in (0, 2):
+        prm = ptgb_mod.GpuRenderer.params(w, h, 1, frame0=frame, mode=mode)
+        gpu = g.render_paths(prm).reshape(-1, 3)
+        ref = o.render_paths(w, h, frame, np.arange(w * h), mode=mode)
+        err = rel_err(gpu, ref)
+        assert err.max() <= REL_TOL, f"max rel err {err.max()}, {np.sum(err > REL_TOL)} paths"
+        assert np.mean(np.all(gpu == ref, axis=1)) > 0.999
+    # progressive accumulation through the texture-colour hand-over of k_finish
+    acc = g.render(ptgb_mod.GpuRenderer.params(w, h, 3, mode=mode))
+    ref, _ = o.render(w, h, 3, mode=mode)
+    assert rel_err(acc[..., :3], ref[..., :3]).max() <= REL_TOL
+    g.close()
+
+
+def test_textured_scene_in_a_batch(ptgb_mod):
+    """A textured scene rendered in a batch beside untextured ones equals its
+    own render (each item reads its own texture tables)."""
+    P = ptgb_mod
+    rs = [P.GpuRenderer(P.texture_zoo(48, 36)), P.GpuRenderer(P.material_zoo(40, 30)),
+          P.GpuRenderer(P.texture_zoo(32, 24))]
+    prms = [P.GpuRenderer.params(48, 36, 3), P.GpuRenderer.params(40, 30, 2),
+            P.GpuRenderer.params(32, 24, 4, frame0=5)]
+    accs = [np.zeros((p.height, p.width, 4), np.float32) for p in prms]
+    b = P.Batch()
+    b.render([(r, p, a) for r, p, a in zip(rs, prms, accs)])
+    b.close()
+    for r, p, a in zip(rs, prms, accs):
+        assert np.array_equal(a, r.render(p))
+        r.close()

@@ -4,7 +4,8 @@ oracle/_ref/libref.so compiles the reference's device programs (programs/ of
 joaovbs96/OptiX-Path-Tracer: raygen.cu, miss.cu, hit.cu, the intersection and
 HitRecord programs of hitables/{sphere,aarect,box,triangle}.cu, the
 closest-hit programs of materials/*.cu with light_sample.cuh's Direct_Light,
-pdfs/{rect,sphere}_pdf.cu, textures/{constant,image}_texture.cu, and the
+pdfs/{rect,sphere}_pdf.cu, textures/{constant,image,checkered,noise,
+gradient}_texture.cu and textures/vector.cu, and the
 headers random.cuh, sampling.cuh, math/trigonometric.cuh,
 materials/{material,microfacets}.cuh and the BRDF headers) unmodified, over
 an OptiX 6 stand-in and a CPU emulation of its runtime (oracle/refhost).
@@ -290,12 +291,13 @@ def full_scenes(ptgb):
         "zoo_env_image": (zoo_img, 40, 30),
         "zoo_constant": (zoo_const, 40, 30),
         "heightfield_env": (P.heightfield_scene(48, 27, cells=10, env_w=64, env_h=32), 48, 27),
+        "textures": (P.texture_zoo(64, 48), 64, 48),
     }
 
 
 @pytest.mark.parametrize("name", ["cornell_reference", "cornell_c1", "spheres", "zoo",
                                   "zoo_env_cylindrical", "zoo_env_image", "zoo_constant",
-                                  "heightfield_env"])
+                                  "heightfield_env", "textures"])
 def test_whole_paths(ptgb_mod, oracle_mod, name):
     """renderPixel of raygen.cu, with every program it reaches, gives the
     oracle's first hits and per-path radiance bit for bit (reference mode,

@@ -219,9 +219,12 @@ PT_API int pt_obj_get(const pt_obj* mesh, float* verts, float* normals, float* u
 PT_API int pt_obj_material(const pt_obj* mesh, size_t k, char* name, size_t name_cap,
                            float ka[3], float kd[3], char* map_kd, size_t map_cap);
 /* Mesh::getGeometryInstance (mesh.hpp:49-204): the mesh into the scene with
- * `material` on every face, or, with PT_OBJ_MTL, one Lambertian per MTL
- * material coloured by its ambient term Ka (mesh.hpp:78-96; map_Kd image
- * textures are not supported and fall back to Ka). */
+ * `material` on every face, or, with PT_OBJ_MTL, as the reference builds it
+ * without a given material (mesh.hpp:78-98): one Lambertian whose colour is
+ * a Vector_Texture of the MTL materials (an image texture of map_Kd, read
+ * with pt_image_load relative to the OBJ file's folder, rows flipped as
+ * Image_Texture does; else a constant texture of Ka), each face indexing
+ * its material (faces without usemtl: the first). */
 PT_API int pt_add_obj(pt_context* ctx, const pt_obj* mesh, uint32_t material,
                       const float xform[12], uint32_t* first_prim_id);
 /* Radiance HDR in (lib/HDRloader.cpp): rgba NULL returns the size only;
@@ -234,6 +237,13 @@ PT_API int pt_hdr_save(const char* path, int w, int h, const float* accum_rgba, 
 PT_API int pt_png_save(const char* path, int w, int h, const float* accum_rgba, int spp);
 /* message of the last failed file-format call of this thread */
 PT_API const char* pt_io_last_error(void);
+/* Image_Texture's file reading (textures.hpp:117-155, through stb_image):
+ * PNG (8/16-bit grey, grey+alpha, RGB, RGBA, 8-bit palette; not interlaced),
+ * PPM (P6, P3) and Radiance HDR; rgba NULL returns the size only, else
+ * w*h*4 floats, first file row first, 8-bit samples / 255 (16-bit / 65535),
+ * alpha 1 where the file has none.  JPEG is not decoded. */
+PT_API int pt_image_load(const char* path, int* w, int* h, float* rgba);
+PT_API const char* pt_image_last_error(void);
 
 /* ---- lights (host_includes/pdfs.hpp + Light_Sampler, host_common.hpp:65-68) */
 /* Rectangle_PDF(a0,a1,b0,b1,k,axis) + emission  pdfs.hpp:17-80 */

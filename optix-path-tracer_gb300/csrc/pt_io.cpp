@@ -127,6 +127,9 @@ bool inside3(const float* vx, const float* vy, float tx, float ty) {
 // corner's normal does not dominate; a triangle is an ear when its corner
 // turns with the polygon's orientation and no other vertex lies inside it;
 // the ear's middle vertex is removed).  Appends corner triples to `out`.
+// The steps are those of tinyobjloader (Syoyo Fujita, MIT licence), the OBJ
+// reader the reference vendors (lib/tiny_obj_loader.h), kept so that a file
+// gives the same triangles and primitive ids.
 void triangulate(const std::vector<Corner>& face, const std::vector<float>& pos,
                  std::vector<Corner>& out) {
   const size_t n0 = face.size();
@@ -245,6 +248,7 @@ struct pt_obj {
   std::vector<uint32_t> mat;        // per triangle: MTL material, or PT_OBJ_NO_MATERIAL
   bool has_nrm = false, has_uv = false;
   std::vector<Mtl> mats;
+  std::string dir;                  // the OBJ file's folder (map_Kd paths are relative to it)
 };
 
 extern "C" {
@@ -330,6 +334,7 @@ PT_API int pt_obj_load(const char* path, pt_obj** out) {
   for (size_t i = 0; i < tri_mat.size(); i++)
     m->mat[i] = tri_mat[i] < 0 ? PT_OBJ_NO_MATERIAL : (uint32_t)tri_mat[i];
   m->mats = std::move(mats);
+  m->dir = dir_of(path);
   *out = m;
   return PT_OK;
 }
@@ -382,32 +387,57 @@ PT_API int pt_add_obj(pt_context* ctx, const pt_obj* m, uint32_t material, const
   const size_t nt = m->mat.size();
   std::vector<uint32_t> idx(3 * nt);
   for (size_t i = 0; i < idx.size(); i++) idx[i] = (uint32_t)i;
-  std::vector<uint32_t> per_tri;
-  uint32_t fallback = material;
+  uint32_t mat_id = material;
+  std::vector<uint32_t> tex_index;
   if (material == PT_OBJ_MTL) {
-    // one Lambertian per MTL material, coloured by its ambient term, as the
-    // reference's Mesh does without a given material (mesh.hpp:78-96);
-    // faces without a material use the first one, or a grey Lambertian
-    std::vector<uint32_t> ids(m->mats.size());
-    for (size_t k = 0; k < m->mats.size(); k++) {
-      int rc = pt_material_lambertian(ctx, m->mats[k].ka, &ids[k]);
-      if (rc) return rc;
-    }
-    if (ids.empty()) {
+    // as the reference's Mesh without a given material (mesh.hpp:78-98):
+    // Lambertian(Vector_Texture(per MTL material: Image_Texture(map_Kd) or
+    // Constant_Texture(Ka))), each face indexing its material; without an
+    // MTL file, a grey Lambertian
+    if (m->mats.empty()) {
       const float grey[3] = {0.5f, 0.5f, 0.5f};
-      ids.resize(1);
-      int rc = pt_material_lambertian(ctx, grey, &ids[0]);
+      int rc = pt_material_lambertian(ctx, grey, &mat_id);
       if (rc) return rc;
+    } else {
+      std::vector<uint32_t> texs(m->mats.size());
+      for (size_t k = 0; k < m->mats.size(); k++) {
+        const Mtl& t = m->mats[k];
+        int rc;
+        if (!t.map_kd.empty()) {
+          std::string file = m->dir + t.map_kd;
+          int w = 0, h = 0;
+          if (pt_image_load(file.c_str(), &w, &h, nullptr))
+            return io_fail(PT_EINVAL, std::string("map_Kd: ") + pt_image_last_error());
+          std::vector<float> px((size_t)w * h * 4), flip((size_t)w * h * 4);
+          if (pt_image_load(file.c_str(), &w, &h, px.data()))
+            return io_fail(PT_EINVAL, std::string("map_Kd: ") + pt_image_last_error());
+          // Image_Texture stores the file's last row first (textures.hpp:140-151)
+          for (int y = 0; y < h; y++)
+            memcpy(&flip[(size_t)y * w * 4], &px[(size_t)(h - 1 - y) * w * 4], (size_t)w * 16);
+          rc = pt_texture_image(ctx, flip.data(), w, h, &texs[k]);
+        } else {
+          rc = pt_texture_constant(ctx, t.ka, &texs[k]);
+        }
+        if (rc) return rc;
+      }
+      uint32_t vec;
+      const float black[3] = {0.f, 0.f, 0.f};
+      int rc = pt_texture_vector(ctx, texs.data(), (int)texs.size(), &vec);
+      if (!rc) rc = pt_material_lambertian(ctx, black, &mat_id);
+      if (!rc) rc = pt_material_set_texture(ctx, mat_id, 0, vec);
+      if (rc) return rc;
+      tex_index.resize(nt);
+      for (size_t i = 0; i < nt; i++) tex_index[i] = m->mat[i] == PT_OBJ_NO_MATERIAL ? 0u : m->mat[i];
     }
-    fallback = ids[0];
-    per_tri.resize(nt);
-    for (size_t i = 0; i < nt; i++) per_tri[i] = m->mat[i] == PT_OBJ_NO_MATERIAL ? fallback : ids[m->mat[i]];
   }
   if (nt == 0) return PT_OK;
-  return pt_add_mesh(ctx, m->pos.data(), 3 * nt, idx.data(), nt,
-                     per_tri.empty() ? nullptr : per_tri.data(), fallback,
-                     m->has_nrm ? m->nrm.data() : nullptr, m->has_uv ? m->uv.data() : nullptr,
-                     xform, first_prim_id);
+  uint32_t first = 0;
+  int rc = pt_add_mesh(ctx, m->pos.data(), 3 * nt, idx.data(), nt, nullptr, mat_id,
+                       m->has_nrm ? m->nrm.data() : nullptr, m->has_uv ? m->uv.data() : nullptr,
+                       xform, &first);
+  if (!rc && !tex_index.empty()) rc = pt_mesh_set_texture_index(ctx, first, nt, tex_index.data());
+  if (!rc && first_prim_id) *first_prim_id = first;
+  return rc;
 }
 
 // ------------------------------------------------------------- HDR ----------

@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + [
     "-I", CSRC,
 ]
 SOURCES = ["pt_kernels.cu", "pt_api.cu", "pt_batch.cu", "pt_guide.cu", "pt_guide_host.cu", "bvh_host.cpp",
-           "bvh_gpu.cu", "pt_io.cpp"]
+           "bvh_gpu.cu", "pt_io.cpp", "pt_image.cpp"]
 
 
 def _nvcc():

@@ -112,6 +112,8 @@ SIGNATURES = {
                         ctypes.c_char_p, ctypes.c_size_t],
     "pt_add_obj": [_P, _P, ctypes.c_uint32, _P, _U32P],
     "pt_hdr_load": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _P],
+    "pt_image_load": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                      _P],
     "pt_hdr_save": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int],
     "pt_png_save": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int],
     "pt_add_light_rect": [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
@@ -174,6 +176,7 @@ def load_library(path=LIB_PATH):
     lib.pt_batch_last_error.restype = ctypes.c_char_p
     lib.pt_io_last_error.argtypes = []
     lib.pt_io_last_error.restype = ctypes.c_char_p
+    lib.pt_image_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 
@@ -200,6 +203,7 @@ class ObjMesh:
         h = _P()
         _io_check(self.lib, self.lib.pt_obj_load(str(path).encode(), ctypes.byref(h)))
         self.h = h
+        self.dir = os.path.dirname(os.path.abspath(str(path)))
         nt, nm = ctypes.c_size_t(), ctypes.c_size_t()
         hn, hu = ctypes.c_int(), ctypes.c_int()
         _io_check(self.lib, self.lib.pt_obj_info(h, ctypes.byref(nt), ctypes.byref(nm),
@@ -231,6 +235,21 @@ class ObjMesh:
             self.close()
         except Exception:
             pass
+
+
+def image_load(path):
+    """An image file read by pt_image_load (PNG, PPM, Radiance HDR): HxWx4
+    float32, first file row first."""
+    lib = load_library()
+    w, h = ctypes.c_int(), ctypes.c_int()
+    rc = lib.pt_image_load(str(path).encode(), ctypes.byref(w), ctypes.byref(h), None)
+    if rc != 0:
+        raise PtError(rc, lib.pt_image_last_error().decode())
+    out = np.zeros((h.value, w.value, 4), np.float32)
+    rc = lib.pt_image_load(str(path).encode(), ctypes.byref(w), ctypes.byref(h), _ptr(out))
+    if rc != 0:
+        raise PtError(rc, lib.pt_image_last_error().decode())
+    return out
 
 
 def hdr_load(path):
@@ -426,25 +445,36 @@ class Scene:
         return first
 
     def obj(self, mesh, material=None, xform=None, via_add_obj=False):
-        """An ObjMesh as the reference's Mesh adds it: `material` on every
-        face, or (None) one Lambertian per MTL material coloured by Ka, faces
-        without usemtl on the first (a grey Lambertian without an MTL file).
-        via_add_obj: the GPU renderer loads it through pt_add_obj instead of
-        pt_add_mesh (the oracle always sees the triangle arrays)."""
+        """An ObjMesh as the reference's Mesh adds it (mesh.hpp:78-98):
+        `material` on every face, or (None) one Lambertian coloured by a
+        vector texture of the MTL materials (an image texture of map_Kd,
+        rows flipped as Image_Texture stores them, else a constant Ka), each
+        face indexing its material (faces without usemtl: the first); a grey
+        Lambertian without an MTL file.  via_add_obj: the GPU renderer loads
+        it through pt_add_obj instead of pt_add_mesh (the oracle always sees
+        the triangle arrays)."""
         nt = mesh.n_tris
-        per = None
         mat = material
-        if material is None:
-            ids = [self.lambertian(tuple(mesh.material(k)["Ka"])) for k in range(mesh.n_materials)]
-            if not ids:
-                ids = [self.lambertian((0.5, 0.5, 0.5))]
-            table = np.array(ids, np.uint32)
-            per = np.where(mesh.mat == PT_OBJ_NO_MATERIAL, table[0],
-                           table[np.minimum(mesh.mat, len(ids) - 1)]).astype(np.uint32)
-            mat = ids[0]
+        tex_index = None
+        if material is None and mesh.n_materials == 0:
+            mat = self.lambertian((0.5, 0.5, 0.5))
+        elif material is None:
+            texs = []
+            for k in range(mesh.n_materials):
+                info = mesh.material(k)
+                if info["map_Kd"]:
+                    img = image_load(os.path.join(mesh.dir, info["map_Kd"]))
+                    texs.append(self.texture_image(img[::-1]))
+                else:
+                    texs.append(self.texture_constant(tuple(info["Ka"])))
+            vec = self.texture_vector(texs)
+            mat = self.lambertian((0.0, 0.0, 0.0))
+            self.set_texture(mat, 0, vec)
+            tex_index = np.where(mesh.mat == PT_OBJ_NO_MATERIAL, 0, mesh.mat).astype(np.uint32)
         first = self.mesh(mesh.verts.reshape(-1, 3), np.arange(3 * nt, dtype=np.uint32).reshape(-1, 3),
-                          mat, per, None if mesh.normals is None else mesh.normals.reshape(-1, 3),
-                          None if mesh.uvs is None else mesh.uvs.reshape(-1, 2), xform)
+                          mat, None, None if mesh.normals is None else mesh.normals.reshape(-1, 3),
+                          None if mesh.uvs is None else mesh.uvs.reshape(-1, 2), xform,
+                          tex_index=tex_index)
         if via_add_obj:
             self.add_obj[len(self.items) - 1] = (mesh, material)
         return first

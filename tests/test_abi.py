@@ -33,7 +33,7 @@ def test_library_exports_declared_symbols(ptgb_mod):
 def test_python_signatures_cover_header(ptgb_mod):
     names = set(declared_symbols())
     covered = set(ptgb_mod.SIGNATURES) | {"pt_last_error", "pt_version", "pt_batch_last_error",
-                                          "pt_io_last_error"}
+                                          "pt_io_last_error", "pt_image_last_error"}
     assert names == covered, names ^ covered
 
 

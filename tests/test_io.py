@@ -212,3 +212,107 @@ def test_obj_crlf_and_convex_fan(ptgb_mod, tmp_path):
     assert np.allclose(v[0, 1:], [[np.cos(ang[1]), np.sin(ang[1]), 0], [np.cos(ang[2]), np.sin(ang[2]), 0]],
                        atol=1e-6)
     m.close()
+
+
+# ------------------------------------------------------------------ images
+def png_bytes(rows, ctype, depth=8, palette=None, trns=None, level=6, filters=None):
+    """A PNG file of the given raw rows (bytes per row), compressed by zlib
+    at `level` (0: stored blocks; 1..9: fixed / dynamic Huffman blocks),
+    each row filtered with filters[y] (0 none, 1 sub, 2 up, 3 average,
+    4 Paeth)."""
+    h = len(rows)
+    bpp = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype] * depth // 8
+    raw = b""
+    prev = bytes(len(rows[0]))
+    for y, r in enumerate(rows):
+        ft = filters[y] if filters else y % 5
+        out = bytearray()
+        for i, x in enumerate(r):
+            a = out_raw_a = r[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            if ft == 0:
+                p = 0
+            elif ft == 1:
+                p = a
+            elif ft == 2:
+                p = b
+            elif ft == 3:
+                p = (a + b) >> 1
+            else:
+                pp = a + b - c
+                pa, pb, pc = abs(pp - a), abs(pp - b), abs(pp - c)
+                p = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+            out.append((x - p) & 0xFF)
+        raw += bytes([ft]) + bytes(out)
+        prev = r
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d))
+
+    w = len(rows[0]) // bpp
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+    if palette is not None:
+        data += chunk(b"PLTE", bytes(palette))
+    if trns is not None:
+        data += chunk(b"tRNS", bytes(trns))
+    data += chunk(b"IDAT", zlib.compress(raw, level)) + chunk(b"IEND", b"")
+    return data
+
+
+@pytest.mark.parametrize("level", [0, 1, 9])
+@pytest.mark.parametrize("ctype", [0, 2, 4, 6])
+def test_png_load_colour_types_filters_and_compression(ptgb_mod, tmp_path, level, ctype):
+    rng = np.random.default_rng(ctype * 10 + level)
+    w, h, ch = 37, 23, {0: 1, 2: 3, 4: 2, 6: 4}[ctype]
+    px = rng.integers(0, 256, (h, w, ch), dtype=np.uint8)
+    px[: h // 2] //= 16                       # runs and repeats for the Huffman coders
+    f = tmp_path / "t.png"
+    f.write_bytes(png_bytes([px[y].tobytes() for y in range(h)], ctype, level=level))
+    img = ptgb_mod.image_load(f)
+    assert img.shape == (h, w, 4)
+    ref = np.ones((h, w, 4), np.float32)
+    v = px.astype(np.float32) / np.float32(255)
+    if ch <= 2:
+        ref[..., :3] = v[..., :1]
+        if ch == 2:
+            ref[..., 3] = v[..., 1]
+    else:
+        ref[..., :ch] = v
+    assert np.array_equal(img, ref)
+
+
+def test_png_load_palette_and_16_bit(ptgb_mod, tmp_path):
+    rng = np.random.default_rng(5)
+    pal = rng.integers(0, 256, 3 * 16, dtype=np.uint8)
+    idx = rng.integers(0, 16, (9, 11), dtype=np.uint8)
+    f = tmp_path / "p.png"
+    f.write_bytes(png_bytes([idx[y].tobytes() for y in range(9)], 3, palette=pal,
+                            trns=[128] * 4))
+    img = ptgb_mod.image_load(f)
+    assert np.array_equal(img[..., :3], pal.reshape(16, 3)[idx].astype(np.float32) / np.float32(255))
+    assert np.array_equal(img[..., 3], np.where(idx < 4, np.float32(128) / np.float32(255), 1.0))
+    v16 = rng.integers(0, 65536, (5, 6, 3), dtype=np.uint16)
+    f16 = tmp_path / "p16.png"
+    f16.write_bytes(png_bytes([v16[y].astype(">u2").tobytes() for y in range(5)], 2, depth=16))
+    img16 = ptgb_mod.image_load(f16)
+    assert np.array_equal(img16[..., :3], v16.astype(np.float32) / np.float32(65535))
+
+
+def test_ppm_load_and_unsupported_formats(ptgb_mod, tmp_path):
+    px = np.arange(2 * 3 * 3, dtype=np.uint8).reshape(2, 3, 3) * 7
+    f = tmp_path / "a.ppm"
+    f.write_bytes(b"P6\n# comment\n3 2\n255\n" + px.tobytes())
+    img = ptgb_mod.image_load(f)
+    assert np.array_equal(img[..., :3], px.astype(np.float32) / np.float32(255))
+    g = tmp_path / "b.ppm"
+    g.write_text("P3 3 2 255\n" + " ".join(str(x) for x in px.reshape(-1)) + "\n")
+    assert np.array_equal(ptgb_mod.image_load(g), img)
+    j = tmp_path / "c.jpg"
+    j.write_bytes(b"\xff\xd8\xff\xe0" + bytes(16))
+    with pytest.raises(ptgb_mod.PtError, match="JPEG"):
+        ptgb_mod.image_load(j)
+    bad = tmp_path / "d.png"
+    bad.write_bytes(png_bytes([bytes(12)] * 2, 2)[:-30])   # truncated
+    with pytest.raises(ptgb_mod.PtError):
+        ptgb_mod.image_load(bad)

@@ -101,6 +101,31 @@ def reduce_over_ranks(dev_s, wall, paths, rays, device):
     return float(mx[0]), float(mx[1]), float(sm[2]), float(sm[3])
 
 
+def reduce_images(acc64, device):
+    """The replicas' accumulators summed into one image: every rank's FP64
+    accumulator (H x W x 4: radiance sums and sample counts of its own
+    frames) is gathered on rank 0 and added there in rank order, so the
+    image is the same on every run (a fixed order of FP64 additions).
+    Returns the sum on rank 0, None on the other ranks; the accumulator
+    itself with one rank."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    a = np.ascontiguousarray(acc64, dtype=np.float64)
+    if not dist.is_initialized() or dist.get_world_size() == 1:
+        return a
+    t = torch.from_numpy(a).to(device)
+    world, rank = dist.get_world_size(), dist.get_rank()
+    parts = [torch.empty_like(t) for _ in range(world)] if rank == 0 else None
+    dist.gather(t, parts, dst=0)
+    if rank != 0:
+        return None
+    total = parts[0].cpu().numpy().copy()
+    for r in range(1, world):
+        total += parts[r].cpu().numpy()
+    return total
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -355,6 +380,22 @@ def run_ours(args, wl):
     if issue is not None and clk:
         issue = issue_fraction(tr, ext, shadow, trace_ms, clk.get("sm_mhz"))
 
+    # ---- the replicas' image: each rank's frames in FP64, summed in rank
+    # order on rank 0 (outside the timed region)
+    image = None
+    if world > 1:
+        acc64 = torch.zeros((h, w, 4), dtype=torch.float64, device=f"cuda:{local}")
+        rend.render64(prm, acc64.data_ptr())
+        torch.cuda.synchronize()
+        t_red = time.perf_counter()
+        total = reduce_images(acc64.cpu().numpy(), f"cuda:{local}")
+        t_red = time.perf_counter() - t_red
+        if rank == 0:
+            image = {"frames": int(total[..., 3].max()), "mean_rgb": [float(x) for x in
+                     (total[..., :3].sum(axis=(0, 1)) / total[..., 3].sum())],
+                     "reduce_ms": 1e3 * t_red,
+                     "order": "FP64 accumulators gathered on rank 0, added in rank order"}
+
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -398,6 +439,8 @@ def run_ours(args, wl):
             "cpu_baseline": cpu,
             "clocks": clk,
         }
+        if image is not None:
+            line["image"] = image
         print(json.dumps(line), flush=True)
     rend.close()
     if world > 1:

@@ -67,8 +67,15 @@ PT_BVH_HD inline void encode_node_dev(const Box& parent, const WideChild* ch, in
   uint32_t meta[2] = {0, 0}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
   uint32_t qlo[3][2] = {{0xffffffffu, 0xffffffffu}, {0xffffffffu, 0xffffffffu},
                         {0xffffffffu, 0xffffffffu}};
+  // internal children take the low slots in their given order (slot ==
+  // rank, the offset of the child node from child_base), leaves follow
+  int ord[8], no = 0;
+  for (int i = 0; i < nch; i++)
+    if (ch[i].internal) ord[no++] = i;
+  for (int i = 0; i < nch; i++)
+    if (!ch[i].internal) ord[no++] = i;
   for (int i = 0; i < nch; i++) {
-    const WideChild& c = ch[i];
+    const WideChild& c = ch[ord[i]];
     uint32_t m;
     if (c.internal) {
       m = 0x80u | rank;

@@ -247,7 +247,8 @@ int build_bvh8_host(const std::vector<Box>& boxes, Bvh8Out& out, int width) {
 }
 
 // Structural check of a BVH8 before it is uploaded: every internal child
-// index lies after its parent and inside the node array, ranks are dense,
+// index lies after its parent and inside the node array, internal children
+// fill the low slots with dense ranks (slot == rank),
 // leaf ranges lie inside the primitive array and cover each primitive once.
 bool validate_bvh8(const Bvh8Out& b, size_t num_prims) {
   size_t nn = b.nodes.size() / 20;
@@ -262,7 +263,7 @@ bool validate_bvh8(const Bvh8Out& b, size_t num_prims) {
       if (!meta) continue;
       if (meta & 0x80u) {
         uint64_t c = (uint64_t)w[4] + (meta & 7u);
-        if ((meta & 7u) != rank || c <= k || c >= nn) return false;
+        if ((meta & 7u) != rank || (uint32_t)i != rank || c <= k || c >= nn) return false;
         rank++;
       } else {
         uint32_t cnt = meta >> 5, off = meta & 31u;
@@ -274,7 +275,7 @@ bool validate_bvh8(const Bvh8Out& b, size_t num_prims) {
         }
       }
     }
-    if (rank != (w[3] >> 24 == 0 ? 0u : (uint32_t)__builtin_popcount(w[3] >> 24))) return false;
+    if ((w[3] >> 24) != (1u << rank) - 1u) return false;  // internal children in slots 0..rank-1
   }
   for (uint8_t v : seen)
     if (v != 1) return false;

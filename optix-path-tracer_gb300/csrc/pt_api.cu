@@ -1325,7 +1325,7 @@ PT_API int pt_trace_first_hits(pt_context* ctx, int width, int height, int frame
   uint32_t* d_err = ctx->d_tmpu.p + 2 * WH;
   CK(cudaMemsetAsync(d_err, 0, 4, st));
   pt::launch_first_hits(ctx->scene, width, height, frame, ctx->d_tmpu.p, ctx->d_tmpu.p + WH,
-                        ctx->d_tmp.p, ctx->max_stack, d_err, st);
+                        ctx->d_tmp.p, ctx->max_stack, d_err, ctx->lc.trace_grid, st);
   CK(cudaGetLastError());
   uint32_t herr = 0;
   CK(cudaMemcpyAsync(prim, ctx->d_tmpu.p, WH * 4, cudaMemcpyDefault, st));

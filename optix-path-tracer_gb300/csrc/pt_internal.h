@@ -165,8 +165,21 @@ struct WaveState {
 #define PT_SLOT_F4 16
 #define PT_SLOT_U4 3
 
+/* Ray kinds of the trace kernels: closest hit of extension rays; closest
+ * hit of a shadow ray (reference mode: the light must be the first thing
+ * hit); first-hit queries; any hit before tmax (consistent-mode occlusion). */
+enum { TRACE_EXT = 0, TRACE_SHADOW = 1, TRACE_FIRST = 2, TRACE_OCCLUDED = 3 };
+
 namespace pt {
+/* Dynamic shared memory of a trace block (pt_trace.cu). */
 size_t trace_smem(int max_stack, int block);
+/* Resident trace blocks per SM (0 if the shape does not fit). */
+int trace_blocks_per_sm(int block, size_t smem);
+/* One trace launch of `mode` (TRACE_EXT, TRACE_SHADOW or TRACE_OCCLUDED)
+ * over the wavefront's rays, with the launch shape of lc. */
+void launch_trace(int mode, bool counters, const DevScene& S, const WaveState& W,
+                  const WaveCtl* ctl, int max_stack, const BatchRefs* br, const LaunchCfg& lc,
+                  cudaStream_t st);
 /* Resident blocks per SM x SMs for a trace (kind 0) or shade (kind 1)
  * kernel of `block` threads. */
 int wave_grid(int kind, int max_stack, int block);
@@ -206,8 +219,9 @@ void launch_accumulate(const float4* results, float4* acc, int w, int h, int fra
 void launch_accumulate64(const float4* results, double* acc, int w, int h, int frames,
                          cudaStream_t st);
 void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st);
+/* First hits of the camera rays of one frame (grid: blocks of PT_TRACE_BLOCK). */
 void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
-                       float* t, int max_stack, uint32_t* err, cudaStream_t st);
+                       float* t, int max_stack, uint32_t* err, int grid, cudaStream_t st);
 void launch_resolve(const float4* acc, uchar4* out, int n, int frame, cudaStream_t st);
 }  // namespace pt
 

@@ -31,564 +31,9 @@
 #include "pt_device.cuh"
 #include "pt_guide.cuh"
 #include "pt_internal.h"
+#include "pt_wave.cuh"
 
 using namespace ptd;
-
-__device__ __forceinline__ uint32_t gen_count(const WaveCounters& c, const WaveCtl& ctl,
-                                              uint32_t slots) {
-  unsigned long long left = ctl.chunk_paths - c.next_path;
-  return (uint32_t)min((unsigned long long)(slots - c.n_cur), left);
-}
-
-__device__ __forceinline__ Ray3 camera_ray(const GpuCamera& cam, uint32_t x, uint32_t y,
-                                           uint32_t Wd, uint32_t Hd, uint32_t& seed) {
-  float u = float((float)x + rnd(seed)) / (float)Wd;
-  float v = float((float)y + rnd(seed)) / (float)Hd;
-  V3 rd = cam.lens_radius * random_in_unit_disk(seed);
-  V3 lens_offset = v3(cam.ux, cam.uy, cam.uz) * rd.x + v3(cam.wx, cam.wy, cam.wz) * rd.y;
-  V3 origin = v3(cam.ox, cam.oy, cam.oz) + lens_offset;
-  V3 direction = v3(cam.lx, cam.ly, cam.lz) + u * v3(cam.hx, cam.hy, cam.hz) +
-                 v * v3(cam.vx, cam.vy, cam.vz) - origin;
-  Ray3 r;
-  r.o = make_float3(origin.x, origin.y, origin.z);
-  r.d = make_float3(direction.x, direction.y, direction.z);
-  return r;
-}
-
-// ------------------------------------------------------------ BVH8 trace --
-// Closest hit through the BVH8 with warp-collective leaf tests.
-//
-// Each lane traverses its own ray (node by node, near-to-far, one stack entry
-// per level: the group of a node's remaining internal children).  Primitive
-// tests are not run by the lane that reaches a leaf: after every node step
-// the warp gathers all (ray, primitive) pairs its lanes produced into shared
-// memory and the 32 lanes test them together, merging the results per ray
-// with a 64-bit atomicMin on (t, primitive id) - the order-independent
-// closest-hit rule of the oracle.  Per-lane leaf loops of 1..24 triangles
-// would otherwise serialise the warp.  A lane whose ray is done takes its
-// next ray at once (persistent threads), and a stack group whose nearest
-// child lies beyond the closest hit is dropped without visiting it.
-#define PT_MAX_PAIRS (32 * 24)
-
-struct WarpShared {
-  float4 ro[32];                  // origin, tmin
-  float4 rd[32];                  // direction, tmax
-  float4 wt[32];                  // watertight-test constants Sx, Sy, Sz, axes
-  unsigned long long best[32];    // (t bits << 32) | primitive id
-  uint32_t pair_prim[PT_MAX_PAIRS];
-  uint8_t pair_owner[PT_MAX_PAIRS];
-};
-
-__device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
-
-// Three-input max / min (one instruction each on sm_100+) and the paired
-// FP32 fused multiply-add: a node step evaluates 8 children x 3 axes of
-// (near, far) slab distances, so pairs share one instruction.
-__device__ __forceinline__ float max3f(float a, float b, float c) {
-  float r;
-  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-}
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-  float r;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-}
-// (a.x * s + t, a.y * s + t), each rounded once.
-__device__ __forceinline__ float2 fma2s(float ax, float ay, float s, float t) {
-  unsigned long long a, b, c, d;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(ax), "f"(ay));
-  asm("mov.b64 %0, {%1, %1};" : "=l"(b) : "f"(s));
-  asm("mov.b64 %0, {%1, %1};" : "=l"(c) : "f"(t));
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
-  return r;
-}
-
-__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
-  uint32_t lo = min(a, b), hi = max(a, b);
-  a = lo;
-  b = hi;
-}
-
-__device__ __forceinline__ WtRay wt_unpack(float4 w) {
-  WtRay r;
-  uint32_t k = __float_as_uint(w.w);
-  r.kx = (int)(k & 3u);
-  r.ky = (int)((k >> 2) & 3u);
-  r.kz = (int)((k >> 4) & 3u);
-  r.Sx = w.x;
-  r.Sy = w.y;
-  r.Sz = w.z;
-  return r;
-}
-
-// Candidate of one primitive for a world-space ray (object space inside).
-__device__ __forceinline__ bool prim_test(const DevScene& S, const PrimRec& p, V3 o, V3 d,
-                                          const WtRay& wt, float tmin, float tmax, float& t,
-                                          float& bu, float& bv) {
-  int type = prim_type(p);
-  bu = bv = 0.f;
-  if (type == PT_PRIM_TRIANGLE) return tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
-  V3 oo = o, dd = d;
-  int xf = prim_xform(p);
-  if (xf >= 0) {
-    const float4* I = S.xforms + 6 * xf + 3;
-    oo = xpoint(I, o);
-    dd = xvector(I, d);
-  }
-  if (type == PT_PRIM_SPHERE) return sphere_candidate(p, oo, dd, tmin, tmax, t);
-  if (type == PT_PRIM_RECT) return rect_candidate(p, oo, dd, tmin, tmax, t);
-  return box_candidate(p, oo, dd, tmin, tmax, t);
-}
-
-struct FirstHitOut {
-  uint32_t* prim;
-  uint32_t* mat;
-  float* t;
-  int width, height, frame;
-  uint32_t* err;
-};
-
-// TRACE_SHADOW: closest hit of a shadow ray (reference mode: the light must
-// be the first thing hit); TRACE_OCCLUDED: any hit before tmax (consistent
-// mode), traversed without ordering the children
-enum { TRACE_EXT = 0, TRACE_SHADOW = 1, TRACE_FIRST = 2, TRACE_OCCLUDED = 3 };
-
-#ifndef PT_ANYHIT_NEAREST
-#define PT_ANYHIT_NEAREST 1  // occlusion rays enter the nearest child first
-#endif
-
-size_t trace_smem_bytes(int max_stack, int block) {
-  return (size_t)(block / 32) * sizeof(WarpShared) +
-         (size_t)block * max_stack * (sizeof(uint2) + sizeof(float));
-}
-
-// BATCH: rays of several scenes; each starts at its scene's root node (the
-// scene index is in the path state word st.z).
-template <int MODE, bool COUNT, bool BATCH>
-__global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
-    k_trace_t(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp, int max_stack,
-              FirstHitOut fo, BatchRefs br, int refetch) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  WarpShared& ws = ((WarpShared*)smem)[threadIdx.x >> 5];
-  unsigned char* stk_base = smem + (blockDim.x >> 5) * sizeof(WarpShared);
-  uint2* stk = (uint2*)stk_base + threadIdx.x;
-  float* stkt = (float*)((uint2*)stk_base + (size_t)max_stack * blockDim.x) + threadIdx.x;
-  const int bd = blockDim.x;
-
-  uint32_t n;
-  WaveCounters c;
-  constexpr bool consistent = MODE == TRACE_OCCLUDED;
-  constexpr bool SHADOWRAY = MODE == TRACE_SHADOW || MODE == TRACE_OCCLUDED;
-  if (MODE == TRACE_EXT) {
-    c = *W.ctr;
-    n = c.n_cur + gen_count(c, *ctlp, (uint32_t)W.slots);
-  } else if (SHADOWRAY) {
-    n = W.ctr->n_shadow;
-  } else {
-    n = (uint32_t)fo.width * (uint32_t)fo.height;
-  }
-  // rays are handed out to warps in arrival order from a per-launch counter
-  // (first-hit queries: a fixed grid-stride assignment)
-  const uint32_t stride = gridDim.x * blockDim.x;
-  uint32_t* take = MODE == TRACE_EXT ? &W.ctr->ray_next[0] : (SHADOWRAY ? &W.ctr->ray_next[1] : nullptr);
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool started = false;
-  uint32_t nn = 0, np = 0;
-
-  // per-lane ray state (the direction and tmax of a lane's ray live in the
-  // warp's shared copy, ws.rd[lane]: the node tests need only o, tmin and
-  // the reciprocal direction)
-  const uint32_t parity = MODE == TRACE_EXT ? c.parity : 0u;
-  V3 o = v3(0.f);
-  float tmin = 0.f, ix = 0.f, iy = 0.f, iz = 0.f, tbest = 0.f;
-  bool negx = false, negy = false, negz = false;
-  uint32_t cur = 0, best_id = PT_NO_HIT;
-  int sp = 0;
-  bool active = false;
-
-  // loads ray i into o, d, tmin, tmax
-  auto load_ray = [&](V3& d, float& tmax) {
-    if (MODE == TRACE_EXT) {
-      float4 ro = W.path[parity].ray_o[i], rdv = W.path[parity].ray_d[i];
-      o = f4xyz(ro);
-      d = f4xyz(rdv);
-      tmin = ro.w;
-      tmax = rdv.w;
-    } else if (SHADOWRAY) {
-      o = f4xyz(W.sh.P[i]);
-      d = f4xyz(W.sh.Wi[i]);
-      tmin = 1e-3f;
-      tmax = consistent ? W.sh.C[i].w : PT_RAY_TMAX;
-    } else {
-      uint32_t x = i % (uint32_t)fo.width, y = i / (uint32_t)fo.width;
-      uint32_t seed = tea64((uint32_t)fo.width * y + x, (uint32_t)fo.frame);
-      Ray3 r = camera_ray(S.cam, x, y, fo.width, fo.height, seed);
-      o = v3(r.o.x, r.o.y, r.o.z);
-      d = v3(r.d.x, r.d.y, r.d.z);
-      tmin = 1e-6f;
-      tmax = PT_RAY_TMAX;
-    }
-  };
-
-  auto finish = [&](V3 d, float tmax) {
-    if (MODE == TRACE_EXT) {
-      float4 h = make_float4(tmax, 0.f, 0.f, __uint_as_float(PT_NO_HIT));
-      if (best_id != PT_NO_HIT) {
-        uint32_t leaf = __ldg(S.leaf_of_id + best_id);
-        PrimRec p = load_prim(S.prims, leaf);
-        float t = tbest, bu = 0.f, bv = 0.f;
-        if (prim_type(p) == PT_PRIM_TRIANGLE) tri_candidate(p, o, wt_setup(d), tmin, tmax, t, bu, bv);
-        h = make_float4(tbest, bu, bv, __uint_as_float(leaf));
-      }
-      W.hit[i] = h;
-    } else if (SHADOWRAY) {
-      bool occluded = true;
-      if (consistent) {
-        occluded = best_id != PT_NO_HIT;  // anything before the light
-      } else if (best_id != PT_NO_HIT) {
-        PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
-        bool is_light = S.mats[prim_material(p)].type == PT_MAT_DIFFUSE_LIGHT;
-        occluded = !(is_light && dot(f4xyz(W.sh.N[i]), d) > 0.f);
-      }
-      W.sh.Wi[i].w = occluded ? 1.f : 0.f;
-    } else {
-      if (best_id == PT_NO_HIT) {
-        fo.prim[i] = PT_NO_HIT;
-        fo.mat[i] = PT_NO_HIT;
-        fo.t[i] = 0.f;
-      } else {
-        PrimRec p = load_prim(S.prims, __ldg(S.leaf_of_id + best_id));
-        fo.prim[i] = best_id;
-        fo.mat[i] = prim_material(p);
-        fo.t[i] = tbest;
-      }
-    }
-  };
-
-  auto finish_traced = [&]() {
-    float4 rdv = ws.rd[lane];
-    finish(f4xyz(rdv), rdv.w);
-  };
-
-  bool idle = true;  // wants a ray (finished one, or none taken yet)
-  // loads ray i (< n) and sets up its traversal
-  auto fetch = [&]() {
-    // a ray with a NaN in its origin or direction hits nothing (every
-    // primitive test fails or yields a NaN distance, which never wins the
-    // closest-hit minimum), and neither does any ray of an empty scene: both
-    // end here, without a traversal (a NaN ray would pass every box test)
-    V3 d;
-    float tmax;
-    load_ray(d, tmax);
-    bool nan = !(o.x == o.x && o.y == o.y && o.z == o.z && d.x == d.x && d.y == d.y &&
-                 d.z == d.z);
-    if (nan || S.num_prims == 0) {
-      best_id = PT_NO_HIT;
-      tbest = tmax;
-      finish(d, tmax);
-      active = false;
-      idle = true;
-      return;
-    }
-    active = true;
-    const float eps = 1e-18f;
-    float dx = fabsf(d.x) < eps ? copysignf(eps, d.x) : d.x;
-    float dy = fabsf(d.y) < eps ? copysignf(eps, d.y) : d.y;
-    float dz = fabsf(d.z) < eps ? copysignf(eps, d.z) : d.z;
-    ix = 1.0f / dx;
-    iy = 1.0f / dy;
-    iz = 1.0f / dz;
-    negx = ix < 0.f;
-    negy = iy < 0.f;
-    negz = iz < 0.f;
-    WtRay w = wt_setup(d);
-    ws.ro[lane] = make_float4(o.x, o.y, o.z, tmin);
-    ws.rd[lane] = make_float4(d.x, d.y, d.z, tmax);
-    ws.wt[lane] = make_float4(w.Sx, w.Sy, w.Sz,
-                              __uint_as_float((uint32_t)w.kx | ((uint32_t)w.ky << 2) |
-                                              ((uint32_t)w.kz << 4)));
-    tbest = tmax;
-    best_id = PT_NO_HIT;
-    ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
-    cur = S.root;
-    if (BATCH) {
-      uint32_t z = MODE == TRACE_EXT ? W.path[parity].st[i].z : W.sh.st[i].z;
-      cur = __ldg(br.roots + (z >> PT_ST_SCENE_SHIFT));
-    }
-    sp = 0;
-  };
-
-  while (true) {
-    // idle lanes take and load their next rays together once `refetch`
-    // lanes wait (or nothing else runs), so the warp pays one load latency
-    // per batch; a lane whose index is past the end has no more work (the
-    // counter only grows)
-    uint32_t busy = __ballot_sync(0xffffffffu, active);
-    uint32_t waiting = __ballot_sync(0xffffffffu, idle);
-    if (waiting && (__popc(waiting) >= refetch || busy == 0)) {
-      if (MODE == TRACE_FIRST) {
-        if (idle) {
-          if (started) i += stride;
-          started = true;
-        }
-      } else {
-        const int leader = __ffs(waiting) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(take, (uint32_t)__popc(waiting));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (idle) i = base + (uint32_t)__popc(waiting & ((1u << lane) - 1u));
-      }
-      if (idle) {
-        idle = false;
-        if (i < n) fetch();
-      }
-      busy = __ballot_sync(0xffffffffu, active);
-      if (!busy) {
-        if (__ballot_sync(0xffffffffu, idle)) continue;  // only rays that ended at load
-        break;
-      }
-    }
-    if (!busy) break;
-    uint32_t leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0, kmin = 0xffffffffu, imask = 0;
-    uint32_t keys[8];
-    int nint = 0;
-#pragma unroll
-    for (int k = 0; k < 8; k++) keys[k] = 0xffffffffu;
-    if (active) {
-      const uint4* nptr = S.nodes + 5 * (size_t)cur;
-      uint4 n0 = __ldg(nptr), n1 = __ldg(nptr + 1), n2 = __ldg(nptr + 2), n3 = __ldg(nptr + 3),
-            n4 = __ldg(nptr + 4);
-      if (COUNT) nn++;
-      child_base = n1.x;
-      pbase = n1.y;
-      mlo = n1.z;
-      mhi = n1.w;
-      // child bound q (8 bits) is read as the float f = 1 + q * 2^-15 built by
-      // one byte permute; t = q*a + b = f*A + B with A = 2^15 a, B = b - A
-      float sx = __uint_as_float((n0.w & 0xffu) << 23);
-      float sy = __uint_as_float(((n0.w >> 8) & 0xffu) << 23);
-      float sz = __uint_as_float(((n0.w >> 16) & 0xffu) << 23);
-      float Ax = 32768.0f * (sx * ix), Ay = 32768.0f * (sy * iy), Az = 32768.0f * (sz * iz);
-      float Bx = (__uint_as_float(n0.x) - o.x) * ix - Ax;
-      float By = (__uint_as_float(n0.y) - o.y) * iy - Ay;
-      float Bz = (__uint_as_float(n0.z) - o.z) * iz - Az;
-      uint32_t nx0 = negx ? n3.z : n2.x, nx1 = negx ? n3.w : n2.y;
-      uint32_t fx0 = negx ? n2.x : n3.z, fx1 = negx ? n2.y : n3.w;
-      uint32_t ny0 = negy ? n4.x : n2.z, ny1 = negy ? n4.y : n2.w;
-      uint32_t fy0 = negy ? n2.z : n4.x, fy1 = negy ? n2.w : n4.y;
-      uint32_t nz0 = negz ? n4.z : n3.x, nz1 = negz ? n4.w : n3.y;
-      uint32_t fz0 = negz ? n3.x : n4.z, fz1 = negz ? n3.y : n4.w;
-      float tlim = tbest * 1.0000005f;
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        const uint32_t sel = 0x7604u | ((uint32_t)(k & 3) << 4);
-        uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
-        float2 tx = fma2s(__uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x3F800000u, sel)),
-                          __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x3F800000u, sel)), Ax, Bx);
-        float2 ty = fma2s(__uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x3F800000u, sel)),
-                          __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x3F800000u, sel)), Ay, By);
-        float2 tz = fma2s(__uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x3F800000u, sel)),
-                          __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x3F800000u, sel)), Az, Bz);
-        float tn = max3f(tx.x, ty.x, fmaxf(tz.x, tmin));
-        float tf = min3f(tx.y, ty.y, fminf(tz.y, tlim));
-        // an empty slot (meta 0) has an inverted box and fails here; were it
-        // to pass (infinite slab distances), it is a leaf of no primitives
-        if (tn <= tf) {
-          if (consistent && (meta & 0x80u)) {
-            imask |= 1u << (meta & 7u);
-            if (PT_ANYHIT_NEAREST) kmin = min(kmin, (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u));
-          } else if (meta & 0x80u) {
-            uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (meta & 7u);
-            keys[k] = key;
-            kmin = min(kmin, key);
-            nint++;
-          } else {
-            leafmask |= 1u << k;
-          }
-        }
-      }
-    }
-    // ---- warp-collective primitive tests
-    uint32_t cnt = 0;
-    {
-      uint32_t m = leafmask;
-      while (m) {
-        int k = __ffs(m) - 1;
-        m &= m - 1;
-        cnt += byte_of(k < 4 ? mlo : mhi, k & 3) >> 5;
-      }
-    }
-    uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
-    uint32_t mx = __reduce_max_sync(0xffffffffu, cnt);
-    if (total && mx * 32u <= 2u * total) {
-      // balanced: each lane tests its own primitives (at least half the
-      // lane-slots do work)
-      uint32_t m = leafmask;
-      float4 w4 = ws.wt[lane];
-      WtRay wt = wt_unpack(w4);
-      unsigned long long bk = ws.best[lane];
-      const float4 rdv = ws.rd[lane];
-      while (m) {
-        int k = __ffs(m) - 1;
-        m &= m - 1;
-        uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
-        uint32_t first = pbase + (meta & 31u);
-        for (uint32_t q = 0; q < (meta >> 5); q++) {
-          PrimRec p = load_prim(S.prims, first + q);
-          if (COUNT) np++;
-          float t, bu, bv;
-          if (prim_test(S, p, o, f4xyz(rdv), wt, tmin, rdv.w, t, bu, bv)) {
-            unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
-            bk = min(bk, key);
-          }
-        }
-      }
-      if (cnt) {
-        ws.best[lane] = bk;
-        tbest = __uint_as_float((uint32_t)(bk >> 32));
-        best_id = (uint32_t)bk;
-      }
-    } else if (total) {
-      // unbalanced: spread the (ray, primitive) pairs over the warp
-      uint32_t incl = cnt;
-#pragma unroll
-      for (int dd = 1; dd < 32; dd <<= 1) {
-        uint32_t t = __shfl_up_sync(0xffffffffu, incl, dd);
-        if (lane >= dd) incl += t;
-      }
-      uint32_t off = incl - cnt;
-      uint32_t m = leafmask;
-      while (m) {
-        int k = __ffs(m) - 1;
-        m &= m - 1;
-        uint32_t meta = byte_of(k < 4 ? mlo : mhi, k & 3);
-        uint32_t first = pbase + (meta & 31u);
-        for (uint32_t q = 0; q < (meta >> 5); q++) {
-          ws.pair_prim[off] = first + q;
-          ws.pair_owner[off] = (uint8_t)lane;
-          off++;
-        }
-      }
-      __syncwarp();
-      for (uint32_t j = lane; j < total; j += 32) {
-        uint32_t pi = ws.pair_prim[j];
-        uint32_t ow = ws.pair_owner[j];
-        PrimRec p = load_prim(S.prims, pi);
-        if (COUNT) np++;
-        float4 ro = ws.ro[ow], rdv = ws.rd[ow];
-        float t, bu, bv;
-        if (prim_test(S, p, f4xyz(ro), f4xyz(rdv), wt_unpack(ws.wt[ow]), ro.w, rdv.w, t, bu, bv)) {
-          unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
-          atomicMin(&ws.best[ow], key);
-        }
-      }
-      __syncwarp();
-      if (active) {
-        unsigned long long k = ws.best[lane];
-        tbest = __uint_as_float((uint32_t)(k >> 32));
-        best_id = (uint32_t)k;
-      }
-    }
-    // ---- consistent-mode shadow rays ask only whether anything lies before
-    // tmax: the first confirmed hit ends the ray
-    if (consistent && active && best_id != PT_NO_HIT) {
-      finish_traced();
-      active = false;
-      idle = true;
-    }
-    // ---- occlusion rays: the nearest hit child (or the lowest slot), the
-    // others pushed as one mask and taken lowest slot first
-    if (consistent && active) {
-      if (imask) {
-        uint32_t b = PT_ANYHIT_NEAREST ? (kmin & 7u) : (uint32_t)(__ffs(imask) - 1);
-        cur = child_base + b;
-        imask &= ~(1u << b);
-        if (imask) {
-          if (sp >= max_stack) {
-            atomicOr(&W.ctr->error, 1u);
-            sp = 0;  // abandon this ray (the host reports the error)
-            finish_traced();
-            active = false;
-            idle = true;
-          } else {
-            stk[sp * bd] = make_uint2(child_base, imask);
-            sp++;
-          }
-        }
-      } else if (sp > 0) {
-        uint2 e = stk[(sp - 1) * bd];
-        cur = e.x + (uint32_t)(__ffs(e.y) - 1);
-        e.y &= e.y - 1;
-        if (e.y == 0) sp--;
-        else stk[(sp - 1) * bd].y = e.y;
-      } else {
-        finish_traced();
-        active = false;
-        idle = true;
-      }
-    }
-    // ---- next node: nearest internal child, else the deepest pending group
-    if (!consistent && active) {
-      if (nint == 1) {
-        cur = child_base + (kmin & 7u);
-      } else if (nint > 1) {
-        cswap(keys[0], keys[1]); cswap(keys[2], keys[3]); cswap(keys[4], keys[5]); cswap(keys[6], keys[7]);
-        cswap(keys[0], keys[2]); cswap(keys[1], keys[3]); cswap(keys[4], keys[6]); cswap(keys[5], keys[7]);
-        cswap(keys[1], keys[2]); cswap(keys[5], keys[6]); cswap(keys[0], keys[4]); cswap(keys[3], keys[7]);
-        cswap(keys[1], keys[5]); cswap(keys[2], keys[6]);
-        cswap(keys[1], keys[4]); cswap(keys[3], keys[6]);
-        cswap(keys[2], keys[4]); cswap(keys[3], keys[5]);
-        cswap(keys[3], keys[4]);
-        uint32_t list = 0;
-#pragma unroll
-        for (int j = 7; j >= 1; j--)
-          if (j < nint) list = (list << 3) | (keys[j] & 7u);
-        if (sp >= max_stack) {
-          atomicOr(MODE == TRACE_FIRST ? fo.err : &W.ctr->error, 1u);
-          sp = 0;  // abandon this ray (the host reports the error)
-          finish_traced();
-          active = false;
-          idle = true;
-        } else {
-          stk[sp * bd] = make_uint2(child_base, list | ((uint32_t)(nint - 1) << 24));
-          stkt[sp * bd] = __uint_as_float(keys[1] & 0xfffffff8u);  // nearest remaining child
-          sp++;
-          cur = child_base + (keys[0] & 7u);
-        }
-      } else {
-        bool found = false;
-        float tlim = tbest * 1.0000005f;
-        while (sp > 0) {
-          uint2 e = stk[(sp - 1) * bd];
-          if (stkt[(sp - 1) * bd] > tlim) {  // every child of the group starts beyond the hit
-            sp--;
-            continue;
-          }
-          uint32_t cn = e.y >> 24, list = e.y & 0xffffffu;
-          cur = e.x + (list & 7u);
-          cn--;
-          if (cn == 0) sp--;
-          else stk[(sp - 1) * bd] = make_uint2(e.x, (list >> 3) | (cn << 24));
-          found = true;
-          break;
-        }
-        if (!found) {
-          finish_traced();
-          active = false;
-          idle = true;
-        }
-      }
-    }
-  }
-  if (COUNT) {
-    atomicAdd(&W.ctr->node_fetches, (unsigned long long)nn);
-    atomicAdd(&W.ctr->prim_tests, (unsigned long long)np);
-  }
-}
 
 // -------------------------------------------------- warp-aggregated push --
 __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool active) {
@@ -1756,14 +1201,11 @@ static int num_sms() {
   return g_num_sms;
 }
 
-size_t trace_smem(int max_stack, int block) { return trace_smem_bytes(max_stack, block); }
-
 int wave_grid(int kind, int max_stack, int block) {
   int blocks = 0;
   cudaError_t e = cudaSuccess;
   if (kind == 0)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace_t<TRACE_EXT, false, false>,
-                                                      block, trace_smem(max_stack, block));
+    blocks = trace_blocks_per_sm(block, trace_smem(max_stack, block));
   else
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false, true, false>, block, 0);
   if (e != cudaSuccess || blocks < 1) {
@@ -1783,46 +1225,6 @@ LaunchCfg default_launch(int max_stack) {
   lc.trace_grid = wave_grid(0, max_stack, lc.trace_block);
   lc.shade_grid = wave_grid(1, max_stack, lc.shade_block);
   return lc;
-}
-
-// Dynamic shared memory limit of kernel k: the per-block opt-in maximum
-// minus its static shared memory.
-template <typename K>
-static cudaError_t smem_attr(K k, int optin) {
-  cudaFuncAttributes fa;
-  cudaError_t e = cudaFuncGetAttributes(&fa, k);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              optin - (int)fa.sharedSizeBytes);
-}
-
-static const int kMaxDev = 64;
-static bool g_smem_set[kMaxDev];
-
-cudaError_t set_trace_smem() {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev >= 0 && dev < kMaxDev && g_smem_set[dev]) return cudaSuccess;
-  int optin = 0;
-  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
-      cudaSuccess)
-    return e;
-  if ((e = smem_attr(k_trace_t<TRACE_EXT, false, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_EXT, true, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_EXT, false, true>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_EXT, true, true>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, false, true>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_SHADOW, true, true>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, false, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, true, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, false, true>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_OCCLUDED, true, true>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_FIRST, false, false>, optin)) != cudaSuccess) return e;
-  if (dev >= 0 && dev < kMaxDev) g_smem_set[dev] = true;
-  return cudaSuccess;
 }
 
 // The shading kernel of the integrator mode, guide, tile order and texture
@@ -1847,9 +1249,8 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
                                int max_stack, bool counters, const LaunchCfg& lc, cudaStream_t st,
                                cudaEvent_t* ev, int mode, const BatchRefs& br, bool use_cond,
                                unsigned long long cond, const GuideInferArgs* gi) {
-  size_t sm = trace_smem(max_stack, lc.trace_block);
-  FirstHitOut none{};
-  const int tb = lc.trace_block, tg = lc.trace_grid, sb = lc.shade_block, sg = lc.shade_grid;
+  const int sb = lc.shade_block, sg = lc.shade_grid;
+  const BatchRefs* brp = BATCH ? &br : nullptr;
   // sorted shading: one block per tile of the buffer (blocks past the live
   // paths return at once), so the block scheduler balances uneven tiles
   const int tile = sb * PT_SORT_ITEMS;
@@ -1861,10 +1262,7 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
   k_generate<BATCH><<<sg, sb, 0, st>>>(S, W, ctl, br);
   if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
-  if (counters)
-    k_trace_t<TRACE_EXT, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
-  else
-    k_trace_t<TRACE_EXT, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
+  launch_trace(TRACE_EXT, counters, S, W, ctl, max_stack, brp, lc, st);
   if (ev) cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal);
   if (mode == 1 && gi) launch_guide_infer(S, W, ctl, *gi, 2 * num_sms(), st);
   if (lc.tex)
@@ -1872,14 +1270,8 @@ static void launch_iteration_t(const DevScene& S, const WaveState& W, const Wave
   else
     launch_shade<BATCH, false>(S, W, ctl, br, mode, gi != nullptr, lc.sort, tgs, sg, sb, st);
   if (ev) cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal);
-  if (mode == 1 && counters)
-    k_trace_t<TRACE_OCCLUDED, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
-  else if (mode == 1)
-    k_trace_t<TRACE_OCCLUDED, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
-  else if (counters)
-    k_trace_t<TRACE_SHADOW, true, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
-  else
-    k_trace_t<TRACE_SHADOW, false, BATCH><<<tg, tb, sm, st>>>(S, W, ctl, max_stack, none, br, lc.refetch);
+  launch_trace(mode == 1 ? TRACE_OCCLUDED : TRACE_SHADOW, counters, S, W, ctl, max_stack, brp, lc,
+               st);
   if (ev) cudaEventRecordWithFlags(ev[4], st, cudaEventRecordExternal);
   if (mode == 1)
     k_finish_c<<<sg, sb, 0, st>>>(S, W, ctl);
@@ -1938,15 +1330,6 @@ void launch_accumulate64(const float4* results, double* acc, int w, int h, int f
 
 void launch_paths_out(const float4* results, float* out, uint32_t n, cudaStream_t st) {
   k_paths_out<<<num_sms() * 8, 256, 0, st>>>(results, out, n);
-}
-
-void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
-                       float* t, int max_stack, uint32_t* err, cudaStream_t st) {
-  FirstHitOut fo{prim, mat, t, w, h, frame, err};
-  WaveState none{};
-  k_trace_t<TRACE_FIRST, false, false>
-      <<<num_sms() * 4, PT_TRACE_BLOCK, trace_smem(max_stack, PT_TRACE_BLOCK), st>>>(
-          S, none, nullptr, max_stack, fo, BatchRefs{}, 32);
 }
 
 void launch_env_cdf(const float4* env, int w, int h, float* marg, float* cond, double* rows,

@@ -20,7 +20,9 @@
  *   n4 = (qhi.y[0..3], qhi.y[4..7], qhi.z[0..3], qhi.z[4..7])
  *   child box = p + q * 2^(e-127) per axis (q: 8-bit, rounded outward)
  *   meta[i] = 0: empty slot (its box inverted: qlo 255, qhi 0);
- *             0x80 | r: internal child, node child_base + r;
+ *             0x80 | r: internal child, node child_base + r; internal
+ *             children fill slots 0..7 first, so r == i and imask is
+ *             (1 << internal children) - 1;
  *             (count << 5) | off (count 1..3): leaf, prims prim_base + off ..
  */
 #ifndef PT_TYPES_H

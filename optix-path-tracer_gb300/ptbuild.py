@@ -22,7 +22,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
     "-I", CSRC,
 ]
-SOURCES = ["pt_kernels.cu", "pt_api.cu", "pt_batch.cu", "pt_guide.cu", "pt_guide_host.cu", "bvh_host.cpp",
+SOURCES = ["pt_kernels.cu", "pt_trace.cu", "pt_api.cu", "pt_batch.cu", "pt_guide.cu", "pt_guide_host.cu", "bvh_host.cpp",
            "bvh_gpu.cu", "pt_io.cpp", "pt_image.cpp"]
 
 

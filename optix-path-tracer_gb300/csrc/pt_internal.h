@@ -12,9 +12,8 @@
 #ifndef PT_TRACE_BLOCK
 #define PT_TRACE_BLOCK 128       /* default threads per trace block */
 #endif
-#define PT_TRACE_MAXTHREADS 256  /* largest trace block the kernels are compiled for */
-#ifndef PT_TRACE_MINBLOCKS
-#define PT_TRACE_MINBLOCKS 3     /* of 256 threads: <= 80 registers per thread, no spills */
+#ifndef PT_TRACE_MAXREG
+#define PT_TRACE_MAXREG 72       /* registers per trace thread: 7 blocks of 128 per SM */
 #endif
 #define PT_SHADE_BLOCK 256       /* default and largest shade block */
 #ifndef PT_SHADE_MINBLOCKS

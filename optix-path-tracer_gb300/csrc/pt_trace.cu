@@ -20,8 +20,11 @@ using namespace ptd;
 // ------------------------------------------------------------ BVH8 trace --
 // Closest hit through the BVH8 with warp-collective leaf tests.
 //
-// Each lane traverses its own ray (node by node, near-to-far, one stack entry
-// per level: the group of a node's remaining internal children).  Primitive
+// Each lane traverses its own ray node by node: into the nearest hit
+// internal child, with one stack entry per level for the group of the
+// node's other hit internal children (the second nearest taken first, the
+// rest in slot order: a node step hits at most two internal children in
+// nearly every case, so two running minima replace a full sort).  Primitive
 // tests are not run by the lane that reaches a leaf: after every node step
 // the warp gathers all (ray, primitive) pairs its lanes produced into shared
 // memory and the 32 lanes test them together, merging the results per ray
@@ -77,12 +80,6 @@ __device__ __forceinline__ float2 fma2s(float ax, float ay, float s, float t) {
   return r;
 }
 
-__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
-  uint32_t lo = min(a, b), hi = max(a, b);
-  a = lo;
-  b = hi;
-}
-
 __device__ __forceinline__ WtRay wt_unpack(float4 w) {
   WtRay r;
   uint32_t k = __float_as_uint(w.w);
@@ -129,11 +126,7 @@ struct FirstHitOut {
 // BATCH: rays of several scenes; each starts at its scene's root node (the
 // scene index is in the path state word st.z).
 template <int MODE, bool COUNT, bool BATCH>
-#ifdef PT_TRACE_MAXREG
 __global__ void __maxnreg__(PT_TRACE_MAXREG)
-#else
-__global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
-#endif
     k_trace_t(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp, int max_stack,
               FirstHitOut fo, BatchRefs br, int refetch) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -334,7 +327,9 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
     // Internal children fill the low slots, slot == offset of the child node
     // from child_base; leaf children follow.
     uint32_t ihit = 0, leafmask = 0, pbase = 0, mlo = 0, mhi = 0, child_base = 0;
-    uint32_t keys[8];
+    // the two nearest hit internal children: entry distance (tn >= 0, so its
+    // bits order like the value) with the slot in the low 3 bits
+    uint32_t k1 = 0xffffffffu, k2 = 0xffffffffu;
     if (active) {
       const uint4* nptr = S.nodes + 5 * (size_t)cur;
       uint4 n0 = __ldg(nptr), n1 = __ldg(nptr + 1), n2 = __ldg(nptr + 2), n3 = __ldg(nptr + 3),
@@ -374,12 +369,11 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         float tf = min3f(tx.y, ty.y, fminf(tz.y, tlim));
         // an empty slot (meta 0) has an inverted box and fails here; were it
         // to pass (infinite slab distances), it is a leaf of no primitives.
-        // Sort key of a hit internal child: entry distance (tn >= 0, so its
-        // bits order like the value) with the slot in the low 3 bits.
-        keys[k] = 0xffffffffu;
         if (tn <= tf) {
           if ((im >> k) & 1u) {
-            keys[k] = (__float_as_uint(tn) & 0xfffffff8u) | (uint32_t)k;
+            const uint32_t key = (__float_as_uint(tn) & 0xfffffff8u) | (uint32_t)k;
+            k2 = min(k2, max(k1, key));
+            k1 = min(k1, key);
             ihit |= 1u << k;
           } else {
             leafmask |= 1u << k;
@@ -399,11 +393,7 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
       if (consistent) {
         if (ihit) {
           uint32_t b = (uint32_t)(__ffs(ihit) - 1);
-          if (PT_ANYHIT_NEAREST) {
-            uint32_t kmin = min(min(min(keys[0], keys[1]), min(keys[2], keys[3])),
-                                min(min(keys[4], keys[5]), min(keys[6], keys[7])));
-            b = kmin & 7u;
-          }
+          if (PT_ANYHIT_NEAREST) b = k1 & 7u;
           cur = child_base + b;
           const uint32_t rest = ihit & ~(1u << b);
           if (rest) {
@@ -425,33 +415,22 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
         } else {
           end_ray();
         }
-      } else if (nint == 1) {
-        const uint32_t kmin = min(min(min(keys[0], keys[1]), min(keys[2], keys[3])),
-                                  min(min(keys[4], keys[5]), min(keys[6], keys[7])));
-        cur = child_base + (kmin & 7u);
-        tnext = __uint_as_float(kmin & 0xfffffff8u);
-      } else if (nint > 1) {
-        cswap(keys[0], keys[1]); cswap(keys[2], keys[3]); cswap(keys[4], keys[5]); cswap(keys[6], keys[7]);
-        cswap(keys[0], keys[2]); cswap(keys[1], keys[3]); cswap(keys[4], keys[6]); cswap(keys[5], keys[7]);
-        cswap(keys[1], keys[2]); cswap(keys[5], keys[6]); cswap(keys[0], keys[4]); cswap(keys[3], keys[7]);
-        cswap(keys[1], keys[5]); cswap(keys[2], keys[6]);
-        cswap(keys[1], keys[4]); cswap(keys[3], keys[6]);
-        cswap(keys[2], keys[4]); cswap(keys[3], keys[5]);
-        cswap(keys[3], keys[4]);
-        uint32_t list = 0;
-#pragma unroll
-        for (int j = 7; j >= 1; j--)
-          if (j < nint) list = (list << 3) | (keys[j] & 7u);
-        if (sp >= max_stack) {
-          atomicOr(MODE == TRACE_FIRST ? fo.err : &W.ctr->error, 1u);
-          sp = 0;  // abandon this ray (the host reports the error)
-          end_ray();
-        } else {
-          stk[sp * bd] = make_uint2(child_base, list | ((uint32_t)(nint - 1) << 24));
-          stkt[sp * bd] = __uint_as_float(keys[1] & 0xfffffff8u);  // nearest remaining child
-          sp++;
-          cur = child_base + (keys[0] & 7u);
-          tnext = __uint_as_float(keys[0] & 0xfffffff8u);
+      } else if (nint >= 1) {
+        cur = child_base + (k1 & 7u);
+        tnext = __uint_as_float(k1 & 0xfffffff8u);
+        if (nint > 1) {
+          // pending group: the other hit children as a slot mask, the second
+          // nearest marked to be taken first (the rest in slot order), and
+          // the entry distance of the second nearest, below every one of them
+          if (sp >= max_stack) {
+            atomicOr(MODE == TRACE_FIRST ? fo.err : &W.ctr->error, 1u);
+            sp = 0;  // abandon this ray (the host reports the error)
+            end_ray();
+          } else {
+            stk[sp * bd] = make_uint2(child_base, (ihit & ~(1u << (k1 & 7u))) | ((k2 & 7u) << 8) | 0x800u);
+            stkt[sp * bd] = __uint_as_float(k2 & 0xfffffff8u);
+            sp++;
+          }
         }
       } else {
         pop = true;
@@ -560,11 +539,12 @@ __global__ void __launch_bounds__(PT_TRACE_MAXTHREADS, PT_TRACE_MINBLOCKS)
             sp--;
             continue;
           }
-          uint32_t cn = e.y >> 24, list = e.y & 0xffffffu;
-          cur = e.x + (list & 7u);
-          cn--;
-          if (cn == 0) sp--;
-          else stk[(sp - 1) * bd] = make_uint2(e.x, (list >> 3) | (cn << 24));
+          uint32_t m = e.y & 0xffu;
+          const uint32_t slot = (e.y & 0x800u) ? (e.y >> 8) & 7u : (uint32_t)(__ffs(m) - 1);
+          m &= ~(1u << slot);
+          cur = e.x + slot;
+          if (m == 0) sp--;
+          else stk[(sp - 1) * bd].y = m;
           found = true;
           break;
         }

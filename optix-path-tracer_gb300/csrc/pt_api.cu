@@ -938,6 +938,7 @@ PT_API int pt_commit(pt_context* ctx) {
   S.tex_list = ctx->d_tex_list.p;
   S.num_lights = (int)ctx->lights.size();
   S.num_prims = (int)n;
+  S.tri_only = pth::all_triangles(ctx) ? 1 : 0;
   S.miss = ctx->miss;
   S.miss.env = ctx->d_env.p;
   S.cam = ctx->cam;
@@ -1123,6 +1124,12 @@ static void reset_render_stats(pt_context* ctx) {
 // the whole warp; rays through a small scene are short and alike.  (GB300,
 // 1080p: 2.1M-triangle heightfield 24 lanes +6% over 32; 488 spheres 32
 // lanes +1% over 24.)
+bool pth::all_triangles(const pt_context* ctx) {
+  for (const HostPrim& p : ctx->prims)
+    if (p.type != PT_PRIM_TRIANGLE) return false;
+  return true;
+}
+
 int pth::auto_refetch(size_t num_prims) { return num_prims > ((size_t)1 << 16) ? 24 : 32; }
 
 bool pth::sort_pays(const pt_context* ctx) {

@@ -254,6 +254,9 @@ static int ensure_geometry(pt_batch* b, const pt_batch_item* items, int n) {
   S.leaf_of_id = b->leaf_of_id.p;
   S.num_prims = (int)P;
   S.root = 0;
+  S.tri_only = 1;
+  for (const pt_context* c : ctxs)
+    if (!pth::all_triangles(c)) S.tri_only = 0;
   b->max_stack = max_depth + 1;
   b->total_nodes = N;
   b->parts_width = width;

@@ -163,6 +163,8 @@ void carve_wave(WaveState& W, float4* f, uint4* u, size_t slots);
 int device_ptr_kind(const void* p, int device);
 /* Whether some material of the scene takes a texture. */
 bool uses_textures(const pt_context* ctx);
+/* Whether every primitive of the scene is a triangle. */
+bool all_triangles(const pt_context* ctx);
 /* Whether shading in material-sorted tiles pays for this scene: it does when
  * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
  * is present, whose code paths diverge most in a mixed warp. */

@@ -96,8 +96,9 @@ __device__ __forceinline__ WtRay wt_unpack(float4 w) {
 __device__ __forceinline__ bool prim_test(const DevScene& S, const PrimRec& p, V3 o, V3 d,
                                           const WtRay& wt, float tmin, float tmax, float& t,
                                           float& bu, float& bv) {
-  int type = prim_type(p);
   bu = bv = 0.f;
+  if (S.tri_only) return tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
+  int type = prim_type(p);
   if (type == PT_PRIM_TRIANGLE) return tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
   V3 oo = o, dd = d;
   int xf = prim_xform(p);

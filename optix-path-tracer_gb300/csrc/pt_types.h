@@ -122,7 +122,7 @@ struct DevScene {
   int num_lights;
   int num_prims;
   uint32_t root;            /* BVH8 node where traversal starts (0 for one scene) */
-  int pad;
+  int tri_only;             /* every primitive is a triangle (no type dispatch in traversal) */
   const GpuTexture* textures;
   const float4* tex_data;   /* image texels (rgba, row 0 at v = 0) and noise tables */
   const int* tex_list;      /* entries of vector textures */

@@ -40,7 +40,7 @@ const float PI_F = 3.141592654f;
 }  // namespace
 
 #ifndef PT_TREELET_ROUNDS
-#define PT_TREELET_ROUNDS 4  /* SAH treelet restructuring passes of the GPU builder */
+#define PT_TREELET_ROUNDS 2  /* SAH treelet restructuring passes of the GPU builder */
 #endif
 
 using namespace pth;

@@ -264,6 +264,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
     G.eval_out.release();
     G.out.release();
     G.rows.release();
+    G.feat.release();
     G.rec.release();
     G.coll_u.release();
     G.coll_f.release();
@@ -1175,6 +1176,7 @@ static int render_device(pt_context* ctx, const pt_render_params* p, void* d_acc
     if (!ctx->guide.ready && (rc = pt_guide_init(ctx, 0)) != PT_OK) return rc;
     CK(ctx->guide.out.ensure((size_t)ctx->slots));
     CK(ctx->guide.rows.ensure((size_t)ctx->slots));
+    CK(ctx->guide.feat.ensure(3 * (size_t)ctx->slots));
     ctx->W.guide = ctx->guide.out.p;
   }
   if (p->frame0 == 0) CK(cudaMemsetAsync(d_acc, 0, WH * (acc64 ? 32 : 16), st));

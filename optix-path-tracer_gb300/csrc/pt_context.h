@@ -66,6 +66,7 @@ struct GuideState {
   DevBuf<float> eval_out;
   DevBuf<GuidePacked> out;   // per path slot: decoded guide
   DevBuf<uint32_t> rows;     // per path slot: positions selected for inference
+  DevBuf<float4> feat;       // per path slot: their hit records (3 float4)
   DevBuf<GuideSample> rec;   // training records of the current frame
   DevBuf<uint32_t> coll_u;   // record collection scratch: per-block counts and offsets
   DevBuf<float> coll_f;      //   and per-block weight sums

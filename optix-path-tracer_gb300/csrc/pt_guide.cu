@@ -508,11 +508,14 @@ __device__ __forceinline__ bool group_and(bool v, int id) {
 
 // Lists the positions of the current buffer whose path needs a guide at
 // this bounce (depth below the guided-bounce limit, a hit on a non-delta
-// material), so that inference runs the network on those rows only; the
+// material), so that inference runs the network on those rows only, and
+// writes each listed row's hit record (point, shading normal, Wo): the chain
+// of dependent loads behind it (hit, primitive record, material, ray) runs
+// here, at full occupancy, instead of in front of the inference MMAs.  The
 // list order does not matter (rows are independent).
 __global__ void __launch_bounds__(256) k_guide_select(DevScene S, WaveState W,
                                                       const WaveCtl* __restrict__ ctlp,
-                                                      uint32_t* rows) {
+                                                      uint32_t* rows, float4* feat) {
   const WaveCounters c = *W.ctr;
   const WaveCtl ctl = *ctlp;
   unsigned long long left = ctl.chunk_paths - c.next_path;
@@ -525,13 +528,19 @@ __global__ void __launch_bounds__(256) k_guide_select(DevScene S, WaveState W,
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t it = 0; it < iters; it++, i += stride) {
     bool take = false;
+    HitRecord rec;
     if (i < n && (pb.st[i].z & PT_ST_DEPTH_MASK) < ctl.guide_depth) {
-      uint32_t leaf = __float_as_uint(W.hit[i].w);
+      const float4 hit = W.hit[i];
+      const uint32_t leaf = __float_as_uint(hit.w);
       if (leaf != PT_NO_HIT) {
-        uint32_t mid = __float_as_uint(__ldg(&S.prims[3 * (size_t)leaf + 2].w));
-        int type = __ldg(&S.mats[mid].type);
+        const PrimRec p = load_prim(S.prims, leaf);
+        const int type = __ldg(&S.mats[prim_material(p)].type);
         take = type == PT_MAT_LAMBERTIAN || type == PT_MAT_OREN_NAYAR ||
                type == PT_MAT_TORRANCE_SPARROW || type == PT_MAT_ASHIKHMIN_SHIRLEY;
+        if (take) {
+          const float4 ro = pb.ray_o[i], rd = pb.ray_d[i];
+          rec = hit_record(S, p, f4xyz(ro), f4xyz(rd), hit.x, hit.y, hit.z, false);
+        }
       }
     }
     uint32_t mask = __ballot_sync(0xffffffffu, take);
@@ -540,7 +549,14 @@ __global__ void __launch_bounds__(256) k_guide_select(DevScene S, WaveState W,
     uint32_t base = 0;
     if (lane == leader) base = atomicAdd(&W.ctr->guide_rows, (uint32_t)__popc(mask));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (take) rows[base + __popc(mask & ((1u << lane) - 1u))] = i;
+    if (take) {
+      const uint32_t li = base + __popc(mask & ((1u << lane) - 1u));
+      rows[li] = i;
+      feat[3 * (size_t)li] = make_float4(rec.P.x, rec.P.y, rec.P.z, 0.f);
+      feat[3 * (size_t)li + 1] =
+          make_float4(rec.shading_normal.x, rec.shading_normal.y, rec.shading_normal.z, 0.f);
+      feat[3 * (size_t)li + 2] = make_float4(rec.Wo.x, rec.Wo.y, rec.Wo.z, 0.f);
+    }
   }
 }
 
@@ -562,7 +578,6 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
   const int bar_id = 1 + grp;
   unsigned char* T = sm + kWeights + grp * kTileT;
   const WaveCounters c = *W.ctr;
-  const WaveCtl ctl = *ctlp;
   const uint32_t nl = min(c.guide_rows, (uint32_t)W.slots);  // listed by k_guide_select
   const uint32_t ntiles = (nl + 127) / 128;
   if (blockIdx.x * 2 >= ntiles) return;  // no tile for this CTA: skip the setup
@@ -585,28 +600,17 @@ __global__ void __launch_bounds__(256) k_guide_infer(DevScene S, WaveState W,
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   uint32_t phase = 0;
   bool failed = false;
-  const PathBuf& pb = W.path[c.parity];
   for (uint32_t tile = blockIdx.x * 2 + grp; tile < ntiles; tile += gridDim.x * 2) {
     const uint32_t li = tile * 128 + row;
-    const uint32_t i = li < nl ? A.rows[li] : 0xffffffffu;
-    bool valid = false;
+    const bool valid = li < nl;  // every listed row needs a guide
+    const uint32_t i = valid ? A.rows[li] : 0xffffffffu;
     float P[3], N[3], Wo[3];
-    if (i < (uint32_t)W.slots && (pb.st[i].z & PT_ST_DEPTH_MASK) < ctl.guide_depth) {
-      float4 hit = W.hit[i];
-      uint32_t leaf = __float_as_uint(hit.w);
-      if (leaf != PT_NO_HIT) {
-        PrimRec p = load_prim(S.prims, leaf);
-        int type = S.mats[prim_material(p)].type;
-        if (type == PT_MAT_LAMBERTIAN || type == PT_MAT_OREN_NAYAR ||
-            type == PT_MAT_TORRANCE_SPARROW || type == PT_MAT_ASHIKHMIN_SHIRLEY) {
-          float4 ro = pb.ray_o[i], rd = pb.ray_d[i];
-          HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rd), hit.x, hit.y, hit.z, false);
-          P[0] = rec.P.x; P[1] = rec.P.y; P[2] = rec.P.z;
-          N[0] = rec.shading_normal.x; N[1] = rec.shading_normal.y; N[2] = rec.shading_normal.z;
-          Wo[0] = rec.Wo.x; Wo[1] = rec.Wo.y; Wo[2] = rec.Wo.z;
-          valid = true;
-        }
-      }
+    if (valid) {
+      const float4 a = A.feat[3 * (size_t)li], b = A.feat[3 * (size_t)li + 1],
+                   e = A.feat[3 * (size_t)li + 2];
+      P[0] = a.x; P[1] = a.y; P[2] = a.z;
+      N[0] = b.x; N[1] = b.y; N[2] = b.z;
+      Wo[0] = e.x; Wo[1] = e.y; Wo[2] = e.z;
     }
     // a pipeline whose 128 rows all need no guide skips the network
     if (group_and(!valid, bar_id)) continue;
@@ -799,7 +803,7 @@ void launch_guide_adam(const GuideAdamArgs& a, cudaStream_t st) {
 
 void launch_guide_infer(const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                         const GuideInferArgs& a, int grid, cudaStream_t st) {
-  k_guide_select<<<grid * 4, 256, 0, st>>>(S, W, ctl, a.rows);
+  k_guide_select<<<grid * 4, 256, 0, st>>>(S, W, ctl, a.rows, a.feat);
   k_guide_infer<<<grid, 256, guide_infer_smem(), st>>>(S, W, ctl, a);
 }
 

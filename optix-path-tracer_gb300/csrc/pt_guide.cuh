@@ -82,6 +82,7 @@ struct GuideInferArgs {
   const __nv_bfloat16* w;   // BF16 weights, row-major, PTG_PARAMS
   GuidePacked* out;         // per buffer position
   uint32_t* rows;           // positions that need a guide this iteration (k_guide_select)
+  float4* feat;             // per listed row: hit point, shading normal, Wo (3 float4)
   float bmin[3], binv[3];   // scene box for the position encoding
   uint32_t* fail;
   uint32_t wait_limit;      // try_waits per tensor-core completion wait

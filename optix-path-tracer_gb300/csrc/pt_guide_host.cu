@@ -105,6 +105,7 @@ GuideInferArgs pth::guide_infer_args(pt_context* ctx) {
   a.w = (const __nv_bfloat16*)G.wbf.p;
   a.out = G.out.p;
   a.rows = G.rows.p;
+  a.feat = G.feat.p;
   memcpy(a.bmin, G.bmin, sizeof(a.bmin));
   memcpy(a.binv, G.binv, sizeof(a.binv));
   a.fail = G.counters.p + 2;  // read back at the end of a guided render

@@ -103,6 +103,8 @@ typedef struct pt_stats {
      shadow trace, finish + queue advance */
   double stage_ms[5];
   uint64_t graph_launches; /* CUDA-graph launches of the last render */
+  uint64_t guide_samples;  /* training samples of each Adam step after the last guided
+                              frame (0 without the guide) */
 } pt_stats;
 
 /* ---- context (replaces optix::Context, host_includes/host_common.hpp:21-45) */

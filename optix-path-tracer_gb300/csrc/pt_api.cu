@@ -1113,7 +1113,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
 static void reset_render_stats(pt_context* ctx) {
   pt_stats& s = ctx->stats;
   s.paths = s.ext_rays = s.shadow_rays = s.node_fetches = s.prim_tests = 0;
-  s.iterations = s.kernel_launches = s.graph_launches = 0;
+  s.iterations = s.kernel_launches = s.graph_launches = s.guide_samples = 0;
   for (double& x : s.stage_ms) x = 0.0;
   s.render_ms = 0.0;
 }
@@ -1206,6 +1206,7 @@ static int render_device(pt_context* ctx, const pt_render_params* p, void* d_acc
     CK(cudaMemcpyAsync(fl, ctx->guide.counters.p, 16, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (fl[1] || fl[2]) return fail(ctx, PT_ETIMEOUT, "guide kernel: tensor-core wait ran out");
+    ctx->stats.guide_samples = std::min<uint64_t>(fl[0], (uint64_t)1 << 18);
   }
   return PT_OK;
 }

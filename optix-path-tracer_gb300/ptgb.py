@@ -57,7 +57,8 @@ class Stats(ctypes.Structure):
                 ("bvh_bytes", ctypes.c_uint64), ("bvh_depth", ctypes.c_int),
                 ("build_ms", ctypes.c_double), ("render_ms", ctypes.c_double),
                 ("iterations", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
-                ("stage_ms", ctypes.c_double * 5), ("graph_launches", ctypes.c_uint64)]
+                ("stage_ms", ctypes.c_double * 5), ("graph_launches", ctypes.c_uint64),
+                ("guide_samples", ctypes.c_uint64)]
 
 
 class BatchItem(ctypes.Structure):

@@ -62,7 +62,7 @@ GUIDE_DESC = ("learned-guide form: 2,097,152-triangle heightfield (TS/AS/ON tile
               "white Lambertian box lit only through a ceiling opening of 0.5 % of the box area "
               "onto a 2048x1024 HDR sky; 1920x1080, consistent mode (NEE + MIS), max depth 50, "
               "RR after depth 10; MLP 76 -> 4x64 -> 8 vMF lobes + selection, BF16 tensor-core "
-              "inference and training (<= 2^18 samples per frame, 8 Adam steps per frame, "
+              "inference and training (<= 2^19 samples per frame, 12 Adam steps per frame, "
               "lr 1e-2); one step = 16 guided frames")
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")

@@ -343,7 +343,7 @@ PT_API int pt_guide_init(pt_context* ctx, uint64_t seed);
  * per frame on that frame's samples, the exponent applied to the sample
  * weights F/q (1 = the KL target; below 1 tempers the heavy tail of bright,
  * rare paths), and how many bounces of a path are guided (0 = all; deeper
- * bounces sample the BSDF alone).  Defaults: 1e-2, 8 steps, exponent 1,
+ * bounces sample the BSDF alone).  Defaults: 1e-2, 12 steps, exponent 1,
  * 4 bounces. */
 PT_API int pt_guide_set_training(pt_context* ctx, float lr, int steps_per_frame, float exponent,
                                  int max_bounces);

@@ -1206,7 +1206,7 @@ static int render_device(pt_context* ctx, const pt_render_params* p, void* d_acc
     CK(cudaMemcpyAsync(fl, ctx->guide.counters.p, 16, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (fl[1] || fl[2]) return fail(ctx, PT_ETIMEOUT, "guide kernel: tensor-core wait ran out");
-    ctx->stats.guide_samples = std::min<uint64_t>(fl[0], (uint64_t)1 << 18);
+    ctx->stats.guide_samples = std::min<uint64_t>(fl[0], (uint64_t)1 << 19);
   }
   return PT_OK;
 }

@@ -72,7 +72,7 @@ struct GuideState {
   DevBuf<float> coll_f;      //   and per-block weight sums
   uint32_t rec_stride = 1, rec_n = 0;
   float lr = 1e-2f;          // Adam learning rate of the online training
-  int steps = 8;             // Adam steps per frame on the frame's samples
+  int steps = 12;            // Adam steps per frame on the frame's samples
   float exponent = 1.f;      // training weight = (F/q)^exponent (1: the KL target)
   int max_bounces = 4;       // guided bounces per path (0: all)
   uint32_t wait_limit = 1u << 24;  // try_waits per tensor-core completion wait

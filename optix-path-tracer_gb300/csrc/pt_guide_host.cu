@@ -115,14 +115,14 @@ GuideInferArgs pth::guide_infer_args(pt_context* ctx) {
 
 int pth::guide_frame_begin(pt_context* ctx, int w, int h) {
   GuideState& G = ctx->guide;
-  const size_t target = (size_t)1 << 17;  // recording paths per frame (2 records each)
+  const size_t target = (size_t)1 << 18;  // recording paths per frame (2 records each)
   size_t wh = (size_t)w * h;
   G.rec_stride = (uint32_t)std::max<size_t>(1, (wh + target - 1) / target);
   G.rec_n = (uint32_t)(2 * ((wh + G.rec_stride - 1) / G.rec_stride));
   GK(G.rec.ensure(G.rec_n));
   GK(G.coll_u.ensure(2 * (size_t)pt::guide_collect_blocks(G.rec_n) + 1));
   GK(G.coll_f.ensure((size_t)pt::guide_collect_blocks(G.rec_n) + 1));
-  GK(G.samples.ensure((size_t)1 << 18));
+  GK(G.samples.ensure((size_t)1 << 19));
   GK(cudaMemsetAsync(G.rec.p, 0, (size_t)G.rec_n * sizeof(GuideSample), ctx->stream));
   return PT_OK;
 }
@@ -130,7 +130,7 @@ int pth::guide_frame_begin(pt_context* ctx, int w, int h) {
 int pth::guide_frame_train(pt_context* ctx) {
   GuideState& G = ctx->guide;
   cudaStream_t st = ctx->stream;
-  const uint32_t cap = 1u << 18;
+  const uint32_t cap = 1u << 19;
   GK(cudaMemsetAsync(G.counters.p, 0, 4, st));  // the failure flags stay
   GK(cudaMemsetAsync(G.scalars.p, 0, 8, st));
   pt::launch_guide_collect(G.rec.p, G.rec_n, G.samples.p, G.counters.p, G.scalars.p + 1, cap,

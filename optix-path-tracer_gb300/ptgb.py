@@ -665,7 +665,7 @@ class GpuRenderer:
     def guide_init(self, seed=0):
         self._c(self.lib.pt_guide_init(self.ctx, seed))
 
-    def guide_training(self, lr=1e-2, steps=8, exponent=1.0, max_bounces=4):
+    def guide_training(self, lr=1e-2, steps=12, exponent=1.0, max_bounces=4):
         self._c(self.lib.pt_guide_set_training(self.ctx, lr, steps, exponent, max_bounces))
 
     def guide_params(self):

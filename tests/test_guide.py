@@ -255,7 +255,7 @@ def test_guide_checkpoint_resume(ptgb_mod):
         first.render64(P(32, 32, 1, frame0=f, mode=1, guide=1))
     state, step = first.guide_state()
     first.close()
-    assert step == 3 * 8  # eight Adam steps per frame
+    assert step == 3 * 12  # twelve Adam steps per frame (the default)
     resumed = ptgb_mod.GpuRenderer(s)
     resumed.guide_set_state(state, step)
     for f in range(3, 6):

@@ -187,6 +187,14 @@ PT_API int pt_mesh_set_texture_index(pt_context* ctx, uint32_t first_prim, size_
 /* Sphere(center, radius, BRDF*)                hitables.hpp:89-128 */
 PT_API int pt_add_sphere(pt_context* ctx, const float center[3], float radius, uint32_t material,
                          const float xform[12], uint32_t* prim_id);
+/* Moving_Sphere(c0, c1, r, t0, t1, BRDF*)     hitables.hpp:130-181: centre c0
+ * at time t0, c1 at t1 (t1 > t0), linear in each path's time (the camera's
+ * time0 + rnd * (time1 - time0), programs/raygen.cu:69), extrapolated outside
+ * [t0, t1]; intersection and record of moving_sphere.cu:57-118.  Its bounds
+ * cover every time the camera can give: a camera change needs pt_commit. */
+PT_API int pt_add_moving_sphere(pt_context* ctx, const float center0[3], const float center1[3],
+                                float radius, float time0, float time1, uint32_t material,
+                                const float xform[12], uint32_t* prim_id);
 /* AARect(a0,a1,b0,b1,k,flip,axis,BRDF*)        hitables.hpp:210-270 */
 PT_API int pt_add_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k, int flip,
                        int axis, uint32_t material, const float xform[12], uint32_t* prim_id);

@@ -7,7 +7,7 @@
  * by changing includes: Constant_Texture, Checker_Texture, Noise_Texture,
  * Image_Texture / HDR_Texture, Gradient_Texture, Vector_Texture (textures.hpp),
  * Lambertian, Metal, Dielectric, Diffuse_Light, Oren_Nayar, Torrance_Sparrow,
- * Ashikhmin_Shirley (materials.hpp), Sphere, AARect, Box, Mesh, Hitable_List
+ * Ashikhmin_Shirley (materials.hpp), Sphere, Moving_Sphere, AARect, Box, Mesh, Hitable_List
  * (hitables.hpp, mesh.hpp), Camera (camera.hpp), Rectangle_PDF, Sphere_PDF,
  * Light_Sampler (pdfs.hpp, host_common.hpp), setRayGenerationProgram,
  * setMissProgram, setExceptionProgram (programs.hpp).  The OptiX objects
@@ -479,6 +479,26 @@ class Sphere : public Hitable {
   }
   const float3v center;
   const float radius;
+};
+
+// Moving_Sphere(center0, center1, radius, time0, time1, material): the
+// sphere's centre moves linearly from center0 at time0 to center1 at time1
+// over each path's time (the Camera's time0..time1).
+class Moving_Sphere : public Hitable {
+ public:
+  Moving_Sphere(const float3v& c0, const float3v& c1, float r, float t0, float t1, BRDF* m)
+      : Hitable(m), center0(c0), center1(c1), radius(r), time0(t0), time1(t1) {}
+  void add(Context& ctx, const std::vector<TransformParameter>& ts) override {
+    float x[12];
+    bool has = compose(ts, x);
+    uint32_t mid = material->assignTo(ctx);
+    ctx->check(pt_add_moving_sphere(ctx.get(), &center0.x, &center1.x, radius, time0, time1, mid,
+                                    has ? x : nullptr, nullptr),
+               "Moving_Sphere");
+    ctx->dirty = true;
+  }
+  const float3v center0, center1;
+  const float radius, time0, time1;
 };
 
 class AARect : public Hitable {

@@ -113,6 +113,24 @@ PT_BVH_HD inline void encode_node_dev(const Box& parent, const WideChild* ch, in
   out[19] = qhi[2][1];
 }
 
+// World box of a moving sphere (f = centre at time0 (3), radius, time0,
+// time1, centre at time1 (3)) over every time a ray can carry: ray times lie
+// in [cam_t0, cam_t0 + (cam_t1 - cam_t0)] (or the reverse), the centre
+// c0 + ((t - time0) / (time1 - time0)) * (c1 - c0) is monotonic in t in
+// floating point too, so the boxes at the two end times hold it.
+PT_BVH_HD inline void moving_sphere_box(const float* f, float cam_t0, float cam_t1, float lo[3],
+                                        float hi[3]) {
+  const float te = cam_t0 + (cam_t1 - cam_t0);
+  const float ta = fminf(fminf(f[4], cam_t0), te), tb = fmaxf(fmaxf(f[5], cam_t0), te);
+  for (int a = 0; a < 3; a++) {
+    const float d = f[6 + a] - f[a];
+    const float ca = f[a] + ((ta - f[4]) / (f[5] - f[4])) * d;
+    const float cb = f[a] + ((tb - f[4]) / (f[5] - f[4])) * d;
+    lo[a] = fminf(ca, cb) - f[3];
+    hi[a] = fmaxf(ca, cb) + f[3];
+  }
+}
+
 inline void encode_node(const Box& parent, const WideChild* ch, int nch, uint32_t child_base,
                         uint32_t prim_base, uint32_t out[20]) {
   encode_node_dev(parent, ch, nch, child_base, prim_base, out);

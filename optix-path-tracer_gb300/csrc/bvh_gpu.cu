@@ -77,7 +77,8 @@ __device__ __forceinline__ GBox box_load_cg(const float4* lo, const float4* hi, 
 
 // Padded world AABB of one primitive record (the host builder's padding).
 __global__ void k_bounds(const float4* __restrict__ rec, const float4* __restrict__ xforms,
-                         uint32_t n, float4* lo, float4* hi, unsigned int* cbox) {
+                         uint32_t n, float cam_t0, float cam_t1, float4* lo, float4* hi,
+                         unsigned int* cbox) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   GBox c;
   for (int k = 0; k < 3; k++) {
@@ -95,6 +96,8 @@ __global__ void k_bounds(const float4* __restrict__ rec, const float4* __restric
         b.lo[a] = fminf(fminf(f[a], f[3 + a]), f[6 + a]);
         b.hi[a] = fmaxf(fmaxf(f[a], f[3 + a]), f[6 + a]);
       }
+    } else if (type == PT_PRIM_SPHERE && (tag & PT_PRIM_MOVING)) {
+      pt::moving_sphere_box(f, cam_t0, cam_t1, b.lo, b.hi);
     } else if (type == PT_PRIM_SPHERE) {
       for (int a = 0; a < 3; a++) {
         b.lo[a] = f[a] - f[3];
@@ -592,7 +595,7 @@ namespace pt {
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
                            uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
-                           cudaStream_t st) {
+                           float cam_t0, float cam_t1, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
   if (width < 2 || width > 8) width = 8;
   float4 *lo = nullptr, *hi = nullptr, *ilo = nullptr, *ihi = nullptr, *slo = nullptr,
@@ -634,7 +637,7 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
   BV(cudaMemcpyAsync(cbox, h_cbox, sizeof(h_cbox), cudaMemcpyHostToDevice, st));
   {
     uint32_t g = (n + 255) / 256;
-    k_bounds<<<g, 256, 0, st>>>(d_rec, d_xforms, n, lo, hi, cbox);
+    k_bounds<<<g, 256, 0, st>>>(d_rec, d_xforms, n, cam_t0, cam_t1, lo, hi, cbox);
     k_morton<<<g, 256, 0, st>>>(lo, hi, n, cbox, keys, vals);
     BV(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0, 30,
                                        st));

@@ -32,7 +32,7 @@ namespace pt {
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
                            uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
-                           cudaStream_t st);
+                           float cam_t0, float cam_t1, cudaStream_t st);
 }
 
 namespace {
@@ -138,6 +138,8 @@ static pt::Box prim_box(const pt_context* ctx, const HostPrim& p) {
       lo[a] = fminf(fminf(f[a], f[3 + a]), f[6 + a]);
       hi[a] = fmaxf(fmaxf(f[a], f[3 + a]), f[6 + a]);
     }
+  } else if (p.type == PT_PRIM_SPHERE && p.moving) {
+    pt::moving_sphere_box(f, ctx->cam.time0, ctx->cam.time1, lo, hi);
   } else if (p.type == PT_PRIM_SPHERE) {
     for (int a = 0; a < 3; a++) {
       lo[a] = f[a] - f[3];
@@ -544,6 +546,29 @@ PT_API int pt_add_sphere(pt_context* ctx, const float center[3], float radius, u
   return push_prim(ctx, p, xform, prim_id);
 }
 
+PT_API int pt_add_moving_sphere(pt_context* ctx, const float center0[3], const float center1[3],
+                                float radius, float time0, float time1, uint32_t material,
+                                const float xform[12], uint32_t* prim_id) {
+  if (!ctx) return PT_EINVAL;
+  if (!finite3(center0) || !finite3(center1) || !std::isfinite(radius) || !(radius > 0.f))
+    return fail(ctx, PT_EINVAL, "moving sphere needs finite centres and radius > 0");
+  if (!std::isfinite(time0) || !std::isfinite(time1) || !(time1 > time0))
+    return fail(ctx, PT_EINVAL, "moving sphere needs finite times with time1 > time0");
+  HostPrim p;
+  memset(&p, 0, sizeof(p));
+  p.type = PT_PRIM_SPHERE;
+  p.moving = 1;
+  p.material = material;
+  for (int a = 0; a < 3; a++) {
+    p.f[a] = center0[a];
+    p.f[6 + a] = center1[a];
+  }
+  p.f[3] = radius;
+  p.f[4] = time0;
+  p.f[5] = time1;
+  return push_prim(ctx, p, xform, prim_id);
+}
+
 PT_API int pt_add_rect(pt_context* ctx, float a0, float a1, float b0, float b1, float k, int flip,
                        int axis, uint32_t material, const float xform[12], uint32_t* prim_id) {
   if (!ctx) return PT_EINVAL;
@@ -771,7 +796,7 @@ PT_API int pt_set_camera(pt_context* ctx, const float lookfrom[3], const float l
 // ------------------------------------------------------------------- commit
 static void prim_record(const HostPrim& p, uint32_t id, float4* out) {
   uint32_t tag = (uint32_t)p.type | ((uint32_t)p.axis << 2) | ((uint32_t)p.flip << 4) |
-                 ((uint32_t)(p.xform + 1) << 8);
+                 (p.moving ? PT_PRIM_MOVING : 0u) | ((uint32_t)(p.xform + 1) << 8);
   float tagf, idf, matf;
   memcpy(&tagf, &tag, 4);
   memcpy(&idf, &id, 4);
@@ -818,7 +843,8 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
     uint32_t nodes = 0;
     int depth = 0;
     CK(pt::build_bvh8_gpu(ctx->d_rec_in.p, ctx->d_xforms.p, (uint32_t)n, d_nodes.p,
-                          d_prims.p, d_leaf_of_id.p, &nodes, &depth, PT_TREELET_ROUNDS, width, st));
+                          d_prims.p, d_leaf_of_id.p, &nodes, &depth, PT_TREELET_ROUNDS, width,
+                          ctx->cam.time0, ctx->cam.time1, st));
     if (depth < 0)
       return fail(ctx, PT_EINVAL,
                   "GPU BVH8 failed validation (collapse check " + std::to_string(-depth) + ")");
@@ -940,6 +966,7 @@ PT_API int pt_commit(pt_context* ctx) {
   S.num_lights = (int)ctx->lights.size();
   S.num_prims = (int)n;
   S.tri_only = pth::all_triangles(ctx) ? 1 : 0;
+  S.has_motion = pth::has_motion(ctx) ? 1 : 0;
   S.miss = ctx->miss;
   S.miss.env = ctx->d_env.p;
   S.cam = ctx->cam;
@@ -957,6 +984,7 @@ PT_API int pt_commit(pt_context* ctx) {
   ctx->lc.sort = ctx->opt.shade_order == 1 || (ctx->opt.shade_order == 0 && pth::sort_pays(ctx));
   ctx->lc.refetch = ctx->opt.refetch_lanes ? ctx->opt.refetch_lanes : pth::auto_refetch(n);
   ctx->lc.tex = pth::uses_textures(ctx) ? 1 : 0;
+  ctx->lc.motion = pth::has_motion(ctx) ? 1 : 0;
   auto t1 = std::chrono::steady_clock::now();
   ctx->stats.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   ctx->stats.bvh_nodes = nn;
@@ -1125,6 +1153,12 @@ static void reset_render_stats(pt_context* ctx) {
 // the whole warp; rays through a small scene are short and alike.  (GB300,
 // 1080p: 2.1M-triangle heightfield 24 lanes +6% over 32; 488 spheres 32
 // lanes +1% over 24.)
+bool pth::has_motion(const pt_context* ctx) {
+  for (const HostPrim& p : ctx->prims)
+    if (p.moving) return true;
+  return false;
+}
+
 bool pth::all_triangles(const pt_context* ctx) {
   for (const HostPrim& p : ctx->prims)
     if (p.type != PT_PRIM_TRIANGLE) return false;

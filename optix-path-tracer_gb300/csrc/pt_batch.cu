@@ -255,8 +255,11 @@ static int ensure_geometry(pt_batch* b, const pt_batch_item* items, int n) {
   S.num_prims = (int)P;
   S.root = 0;
   S.tri_only = 1;
-  for (const pt_context* c : ctxs)
+  S.has_motion = 0;
+  for (const pt_context* c : ctxs) {
     if (!pth::all_triangles(c)) S.tri_only = 0;
+    if (pth::has_motion(c)) S.has_motion = 1;
+  }
   b->max_stack = max_depth + 1;
   b->total_nodes = N;
   b->parts_width = width;
@@ -419,7 +422,11 @@ static int batch_render(pt_batch* b, const pt_batch_item* items, int n, float4* 
   if (b->tune.shade_order == 0)
     for (const ScenePart& p : b->parts) lc.sort = lc.sort || sort_pays(p.ctx);
   lc.tex = 0;
-  for (const ScenePart& p : b->parts) lc.tex = lc.tex || uses_textures(p.ctx);
+  lc.motion = 0;
+  for (const ScenePart& p : b->parts) {
+    lc.tex = lc.tex || uses_textures(p.ctx);
+    lc.motion = lc.motion || has_motion(p.ctx);
+  }
   lc.refetch = b->tune.refetch_lanes;
   if (lc.refetch == 0) {  // automatic: by the largest scene of the batch
     size_t most = 0;

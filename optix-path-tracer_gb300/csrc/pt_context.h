@@ -20,6 +20,7 @@ struct HostPrim {
   int type, axis, flip, xform;
   uint32_t material;
   float f[9];
+  int moving;  // a moving sphere (type sphere, f as in pt_types.h)
 };
 
 template <typename T>
@@ -166,6 +167,8 @@ int device_ptr_kind(const void* p, int device);
 bool uses_textures(const pt_context* ctx);
 /* Whether every primitive of the scene is a triangle. */
 bool all_triangles(const pt_context* ctx);
+/* Whether some sphere of the scene moves. */
+bool has_motion(const pt_context* ctx);
 /* Whether shading in material-sorted tiles pays for this scene: it does when
  * one of the costly BRDFs (Oren-Nayar, Torrance-Sparrow, Ashikhmin-Shirley)
  * is present, whose code paths diverge most in a mixed warp. */

@@ -187,6 +187,7 @@ PTD int prim_type(const PrimRec& p) { return (int)(__float_as_uint(p.r0.w) & 3u)
 PTD int prim_axis(const PrimRec& p) { return (int)((__float_as_uint(p.r0.w) >> 2) & 3u); }
 PTD int prim_flip(const PrimRec& p) { return (int)((__float_as_uint(p.r0.w) >> 4) & 1u); }
 PTD int prim_xform(const PrimRec& p) { return (int)(__float_as_uint(p.r0.w) >> 8) - 1; }
+PTD bool prim_moving(const PrimRec& p) { return (__float_as_uint(p.r0.w) & PT_PRIM_MOVING) != 0u; }
 PTD uint32_t prim_id(const PrimRec& p) { return __float_as_uint(p.r1.w); }
 PTD uint32_t prim_material(const PrimRec& p) { return __float_as_uint(p.r2.w); }
 
@@ -198,9 +199,21 @@ PTD PrimRec load_prim(const float4* prims, uint32_t i) {
   return p;
 }
 
+// Centre of a sphere at `time`: the record's centre, or for a moving sphere
+// programs/hitables/moving_sphere.cu:47-49 (linear in time, also outside
+// [time0, time1]).
+PTD V3 sphere_center(const PrimRec& p, float time) {
+  V3 c0 = v3(p.r0.x, p.r0.y, p.r0.z);
+  if (!prim_moving(p)) return c0;
+  V3 c1 = v3(p.r2.x, p.r2.y, p.r2.z);
+  return c0 + ((time - p.r1.y) / (p.r1.z - p.r1.y)) * (c1 - c0);
+}
+
 // programs/hitables/sphere.cu:32-62 - near root if in range, else far root
-PTD bool sphere_candidate(const PrimRec& p, V3 o, V3 d, float tmin, float tmax, float& t) {
-  V3 center = v3(p.r0.x, p.r0.y, p.r0.z);
+// (a moving sphere, moving_sphere.cu:57-118: the same roots at its centre
+// for the ray's time: sphere_candidate_at(p, sphere_center(p, time), ...))
+PTD bool sphere_candidate_at(const PrimRec& p, V3 center, V3 o, V3 d, float tmin, float tmax,
+                             float& t) {
   float radius = p.r1.x;
   V3 oc = o - center;
   float a = dot(d, d);
@@ -213,6 +226,11 @@ PTD bool sphere_candidate(const PrimRec& p, V3 o, V3 d, float tmin, float tmax, 
   float t1 = (-b + ptm_sqrt(discriminant)) / a;
   if (t1 > tmin && t1 < tmax) { t = t1; return true; }
   return false;
+}
+
+PTD bool sphere_candidate(const PrimRec& p, V3 o, V3 d, float tmin, float tmax, float& t,
+                          float time = 0.f) {
+  return sphere_candidate_at(p, sphere_center(p, time), o, d, tmin, tmax, t);
 }
 
 // programs/hitables/aarect.cu:20-69
@@ -316,7 +334,7 @@ struct HitRecord {
 // (the shading kernels pass false and compute them out of line, in
 // textured_colours, for textured materials only; u, v feed nothing else).
 PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, float t_hit,
-                         float bu, float bv, bool need_uv = true) {
+                         float bu, float bv, bool need_uv = true, float time = 0.f) {
   HitRecord rec;
   rec.Wo = normalize(-rd);
   int xf = prim_xform(p);
@@ -331,7 +349,9 @@ PTD HitRecord hit_record(const DevScene& S, const PrimRec& p, V3 ro, V3 rd, floa
   rec.tindex = 0;
   int type = prim_type(p);
   if (type == PT_PRIM_SPHERE) {
-    V3 center = v3(p.r0.x, p.r0.y, p.r0.z);
+    // a moving sphere's record (moving_sphere.cu:80-96) is the sphere's at
+    // its centre for the ray's time
+    V3 center = sphere_center(p, time);
     float radius = p.r1.x;
     V3 hit_point = o + t_hit * d;
     rec.P = M ? xpoint(M, hit_point) : hit_point;

@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(256) k_guide_select(DevScene S, WaveState W,
                type == PT_MAT_TORRANCE_SPARROW || type == PT_MAT_ASHIKHMIN_SHIRLEY;
         if (take) {
           const float4 ro = pb.ray_o[i], rd = pb.ray_d[i];
-          rec = hit_record(S, p, f4xyz(ro), f4xyz(rd), hit.x, hit.y, hit.z, false);
+          rec = hit_record(S, p, f4xyz(ro), f4xyz(rd), hit.x, hit.y, hit.z, false, pb.thr[i].w);
         }
       }
     }

@@ -35,6 +35,7 @@ struct LaunchCfg {
   int sort;            /* shade in material-sorted tiles */
   int refetch;         /* idle lanes of a trace warp that take new rays together (1..32) */
   int tex;             /* some material takes a texture: the texture variants of shading */
+  int motion;          /* some sphere moves: the trace variants that carry ray times */
 };
 
 struct Ray3 {

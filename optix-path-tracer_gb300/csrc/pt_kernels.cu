@@ -73,10 +73,11 @@ struct Tail {
 };
 
 // Ends the path or appends it, compacted, to the next path buffer.  All
-// lanes of the warp call it (the append is a warp-aggregated atomic).
+// lanes of the warp call it (the append is a warp-aggregated atomic).  tm:
+// the path's time (color()'s prd.time), carried in the throughput's w.
 __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters& c,
                                           const PathCtl& ctl, uint4 st, V3 thr, V3 rad,
-                                          const Tail& tl, bool active) {
+                                          const Tail& tl, bool active, float tm) {
   bool cont = false;
   if (active) {
     uint32_t depth = st.z & PT_ST_DEPTH_MASK;
@@ -121,7 +122,7 @@ __device__ __forceinline__ void path_tail(const WaveState& W, const WaveCounters
     const PathBuf& nb = W.path[c.parity ^ 1u];
     nb.ray_o[pos] = make_float4(tl.origin.x, tl.origin.y, tl.origin.z, 1e-3f);
     nb.ray_d[pos] = make_float4(tl.direction.x, tl.direction.y, tl.direction.z, PT_RAY_TMAX);
-    nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, tm);
     nb.rad[pos] = make_float4(rad.x, rad.y, rad.z, 0.f);
     nb.st[pos] = st;
   }
@@ -181,10 +182,9 @@ __global__ void k_generate(DevScene S0, WaveState W, const WaveCtl* __restrict__
     Ray3 r = camera_ray(S.cam, x, y, width, height, seed);
     // color(): prd.time draw, programs/raygen.cu:69
     float tm = S.cam.time0 + rnd(seed) * (S.cam.time1 - S.cam.time0);
-    (void)tm;
     pb.ray_o[pos] = make_float4(r.o.x, r.o.y, r.o.z, 1e-6f);
     pb.ray_d[pos] = make_float4(r.d.x, r.d.y, r.d.z, PT_RAY_TMAX);
-    pb.thr[pos] = make_float4(1.f, 1.f, 1.f, 0.f);
+    pb.thr[pos] = make_float4(1.f, 1.f, 1.f, tm);
     pb.rad[pos] = make_float4(0.f, 0.f, 0.f, 0.f);
     pb.st[pos] = make_uint4(seed, pid, scene << PT_ST_SCENE_SHIFT, 0u);
   }
@@ -298,8 +298,9 @@ __device__ __forceinline__ V3 env_lookup(const GpuMiss& ms, float u, float v) {
 // with textures (the TEX variants): untextured shading never computes the
 // texture coordinates.
 __device__ __forceinline__ void apply_textures(const DevScene& S, GpuMaterial& m, const PrimRec& p,
-                                               V3 ro, V3 rd, float t, float bu, float bv) {
-  HitRecord rec = hit_record(S, p, ro, rd, t, bu, bv, true);
+                                               V3 ro, V3 rd, float t, float bu, float bv,
+                                               float tm) {
+  HitRecord rec = hit_record(S, p, ro, rd, t, bu, bv, true, tm);
   resolve_textures(S, m, rec.u, rec.v, rec.P, rec.tindex);
 }
 
@@ -427,6 +428,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
   const PathBuf& pb = W.path[c.parity];
   uint4 st = make_uint4(0, 0, 0, 0);
   V3 thr = v3(0.f), rad = v3(0.f);
+  float tm = 0.f;
   Tail tl;
   tl.event = 1;
   tl.isSpecular = false;
@@ -443,6 +445,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
   if (active) {
     float4 t4 = pb.thr[i], r4 = pb.rad[i];
     thr = f4xyz(t4);
+    tm = t4.w;
     rad = f4xyz(r4);
     float4 hit = W.hit[i];
     float4 ro = pb.ray_o[i], rdv = pb.ray_d[i];
@@ -453,12 +456,12 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
       missed = true;
     } else {
       PrimRec p = load_prim(S.prims, leaf);
-      HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, false);
+      HitRecord rec = hit_record(S, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, false, tm);
       mid = rec.index;
       GpuMaterial m = S.mats[mid];
       textured = TEX && (m.tex0 >= 0 || m.tex1 >= 0);
       if (textured) {
-        apply_textures(S, m, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z);
+        apply_textures(S, m, p, f4xyz(ro), f4xyz(rdv), hit.x, hit.y, hit.z, tm);
         tcol = v3(m.c0x, m.c0y, m.c0z);
       }
       P = rec.P;
@@ -550,11 +553,11 @@ __device__ __forceinline__ void shade_path(const DevScene& S0, const WaveState& 
     W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
     if (textured) W.sh.C[spos] = make_float4(tcol.x, tcol.y, tcol.z, 0.f);
     W.sh.st[spos] = st;
-    W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, tm);
     W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, 0.f);
   }
   if (missed) finalize_path(W, st.y, col);  // misses end here
-  path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, tail);
+  path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, tail, tm);
 }
 
 // TEX: the scene has textured materials (their colours are evaluated at
@@ -584,13 +587,16 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S0, WaveStat
     bool active = i < n;
     uint4 st = make_uint4(0, 0, 0, 0);
     V3 thr = v3(0.f), rad = v3(0.f);
+    float tm = 0.f;
     Tail tl;
     tl.event = 1;
     tl.isSpecular = false;
     if (active) st = W.sh.st[i];
     const DevScene& S = path_scene<BATCH>(S0, br, st.z);
     if (active) {
-      thr = f4xyz(W.sh.thr[i]);
+      const float4 t4 = W.sh.thr[i];
+      thr = f4xyz(t4);
+      tm = t4.w;
       rad = f4xyz(W.sh.rad[i]);
       float4 P4 = W.sh.P[i], N4 = W.sh.N[i], Wo4 = W.sh.Wo[i], Wi4 = W.sh.Wi[i];
       GpuMaterial m = S.mats[__float_as_uint(Wo4.w)];
@@ -605,7 +611,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish(DevScene S0, WaveStat
                           Wi4.w != 0.f);
       after_nee(m, st.x, P, Wo, N, direct, thr, rad, tl);
     }
-    path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, active);
+    path_tail(W, c, path_ctl<BATCH>(ctl, br, st.z), st, thr, rad, tl, active, tm);
   }
 }
 
@@ -618,17 +624,18 @@ __device__ __forceinline__ float lights_pdf_c(const DevScene& S, V3 P, V3 d, int
   return acc / (float)n_sel;
 }
 
-// Appends a continuing path (consistent mode) to the next buffer; rad_w is
-// the guide-record word carried in the radiance's w (0 without the guide).
+// Appends a continuing path (consistent mode) to the next buffer; tm is the
+// path's time (in the throughput's w), rad_w the guide-record word carried
+// in the radiance's w (0 without the guide).
 __device__ __forceinline__ void path_push(const WaveState& W, const WaveCounters& c, uint4 st,
-                                          V3 thr, V3 rad, V3 o, V3 d, bool cont,
+                                          V3 thr, V3 rad, V3 o, V3 d, bool cont, float tm,
                                           float rad_w = 0.f) {
   uint32_t pos = warp_push(&W.ctr->n_next, cont);
   if (cont) {
     const PathBuf& nb = W.path[c.parity ^ 1u];
     nb.ray_o[pos] = make_float4(o.x, o.y, o.z, 1e-3f);
     nb.ray_d[pos] = make_float4(d.x, d.y, d.z, PT_RAY_TMAX);
-    nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    nb.thr[pos] = make_float4(thr.x, thr.y, thr.z, tm);
     nb.rad[pos] = make_float4(rad.x, rad.y, rad.z, rad_w);
     nb.st[pos] = st;
   }
@@ -677,14 +684,16 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
   const PathBuf& pb = W.path[c.parity];
   uint4 st = make_uint4(0, 0, 0, 0);
   V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), Wi = v3(0.f), dcont = v3(0.f), C = v3(0.f);
-  float tmax = 0.f, code = 0.f;
+  float tmax = 0.f, code = 0.f, tm = 0.f;
   bool ended = false, shadow = false;
   if (active) st = pb.st[i];
   const DevScene& S = path_scene<BATCH>(S0, br, st.z);
   const int n_sel = S.num_lights + (S.env_valid ? 1 : 0);
   if (active) {
     const PathCtl pc = path_ctl<BATCH>(ctl, br, st.z);
-    thr = f4xyz(pb.thr[i]);
+    const float4 t4 = pb.thr[i];
+    thr = f4xyz(t4);
+    tm = t4.w;
     float4 r4 = pb.rad[i];
     rad = f4xyz(r4);
     code = GUIDE ? r4.w : 0.f;
@@ -704,10 +713,10 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
       ended = true;
     } else {
       PrimRec p = load_prim(S.prims, leaf);
-      HitRecord rec = hit_record(S, p, f4xyz(ro), d, hit.x, hit.y, hit.z, false);
+      HitRecord rec = hit_record(S, p, f4xyz(ro), d, hit.x, hit.y, hit.z, false, tm);
       GpuMaterial m = S.mats[rec.index];
       if (TEX && (m.tex0 >= 0 || m.tex1 >= 0))
-        apply_textures(S, m, p, f4xyz(ro), d, hit.x, hit.y, hit.z);
+        apply_textures(S, m, p, f4xyz(ro), d, hit.x, hit.y, hit.z, tm);
       P = rec.P;
       V3 Wo = rec.Wo, N = rec.shading_normal;
       if (m.type == PT_MAT_DIFFUSE_LIGHT) {
@@ -858,7 +867,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
     W.sh.Wi[spos] = make_float4(Wi.x, Wi.y, Wi.z, 0.f);
     W.sh.C[spos] = make_float4(C.x, C.y, C.z, tmax);
     W.sh.Wo[spos] = make_float4(dcont.x, dcont.y, dcont.z, ended ? 1.f : 0.f);
-    W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, 0.f);
+    W.sh.thr[spos] = make_float4(thr.x, thr.y, thr.z, tm);
     W.sh.rad[spos] = make_float4(rad.x, rad.y, rad.z, code);
     W.sh.st[spos] = st;
   }
@@ -868,7 +877,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
   }
   // the next vertex starts without a pending record of its own
   float cw = GUIDE ? (float)(((int)code >> 1) * 2) : 0.f;
-  path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended, cw);
+  path_push(W, c, st, thr, rad, P, dcont, active && !shadow && !ended, tm, cw);
 }
 
 template <bool BATCH, bool SORT, bool GUIDE, bool TEX>
@@ -896,10 +905,12 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveSta
     uint4 st = make_uint4(0, 0, 0, 0);
     V3 thr = v3(0.f), rad = v3(0.f), P = v3(0.f), dcont = v3(0.f);
     bool ended = false;
-    float code = 0.f;
+    float code = 0.f, tm = 0.f;
     if (active) {
       st = W.sh.st[i];
-      thr = f4xyz(W.sh.thr[i]);
+      const float4 t4 = W.sh.thr[i];
+      thr = f4xyz(t4);
+      tm = t4.w;
       float4 r4 = W.sh.rad[i];
       rad = f4xyz(r4);
       code = r4.w;
@@ -920,7 +931,7 @@ __global__ void __launch_bounds__(PT_SHADE_BLOCK) k_finish_c(DevScene S, WaveSta
         if (code != 0.f) guide_end(W, st.y, code, rad);
       }
     }
-    path_push(W, c, st, thr, rad, P, dcont, active && !ended, (float)(((int)code >> 1) * 2));
+    path_push(W, c, st, thr, rad, P, dcont, active && !ended, tm, (float)(((int)code >> 1) * 2));
   }
 }
 
@@ -1222,6 +1233,7 @@ LaunchCfg default_launch(int max_stack) {
   lc.sort = 1;
   lc.refetch = 32;
   lc.tex = 0;
+  lc.motion = 0;
   lc.trace_grid = wave_grid(0, max_stack, lc.trace_block);
   lc.shade_grid = wave_grid(1, max_stack, lc.shade_block);
   return lc;

@@ -49,6 +49,7 @@ struct WarpShared {
   float4 rd[32];                  // direction, tmax
   float4 wt[32];                  // watertight-test constants Sx, Sy, Sz, axes
   unsigned long long best[32];    // (t bits << 32) | primitive id
+  float tm[32];                   // the ray's path time (scenes with moving spheres)
   uint32_t pair_prim[PT_PAIR_CAP];
   uint8_t pair_owner[PT_PAIR_CAP];
 };
@@ -92,10 +93,12 @@ __device__ __forceinline__ WtRay wt_unpack(float4 w) {
   return r;
 }
 
-// Candidate of one primitive for a world-space ray (object space inside).
+// Candidate of one primitive for a world-space ray (object space inside);
+// MOTION: spheres may move (at the ray's `time`), else every sphere is static.
+template <bool MOTION>
 __device__ __forceinline__ bool prim_test(const DevScene& S, const PrimRec& p, V3 o, V3 d,
                                           const WtRay& wt, float tmin, float tmax, float& t,
-                                          float& bu, float& bv) {
+                                          float& bu, float& bv, float time) {
   bu = bv = 0.f;
   if (S.tri_only) return tri_candidate(p, o, wt, tmin, tmax, t, bu, bv);
   int type = prim_type(p);
@@ -107,7 +110,9 @@ __device__ __forceinline__ bool prim_test(const DevScene& S, const PrimRec& p, V
     oo = xpoint(I, o);
     dd = xvector(I, d);
   }
-  if (type == PT_PRIM_SPHERE) return sphere_candidate(p, oo, dd, tmin, tmax, t);
+  if (type == PT_PRIM_SPHERE)
+    return sphere_candidate_at(p, MOTION ? sphere_center(p, time) : v3(p.r0.x, p.r0.y, p.r0.z), oo,
+                               dd, tmin, tmax, t);
   if (type == PT_PRIM_RECT) return rect_candidate(p, oo, dd, tmin, tmax, t);
   return box_candidate(p, oo, dd, tmin, tmax, t);
 }
@@ -125,8 +130,9 @@ struct FirstHitOut {
 #endif
 
 // BATCH: rays of several scenes; each starts at its scene's root node (the
-// scene index is in the path state word st.z).
-template <int MODE, bool COUNT, bool BATCH>
+// scene index is in the path state word st.z).  MOTION: the scene has moving
+// spheres, so each ray carries its path's time (other scenes do without).
+template <int MODE, bool COUNT, bool BATCH, bool MOTION>
 __global__ void __maxnreg__(PT_TRACE_MAXREG)
     k_trace_t(DevScene S, WaveState W, const WaveCtl* __restrict__ ctlp, int max_stack,
               FirstHitOut fo, BatchRefs br, int refetch) {
@@ -190,6 +196,8 @@ __global__ void __maxnreg__(PT_TRACE_MAXREG)
       d = v3(r.d.x, r.d.y, r.d.z);
       tmin = 1e-6f;
       tmax = PT_RAY_TMAX;
+      if (MOTION)  // color()'s prd.time, programs/raygen.cu:69
+        ws.tm[lane] = S.cam.time0 + rnd(seed) * (S.cam.time1 - S.cam.time0);
     }
   };
 
@@ -281,6 +289,8 @@ __global__ void __maxnreg__(PT_TRACE_MAXREG)
     tbest = tmax;
     best_id = PT_NO_HIT;
     ws.best[lane] = ((unsigned long long)__float_as_uint(tmax) << 32) | 0xffffffffull;
+    if (MOTION && MODE != TRACE_FIRST)  // the path's time rides in throughput.w
+      ws.tm[lane] = MODE == TRACE_EXT ? W.path[parity].thr[i].w : W.sh.thr[i].w;
     cur = S.root;
     if (BATCH) {
       uint32_t z = MODE == TRACE_EXT ? W.path[parity].st[i].z : W.sh.st[i].z;
@@ -469,7 +479,8 @@ __global__ void __maxnreg__(PT_TRACE_MAXREG)
             PrimRec p = load_prim(S.prims, pbase + (uint32_t)j);
             if (COUNT) np++;
             float t, bu, bv;
-            if (prim_test(S, p, o, f4xyz(rdv), wt, tmin, rdv.w, t, bu, bv)) {
+            if (prim_test<MOTION>(S, p, o, f4xyz(rdv), wt, tmin, rdv.w, t, bu, bv,
+                                  MOTION ? ws.tm[lane] : 0.f)) {
               unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
               bk = min(bk, key);
             }
@@ -511,7 +522,8 @@ __global__ void __maxnreg__(PT_TRACE_MAXREG)
             if (COUNT) np++;
             float4 ro = ws.ro[ow], rdv = ws.rd[ow];
             float t, bu, bv;
-            if (prim_test(S, p, f4xyz(ro), f4xyz(rdv), wt_unpack(ws.wt[ow]), ro.w, rdv.w, t, bu, bv)) {
+            if (prim_test<MOTION>(S, p, f4xyz(ro), f4xyz(rdv), wt_unpack(ws.wt[ow]), ro.w, rdv.w, t,
+                                  bu, bv, MOTION ? ws.tm[ow] : 0.f)) {
               unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | prim_id(p);
               atomicMin(&ws.best[ow], key);
             }
@@ -571,7 +583,7 @@ size_t trace_smem(int max_stack, int block) {
 int trace_blocks_per_sm(int block, size_t smem) {
   int blocks = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &blocks, k_trace_t<TRACE_EXT, false, false>, block, smem);
+      &blocks, k_trace_t<TRACE_EXT, false, false, false>, block, smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -590,13 +602,13 @@ static cudaError_t smem_attr(K k, int optin) {
                               optin - (int)fa.sharedSizeBytes);
 }
 
-template <int MODE>
+template <int MODE, bool MOTION>
 static cudaError_t smem_attr_mode(int optin) {
   cudaError_t e;
-  if ((e = smem_attr(k_trace_t<MODE, false, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<MODE, true, false>, optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<MODE, false, true>, optin)) != cudaSuccess) return e;
-  return smem_attr(k_trace_t<MODE, true, true>, optin);
+  if ((e = smem_attr(k_trace_t<MODE, false, false, MOTION>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<MODE, true, false, MOTION>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<MODE, false, true, MOTION>, optin)) != cudaSuccess) return e;
+  return smem_attr(k_trace_t<MODE, true, true, MOTION>, optin);
 }
 
 static const int kMaxDev = 64;
@@ -611,56 +623,69 @@ cudaError_t set_trace_smem() {
   if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
       cudaSuccess)
     return e;
-  if ((e = smem_attr_mode<TRACE_EXT>(optin)) != cudaSuccess) return e;
-  if ((e = smem_attr_mode<TRACE_SHADOW>(optin)) != cudaSuccess) return e;
-  if ((e = smem_attr_mode<TRACE_OCCLUDED>(optin)) != cudaSuccess) return e;
-  if ((e = smem_attr(k_trace_t<TRACE_FIRST, false, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr_mode<TRACE_EXT, false>(optin)) != cudaSuccess) return e;
+  if ((e = smem_attr_mode<TRACE_SHADOW, false>(optin)) != cudaSuccess) return e;
+  if ((e = smem_attr_mode<TRACE_OCCLUDED, false>(optin)) != cudaSuccess) return e;
+  if ((e = smem_attr_mode<TRACE_EXT, true>(optin)) != cudaSuccess) return e;
+  if ((e = smem_attr_mode<TRACE_SHADOW, true>(optin)) != cudaSuccess) return e;
+  if ((e = smem_attr_mode<TRACE_OCCLUDED, true>(optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_FIRST, false, false, false>, optin)) != cudaSuccess) return e;
+  if ((e = smem_attr(k_trace_t<TRACE_FIRST, false, false, true>, optin)) != cudaSuccess) return e;
   if (dev >= 0 && dev < kMaxDev) g_smem_set[dev] = true;
   return cudaSuccess;
 }
 
-template <int MODE, bool BATCH>
+template <int MODE, bool BATCH, bool MOTION>
 static void launch_mode(bool counters, const DevScene& S, const WaveState& W, const WaveCtl* ctl,
                         int max_stack, const BatchRefs& br, const LaunchCfg& lc, size_t smem,
                         cudaStream_t st) {
   FirstHitOut none{};
   if (counters)
-    k_trace_t<MODE, true, BATCH><<<lc.trace_grid, lc.trace_block, smem, st>>>(
+    k_trace_t<MODE, true, BATCH, MOTION><<<lc.trace_grid, lc.trace_block, smem, st>>>(
         S, W, ctl, max_stack, none, br, lc.refetch);
   else
-    k_trace_t<MODE, false, BATCH><<<lc.trace_grid, lc.trace_block, smem, st>>>(
+    k_trace_t<MODE, false, BATCH, MOTION><<<lc.trace_grid, lc.trace_block, smem, st>>>(
         S, W, ctl, max_stack, none, br, lc.refetch);
 }
 
-template <bool BATCH>
+template <bool BATCH, bool MOTION>
 static void launch_kind(int mode, bool counters, const DevScene& S, const WaveState& W,
                         const WaveCtl* ctl, int max_stack, const BatchRefs& br,
                         const LaunchCfg& lc, size_t smem, cudaStream_t st) {
   if (mode == TRACE_EXT)
-    launch_mode<TRACE_EXT, BATCH>(counters, S, W, ctl, max_stack, br, lc, smem, st);
+    launch_mode<TRACE_EXT, BATCH, MOTION>(counters, S, W, ctl, max_stack, br, lc, smem, st);
   else if (mode == TRACE_SHADOW)
-    launch_mode<TRACE_SHADOW, BATCH>(counters, S, W, ctl, max_stack, br, lc, smem, st);
+    launch_mode<TRACE_SHADOW, BATCH, MOTION>(counters, S, W, ctl, max_stack, br, lc, smem, st);
   else
-    launch_mode<TRACE_OCCLUDED, BATCH>(counters, S, W, ctl, max_stack, br, lc, smem, st);
+    launch_mode<TRACE_OCCLUDED, BATCH, MOTION>(counters, S, W, ctl, max_stack, br, lc, smem, st);
 }
 
 void launch_trace(int mode, bool counters, const DevScene& S, const WaveState& W,
                   const WaveCtl* ctl, int max_stack, const BatchRefs* br, const LaunchCfg& lc,
                   cudaStream_t st) {
   const size_t smem = trace_smem(max_stack, lc.trace_block);
-  if (br)
-    launch_kind<true>(mode, counters, S, W, ctl, max_stack, *br, lc, smem, st);
+  if (br && lc.motion)
+    launch_kind<true, true>(mode, counters, S, W, ctl, max_stack, *br, lc, smem, st);
+  else if (br)
+    launch_kind<true, false>(mode, counters, S, W, ctl, max_stack, *br, lc, smem, st);
+  else if (lc.motion)
+    launch_kind<false, true>(mode, counters, S, W, ctl, max_stack, BatchRefs{}, lc, smem, st);
   else
-    launch_kind<false>(mode, counters, S, W, ctl, max_stack, BatchRefs{}, lc, smem, st);
+    launch_kind<false, false>(mode, counters, S, W, ctl, max_stack, BatchRefs{}, lc, smem, st);
 }
 
 void launch_first_hits(const DevScene& S, int w, int h, int frame, uint32_t* prim, uint32_t* mat,
                        float* t, int max_stack, uint32_t* err, int grid, cudaStream_t st) {
   FirstHitOut fo{prim, mat, t, w, h, frame, err};
   WaveState none{};
-  k_trace_t<TRACE_FIRST, false, false>
-      <<<grid, PT_TRACE_BLOCK, trace_smem(max_stack, PT_TRACE_BLOCK), st>>>(
-          S, none, nullptr, max_stack, fo, BatchRefs{}, 32);
+  if (S.has_motion)
+    k_trace_t<TRACE_FIRST, false, false, true>
+        <<<grid, PT_TRACE_BLOCK, trace_smem(max_stack, PT_TRACE_BLOCK), st>>>(
+            S, none, nullptr, max_stack, fo, BatchRefs{}, 32);
+  else
+    k_trace_t<TRACE_FIRST, false, false, false>
+        <<<grid, PT_TRACE_BLOCK, trace_smem(max_stack, PT_TRACE_BLOCK), st>>>(
+            S, none, nullptr, max_stack, fo, BatchRefs{}, 32);
 }
 
 }  // namespace pt

@@ -2,12 +2,14 @@
  * pt_types.h - data layout in device memory, shared by host and device code.
  *
  * Primitive record (48 B, 3 x float4, stored in BVH leaf order):
- *   r0 = (f0, f1, f2, tag)     tag bits 0-1 type, 2-3 axis, 4 flip,
- *                              8-31 transform index + 1 (0 = world space)
+ *   r0 = (f0, f1, f2, tag)     tag bits 0-1 type, 2-3 axis, 4 flip, 5 moving
+ *                              sphere, 8-31 transform index + 1 (0 = world space)
  *   r1 = (f3, f4, f5, prim id) prim id = call-order id (tie-break, output)
  *   r2 = (f6, f7, f8, material id)
  *   triangle: f0..2 = v0, f3..5 = v1, f6..8 = v2 (world space)
  *   sphere:   f0..2 = centre, f3 = radius
+ *   moving sphere (type sphere, tag bit 5): f0..2 = centre at time0,
+ *             f3 = radius, f4 = time0, f5 = time1, f6..8 = centre at time1
  *   rect:     f0..4 = a0, a1, b0, b1, k
  *   box:      f0..2 = min, f3..5 = max
  * BVH8 node (80 B, 5 x uint4), compressed child boxes after Ylitie, Karras &
@@ -34,6 +36,7 @@
 #define PT_PRIM_SPHERE 1
 #define PT_PRIM_RECT 2
 #define PT_PRIM_BOX 3
+#define PT_PRIM_MOVING 0x20u  /* tag bit of a moving sphere */
 
 #define PT_MAT_LAMBERTIAN 0
 #define PT_MAT_METAL 1
@@ -123,6 +126,8 @@ struct DevScene {
   int num_prims;
   uint32_t root;            /* BVH8 node where traversal starts (0 for one scene) */
   int tri_only;             /* every primitive is a triangle (no type dispatch in traversal) */
+  int has_motion;           /* some sphere moves: rays carry their path's time */
+  int pad;
   const GpuTexture* textures;
   const float4* tex_data;   /* image texels (rgba, row 0 at v = 0) and noise tables */
   const int* tex_list;      /* entries of vector textures */

@@ -99,6 +99,8 @@ SIGNATURES = {
     "pt_material_set_texture": [_P, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint32],
     "pt_mesh_set_texture_index": [_P, ctypes.c_uint32, ctypes.c_size_t, _P],
     "pt_add_sphere": [_P, _F3, ctypes.c_float, ctypes.c_uint32, _P, _U32P],
+    "pt_add_moving_sphere": [_P, _F3, _F3, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_uint32, _P, _U32P],
     "pt_add_rect": [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                     ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, _P, _U32P],
     "pt_add_box": [_P, _F3, _F3, ctypes.c_uint32, _P, _U32P],
@@ -335,7 +337,7 @@ class Scene:
         self.textures = []    # (kind, a, b, c[9], data, perm, ids)
         self.mat_textures = []  # (material, slot, texture) in call order
         self.tex_index = {}   # mesh item index -> per-face texture index (uint32)
-        self.items = []       # ("sphere"|"rect"|"box"|"mesh", args...)
+        self.items = []       # ("sphere"|"msphere"|"rect"|"box"|"mesh", args...)
         self.add_obj = {}     # item index -> (ObjMesh, material or None): load with pt_add_obj
         self.lights = []      # ("rect"|"sphere", args..., emission)
         self.miss = ("constant", (0.0, 0.0, 0.0))
@@ -415,6 +417,14 @@ class Scene:
     # geometry (host_includes/hitables.hpp, mesh.hpp)
     def sphere(self, center, radius, mat, xform=None):
         self.items.append(("sphere", tuple(center), float(radius), mat, xform))
+        self.n_prims += 1
+        return self.n_prims - 1
+
+    def moving_sphere(self, center0, center1, radius, time0, time1, mat, xform=None):
+        """Moving_Sphere (hitables.hpp:130-181): centre center0 at time0,
+        center1 at time1, linear in the path's time."""
+        self.items.append(("msphere", tuple(center0), tuple(center1), float(radius), float(time0),
+                           float(time1), mat, xform))
         self.n_prims += 1
         return self.n_prims - 1
 
@@ -601,6 +611,10 @@ class GpuRenderer:
             elif it[0] == "sphere":
                 _, cen, r, m, xf = it
                 self._c(L.pt_add_sphere(c, f3(cen), r, mids[m], _ptr(xf), ctypes.byref(pid)))
+            elif it[0] == "msphere":
+                _, c0, c1, r, t0, t1, m, xf = it
+                self._c(L.pt_add_moving_sphere(c, f3(c0), f3(c1), r, t0, t1, mids[m], _ptr(xf),
+                                               ctypes.byref(pid)))
             elif it[0] == "rect":
                 _, (a0, a1, b0, b1, k), flip, axis, m, xf = it
                 self._c(L.pt_add_rect(c, a0, a1, b0, b1, k, flip, axis, mids[m], _ptr(xf),
@@ -912,6 +926,41 @@ def random_spheres(width=1920, height=1080, seed=0, grid=11):
     return s
 
 
+def moving_spheres(width=640, height=360, seed=0, grid=5):
+    """Motion-blur form of the random spheres (the reference's
+    Moving_Sphere, hitables.hpp:130-181): the diffuse small spheres rise by
+    up to 0.5 between time 0 and time 1, the camera's shutter spans [0, 1];
+    a ceiling light quad over the scene is sampled by NEE, so shadow rays
+    meet the moving spheres at their path's time too."""
+    rng = SplitMix64(seed)
+    U = rng.uniform
+    s = Scene()
+    s.miss_gradient((1.0, 1.0, 1.0), (0.5, 0.7, 1.0))
+    ground = s.lambertian((0.5, 0.5, 0.5))
+    s.sphere((0.0, -1000.0, 0.0), 1000.0, ground)
+    for a in range(-grid, grid):
+        for b in range(-grid, grid):
+            choose = U()
+            center = (a + 0.9 * U(), 0.2, b + 0.9 * U())
+            if choose < 0.7:
+                m = s.lambertian((U() * U(), U() * U(), U() * U()))
+                s.moving_sphere(center, (center[0], center[1] + 0.5 * U(), center[2]), 0.2, 0.0,
+                                1.0, m)
+            elif choose < 0.9:
+                m = s.metal((0.5 * (1 + U()), 0.5 * (1 + U()), 0.5 * (1 + U())), 0.5 * U())
+                s.sphere(center, 0.2, m)
+            else:
+                s.moving_sphere(center, (center[0] + 0.3 * U(), center[1], center[2]), 0.2, 0.25,
+                                0.75, s.dielectric((1.0, 1.0, 1.0), (U(), U(), U()), 1.5))
+    s.sphere((0.0, 1.0, 0.5), 1.0, s.lambertian((0.4, 0.2, 0.1)))
+    s.moving_sphere((-3.0, 1.0, 1.0), (-3.0, 1.6, 1.0), 1.0, 0.0, 1.0, s.metal((0.7, 0.6, 0.5), 0.0))
+    lt = s.diffuse_light((8.0, 8.0, 8.0))
+    s.rect(-1.5, 1.5, -1.5, 1.5, 5.0, 1, 1, lt)
+    s.light_rect(-1.5, 1.5, -1.5, 1.5, 5.0, 1, (8.0, 8.0, 8.0))
+    s.set_camera((13, 2, 3), (0, 0, 0), (0, 1, 0), 20.0, width / height, 0.1, 10.0, 0.0, 1.0)
+    return s
+
+
 def _hash01(i, j, seed):
     """Uniform [0,1) lattice values: splitmix64 finaliser of (i, j, seed)."""
     with np.errstate(over="ignore"):
@@ -1113,7 +1162,7 @@ def material_zoo(width=128, height=96, cells=12):
 # ------------------------------------------------------------ headless CLI
 SCENES = {"cornell": cornell_c1, "cornell_reference": cornell_reference,
           "spheres": random_spheres, "heightfield": heightfield_scene,
-          "guide_box": guide_box_scene, "zoo": material_zoo}
+          "guide_box": guide_box_scene, "zoo": material_zoo, "moving_spheres": moving_spheres}
 
 
 def main(argv=None):

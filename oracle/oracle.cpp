@@ -217,7 +217,9 @@ inline V3 Spherical_Vector(float sintheta, float costheta, float phi) {
 // ------------------------------------------------------------------ scene --
 enum { MAT_LAMBERTIAN = 0, MAT_METAL, MAT_DIELECTRIC, MAT_DIFFUSE_LIGHT,
        MAT_OREN_NAYAR, MAT_TORRANCE_SPARROW, MAT_ASHIKHMIN_SHIRLEY };
-enum { PRIM_TRIANGLE = 0, PRIM_SPHERE = 1, PRIM_RECT = 2, PRIM_BOX = 3 };
+// PRIM_MSPHERE: the moving sphere of programs/hitables/moving_sphere.cu,
+// f = center0 (3), radius, time0, time1, center1 (3)
+enum { PRIM_TRIANGLE = 0, PRIM_SPHERE = 1, PRIM_RECT = 2, PRIM_BOX = 3, PRIM_MSPHERE = 4 };
 enum { LIGHT_RECT = 0, LIGHT_SPHERE = 1 };
 enum { MISS_GRADIENT = 0, MISS_CONSTANT = 1, MISS_ENV = 2, MISS_IMAGE = 3 };
 
@@ -359,6 +361,7 @@ void affine_inverse(const float* m, float* out) {
 struct Ray {
   V3 o, d;
   float tmin, tmax;
+  float time = 0.f;  // the path's time (color(): prd.time, programs/raygen.cu:69)
 };
 
 struct HitRecord {
@@ -369,11 +372,17 @@ struct HitRecord {
   V3 geometric_normal, shading_normal, Wo;
 };
 
+// Centre of a moving sphere at `time`: programs/hitables/moving_sphere.cu:47-49
+// (linear in time, also outside [time0, time1]).
+inline V3 msphere_center(const Prim& p, float time) {
+  V3 c0 = v3(p.f[0], p.f[1], p.f[2]), c1 = v3(p.f[6], p.f[7], p.f[8]);
+  return c0 + ((time - p.f[4]) / (p.f[5] - p.f[4])) * (c1 - c0);
+}
+
 // Candidate t of one primitive for an (object-space) ray; false if none.
-// programs/hitables/sphere.cu:32-62
-bool sphere_candidate(const Prim& p, V3 o, V3 d, float tmin, float tmax, float& t) {
-  V3 center = v3(p.f[0], p.f[1], p.f[2]);
-  float radius = p.f[3];
+// programs/hitables/sphere.cu:32-62 (a moving sphere: moving_sphere.cu:57-118
+// at its centre for the ray's time, the same two roots)
+bool sphere_candidate(V3 center, float radius, V3 o, V3 d, float tmin, float tmax, float& t) {
   V3 oc = o - center;
   float a = dot(d, d);
   float b = dot(oc, d);
@@ -476,7 +485,8 @@ bool prim_candidate(const Scene& s, const Prim& p, const Ray& r, float& t, float
   object_ray(s, p, r, o, d);
   bu = bv = 0.0f;
   switch (p.type) {
-    case PRIM_SPHERE: return sphere_candidate(p, o, d, r.tmin, r.tmax, t);
+    case PRIM_SPHERE: return sphere_candidate(v3(p.f[0], p.f[1], p.f[2]), p.f[3], o, d, r.tmin, r.tmax, t);
+    case PRIM_MSPHERE: return sphere_candidate(msphere_center(p, r.time), p.f[3], o, d, r.tmin, r.tmax, t);
     case PRIM_RECT: return rect_candidate(p, o, d, r.tmin, r.tmax, t);
     case PRIM_BOX: return box_candidate(p, o, d, r.tmin, r.tmax, t);
     default: return tri_candidate(p, o, d, r.tmin, r.tmax, t, bu, bv);
@@ -494,8 +504,10 @@ HitRecord hit_record(const Scene& s, const Prim& p, const Ray& r, float t_hit, f
   const float* I = p.xform >= 0 ? s.xforms[p.xform].inv : nullptr;
   rec.index = p.material;
   rec.tindex = p.type == PRIM_TRIANGLE ? p.tindex : 0;
-  if (p.type == PRIM_SPHERE) {  // programs/hitables/sphere.cu:65-93
-    V3 center = v3(p.f[0], p.f[1], p.f[2]);
+  if (p.type == PRIM_SPHERE || p.type == PRIM_MSPHERE) {
+    // programs/hitables/sphere.cu:65-93; the moving sphere's record
+    // (moving_sphere.cu:80-96) is the same at its centre for the ray's time
+    V3 center = p.type == PRIM_SPHERE ? v3(p.f[0], p.f[1], p.f[2]) : msphere_center(p, r.time);
     float radius = p.f[3];
     V3 hit_point = o + t_hit * d;
     rec.P = M ? xpoint(M, hit_point) : hit_point;
@@ -678,6 +690,15 @@ AABB prim_bounds(const Scene& s, const Prim& p) {
   } else if (p.type == PRIM_SPHERE) {
     lo = v3(p.f[0] - p.f[3], p.f[1] - p.f[3], p.f[2] - p.f[3]);
     hi = v3(p.f[0] + p.f[3], p.f[1] + p.f[3], p.f[2] + p.f[3]);
+  } else if (p.type == PRIM_MSPHERE) {
+    // every centre a ray can meet: the ray times lie between cam.time0 and
+    // cam.time0 + (cam.time1 - cam.time0), and the centre is monotonic in
+    // time (moving_sphere.cu:136-147 bounds [time0, time1] only)
+    float te = s.cam.time0 + (s.cam.time1 - s.cam.time0);
+    float ta = fminf(fminf(p.f[4], s.cam.time0), te), tb = fmaxf(fmaxf(p.f[5], s.cam.time0), te);
+    V3 ca = msphere_center(p, ta), cb = msphere_center(p, tb);
+    lo = v3(fminf(ca.x, cb.x) - p.f[3], fminf(ca.y, cb.y) - p.f[3], fminf(ca.z, cb.z) - p.f[3]);
+    hi = v3(fmaxf(ca.x, cb.x) + p.f[3], fmaxf(ca.y, cb.y) + p.f[3], fmaxf(ca.z, cb.z) + p.f[3]);
   } else if (p.type == PRIM_RECT) {
     float a0 = p.f[0], a1 = p.f[1], b0 = p.f[2], b1 = p.f[3], k = p.f[4];
     if (p.axis == 0) { lo = v3(k, a0, b0); hi = v3(k, a1, b1); }
@@ -1518,10 +1539,11 @@ struct Tracer {
   const Scene& s;
   Counters* cnt;
   uint64_t ext = 0, shadow = 0;
+  float tm = 0.f;  // the current path's time: every ray of the path carries it
 
   // Shadow test: true if occluded.  programs/hit.cu:16-24 under closest-hit.
   bool occluded(V3 P, V3 Wi, V3 N) {
-    Ray r{P, Wi, 1e-3f, RAY_TMAX};
+    Ray r{P, Wi, 1e-3f, RAY_TMAX, tm};
     shadow++;
     Hit h = trace(s, r, cnt);
     if (h.prim < 0) return true;
@@ -1721,6 +1743,8 @@ struct Tracer {
     PRD prd;
     prd.seed = seed;
     prd.time = s.cam.time0 + rnd(prd.seed) * (s.cam.time1 - s.cam.time0);
+    tm = prd.time;
+    ray.time = tm;
     prd.throughput = v3(1.f);
     prd.radiance = v3(0.f);
     prd.isSpecular = false;
@@ -1738,7 +1762,7 @@ struct Tracer {
       } else if (prd.scatterEvent == EV_CANCELLED) {
         return prd.radiance;
       } else {
-        ray = Ray{prd.origin, prd.direction, 1e-3f, RAY_TMAX};
+        ray = Ray{prd.origin, prd.direction, 1e-3f, RAY_TMAX, tm};
         previousHitSpecular = prd.isSpecular;
       }
       if (pr.rr_enable) {
@@ -1764,8 +1788,8 @@ struct Tracer {
   }
 
   V3 color_c(Ray ray, uint32_t seed, const Params& pr) {
-    float tm = s.cam.time0 + rnd(seed) * (s.cam.time1 - s.cam.time0);
-    (void)tm;
+    tm = s.cam.time0 + rnd(seed) * (s.cam.time1 - s.cam.time0);
+    ray.time = tm;
     V3 thr = v3(1.f), rad = v3(0.f);
     bool prev_spec = true;
     float pdf_prev = 0.f;
@@ -1803,7 +1827,7 @@ struct Tracer {
         closest_hit(prd, ray, h);
         seed = prd.seed;
         thr = prd.throughput;
-        ray = Ray{prd.origin, prd.direction, 1e-3f, RAY_TMAX};
+        ray = Ray{prd.origin, prd.direction, 1e-3f, RAY_TMAX, tm};
         prev_spec = true;
       } else {
         Frame fr(N);
@@ -1850,7 +1874,7 @@ struct Tracer {
             V3 c = f * Le * (cs * power_mis(pls, pb) / pls);
             if (!isNull(c)) {
               shadow++;
-              Ray sr{P, Wi, 1e-3f, tmax};
+              Ray sr{P, Wi, 1e-3f, tmax, tm};
               Hit sh = trace(s, sr, cnt);
               if (sh.prim < 0) rad += thr * c;
             }
@@ -1864,7 +1888,7 @@ struct Tracer {
         thr *= f * (wi_l.y / pb);
         prev_spec = false;
         pdf_prev = pb;
-        ray = Ray{P, fr.to_world(wi_l), 1e-3f, RAY_TMAX};
+        ray = Ray{P, fr.to_world(wi_l), 1e-3f, RAY_TMAX, tm};
       }
       if (pr.rr_enable && depth > pr.rr_depth) {
         float q = fminf(1.f, max_component(thr));
@@ -1944,7 +1968,8 @@ static int add_xform(Scene& s, const float* x) {
 }
 
 // type PRIM_SPHERE: f = cx,cy,cz,r; PRIM_RECT: a0,a1,b0,b1,k (axis, flip);
-// PRIM_BOX: x0,y0,z0,x1,y1,z1.  Returns the primitive id.
+// PRIM_BOX: x0,y0,z0,x1,y1,z1; PRIM_MSPHERE: c0 (3), r, t0, t1, c1 (3).
+// Returns the primitive id.
 int or_add_prim(void* sp, int type, const float* f, int axis, int flip, int material,
                 const float* xform) {
   Scene& s = *(Scene*)sp;
@@ -1955,7 +1980,7 @@ int or_add_prim(void* sp, int type, const float* f, int axis, int flip, int mate
   p.flip = flip;
   p.material = material;
   p.mesh = -1;
-  memcpy(p.f, f, sizeof(float) * (type == PRIM_SPHERE ? 4 : (type == PRIM_RECT ? 5 : 6)));
+  memcpy(p.f, f, sizeof(float) * (type == PRIM_SPHERE ? 4 : (type == PRIM_RECT ? 5 : (type == PRIM_MSPHERE ? 9 : 6))));
   p.xform = add_xform(s, xform);
   s.prims.push_back(p);
   return (int)s.prims.size() - 1;
@@ -2122,6 +2147,7 @@ void or_first_hits(void* sp, int W, int H, int frame, int32_t* prim, int32_t* ma
     uint32_t x = p % W, y = p / W;
     uint32_t seed = tea64((uint32_t)W * y + x, (uint32_t)frame);
     Ray ray = tr.camera_ray(x, y, W, H, seed);
+    ray.time = s.cam.time0 + rnd(seed) * (s.cam.time1 - s.cam.time0);  // color()'s prd.time
     Hit h = trace(s, ray, nullptr);
     prim[p] = h.prim;
     mat[p] = h.prim >= 0 ? s.prims[h.prim].material : -1;
@@ -2499,6 +2525,7 @@ bool cand64(const Scene& s, const Prim& p, D3 o, D3 d, double tmin, Cand64& c64)
   c64.margin = -1.0;
   c64.mslack = 1.0;
   bool hit = false;
+  if (p.type == PRIM_MSPHERE) return false;  // (the statement covers static primitives)
   if (p.type == PRIM_SPHERE) {
     double r = f[3];
     D3 oc = dsub(o, D3{f[0], f[1], f[2]});
@@ -2673,4 +2700,33 @@ extern "C" int or_prim64(void* sp, int prim, const float* o, const float* d, flo
   out[2] = c.mslack;
   out[3] = c.tslack;
   return hit ? 1 : 0;
+}
+
+// A moving sphere (f = centre at time0 (3), radius, time0, time1, centre at
+// time1 (3)) against one ray at `time`: 1 on a hit, out = t, P (3), shading
+// normal (3), u, v, Wo (3); and its box for camera times cam_t0, cam_t1
+// (box6 = lo, hi).  Test infrastructure: pins the oracle's moving sphere to
+// programs/hitables/moving_sphere.cu.
+extern "C" int or_msphere(const float* f, const float* o, const float* d, float tmin, float tmax,
+                          float time, float* out, float cam_t0, float cam_t1, float* box6) {
+  Scene s;
+  s.cam.time0 = cam_t0;
+  s.cam.time1 = cam_t1;
+  Prim p;
+  memset(&p, 0, sizeof(p));
+  p.type = PRIM_MSPHERE;
+  p.xform = -1;
+  p.mesh = -1;
+  memcpy(p.f, f, 9 * sizeof(float));
+  AABB b = prim_bounds(s, p);
+  box6[0] = b.lo.x; box6[1] = b.lo.y; box6[2] = b.lo.z;
+  box6[3] = b.hi.x; box6[4] = b.hi.y; box6[5] = b.hi.z;
+  Ray r{v3(o[0], o[1], o[2]), v3(d[0], d[1], d[2]), tmin, tmax, time};
+  float t = 0.f, bu = 0.f, bv = 0.f;
+  if (!prim_candidate(s, p, r, t, bu, bv)) return 0;
+  HitRecord rec = hit_record(s, p, r, t, bu, bv);
+  float v[13] = {t, rec.P.x, rec.P.y, rec.P.z, rec.shading_normal.x, rec.shading_normal.y,
+                 rec.shading_normal.z, rec.u, rec.v, rec.Wo.x, rec.Wo.y, rec.Wo.z, 0.f};
+  memcpy(out, v, 12 * sizeof(float));
+  return 1;
 }

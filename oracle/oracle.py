@@ -76,6 +76,8 @@ def load():
     L.or_camera_rays.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]
     L.or_trace64.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_float, _P, _P, ctypes.c_int]
     L.or_prim64.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_float, _P]
+    L.or_msphere.argtypes = [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P,
+                             ctypes.c_float, ctypes.c_float, _P]
     _lib = L
     return L
 
@@ -107,6 +109,11 @@ def replay(L, prefix, h, s):
         if it[0] == "sphere":
             _, cen, r, m, xf = it
             fn("add_prim")(h, 1, _p(_f(list(cen) + [r])), 0, 0, m, _p(xf))
+        elif it[0] == "msphere":
+            if prefix != "or_":
+                raise NotImplementedError("the reference harness has no moving sphere scene path")
+            _, c0, c1, r, t0, t1, m, xf = it
+            fn("add_prim")(h, 4, _p(_f(list(c0) + [r, t0, t1] + list(c1))), 0, 0, m, _p(xf))
         elif it[0] == "rect":
             _, v5, flip, axis, m, xf = it
             fn("add_prim")(h, 2, _p(_f(v5)), axis, flip, m, _p(xf))
@@ -252,3 +259,15 @@ def bsdf_c_batch(mtype, c0, c1, p0, p1, wo, wi):
     c1a = None if c1 is None else _f(c1)
     L.or_bsdf_c_batch(mtype, _p(_f(c0)), _p(c1a), p0, p1, _p(_f(wo)), n, _p(wi), _p(f), _p(pdf))
     return f, pdf
+
+
+def msphere(f9, o, d, tmin, tmax, time, cam_t0=0.0, cam_t1=1.0):
+    """The oracle's moving sphere (f9 = centre at time0, radius, time0,
+    time1, centre at time1) against one ray at `time`: (hit, [t, P, shading
+    normal, u, v, Wo] as 12 floats, box6 for the camera times)."""
+    L = load()
+    out = np.zeros(12, np.float32)
+    box = np.zeros(6, np.float32)
+    hit = L.or_msphere(_p(_f(f9)), _p(_f(o)), _p(_f(d)), tmin, tmax, time, _p(out), cam_t0, cam_t1,
+                       _p(box))
+    return bool(hit), out, box

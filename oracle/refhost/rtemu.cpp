@@ -260,6 +260,7 @@ bool rtemu_report_intersection(unsigned int) {
 void rtemu_terminate_ray() {}
 
 float3 rtemu_transform_point(int kind, const float3& p) {
+  if (cur_prim < 0) return p;  // a program called on its own: object = world
   const Prim& pr = g->prims[cur_prim];
   if (pr.xform < 0) return p;
   const Xform& x = g->xforms[pr.xform];
@@ -267,6 +268,7 @@ float3 rtemu_transform_point(int kind, const float3& p) {
 }
 
 float3 rtemu_transform_normal(int kind, const float3& n) {
+  if (cur_prim < 0) return n;
   const Prim& pr = g->prims[cur_prim];
   if (pr.xform < 0) return n;
   const Xform& x = g->xforms[pr.xform];
@@ -778,3 +780,29 @@ void rh_stats(void* sp, uint64_t* out) {
 }
 
 }  // extern "C"
+
+// The moving sphere of programs/hitables/moving_sphere.cu (f = centre at
+// time0 (3), radius, time0, time1, centre at time1 (3)) against one ray at
+// `time`: 1 and out = t, P (3), shading normal (3), u, v, Wo (3) if it
+// reports a hit; box6 = its get_bounds box.
+extern "C" int rh_msphere(const float* f, const float* o, const float* d, float tmin, float tmax,
+                          float time, float* out, float* box6) {
+  ref_msphere_bounds(f, box6);
+  Ray r = make_Ray(make_float3(o[0], o[1], o[2]), make_float3(d[0], d[1], d[2]), 0, tmin, tmax);
+  TraceState st;
+  memset(&st, 0, sizeof(st));
+  st.tmin = tmin;
+  st.tmax = tmax;
+  TraceState* saved = ts;
+  int saved_prim = cur_prim;
+  ts = &st;
+  cur_prim = -1;
+  float rec[11];
+  ref_msphere_intersect(f, &r, time, rec);
+  ts = saved;
+  cur_prim = saved_prim;
+  if (!st.reported) return 0;
+  out[0] = st.tmax;
+  for (int k = 0; k < 11; k++) out[1 + k] = rec[k];
+  return 1;
+}

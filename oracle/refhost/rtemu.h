@@ -49,6 +49,10 @@ void ref_box_intersect(const float* f, const Ray* ray, int* geo_index, float2* b
 void ref_box_hitrecord(const float* f, int index, const Ray* ray, float t, float2 bc,
                        EmuRec* out);
 void ref_box_bounds(const float* f, float* box6);
+// programs/hitables/moving_sphere.cu (its record is the hit_rec attribute;
+// out = P, shading normal, u, v, Wo of the reported hit)
+void ref_msphere_intersect(const float* f, const Ray* ray, float time, float* out);
+void ref_msphere_bounds(const float* f, float* box6);
 void ref_triangle_bind(const float3* verts, size_t nv, const float3* normals, size_t nn,
                        const float2* uvs, size_t nuv, const int3* idx, size_t nt,
                        const int* mats);

@@ -182,7 +182,16 @@ inline Ray make_Ray(float3 origin, float3 direction, unsigned int ray_type, floa
   return r;
 }
 
-struct Aabb { float3 m_min, m_max; };
+struct Aabb {
+  float3 m_min, m_max;
+  // optix::Aabb::include: grows the box to hold b (component min / max)
+  void include(const Aabb& b) {
+    m_min = make_float3(std::fmin(m_min.x, b.m_min.x), std::fmin(m_min.y, b.m_min.y),
+                        std::fmin(m_min.z, b.m_min.z));
+    m_max = make_float3(std::fmax(m_max.x, b.m_max.x), std::fmax(m_max.y, b.m_max.y),
+                        std::fmax(m_max.z, b.m_max.z));
+  }
+};
 struct rtObject {};
 
 // The scene-graph root `world`.  light_sample.cuh:69 names it inside the

@@ -76,6 +76,7 @@ def load():
     L.rh_triangle_sw.argtypes = [_P, i, _P, _P, fl, _P]
     L.rh_light.argtypes = [_P, i, i, _P, _P, _P, _P]
     L.rh_stats.argtypes = [_P, _P]
+    L.rh_msphere.argtypes = [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, _P]
     L.ref_tea64.argtypes = [u, u]
     L.ref_tea64.restype = u
     L.ref_lcg_stream.argtypes = [u, i, _P]
@@ -228,3 +229,13 @@ def oracle_probe(orc, o, d, tmin=1e-6):
     rec = np.zeros(17, np.float32)
     pid = L.or_probe(orc.h, _p(_f(o)), _p(_f(d)), tmin, _p(t), _p(rec))
     return pid, float(t[0]), rec
+
+
+def msphere(f9, o, d, tmin, tmax, time):
+    """programs/hitables/moving_sphere.cu on one ray at `time`: (hit, [t, P,
+    shading normal, u, v, Wo] as 12 floats, get_bounds box6)."""
+    L = load()
+    out = np.zeros(12, np.float32)
+    box = np.zeros(6, np.float32)
+    hit = L.rh_msphere(_p(_f(f9)), _p(_f(o)), _p(_f(d)), tmin, tmax, time, _p(out), _p(box))
+    return bool(hit), out, box

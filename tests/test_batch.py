@@ -25,6 +25,7 @@ def renderers(ptgb_mod):
         "zoo": P.GpuRenderer(P.material_zoo(32, 24)),
         "heightfield": P.GpuRenderer(P.heightfield_scene(48, 27, cells=40, env_w=128, env_h=64)),
         "empty": P.GpuRenderer(empty_scene(P, 16, 12)),
+        "moving": P.GpuRenderer(P.moving_spheres(40, 24, grid=3)),
     }
     yield out
     for r in out.values():
@@ -41,6 +42,7 @@ def jobs_ref_mode(P, R):
         (R["empty"], prm(16, 12, 3)),
         (R["cornell_ref"], prm(24, 24, 5, rr_enable=0, max_depth=12)),
         (R["spheres"], prm(48, 27, 3, frame0=0, rr_depth=2)),  # same scene, other params
+        (R["moving"], prm(40, 24, 3)),  # moving spheres: the paths' times in a batch
     ]
 
 

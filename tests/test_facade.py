@@ -33,6 +33,8 @@ void build(Context& ctx) {
   as.assignTo(ctx);
   glass.assignTo(ctx);
   (void)noiseZ;
+  Hitable_List list;
+  list.push(new Moving_Sphere(make_float3(0, 0, 0), make_float3(0, 1, 0), 0.5f, 0.f, 1.f, &lam));
 }
 int main(){ pt::Hitable_List l; (void)l; (void)&build; return 0; }
 ''')

@@ -18,6 +18,7 @@ def scenes(ptgb):
         "zoo": (ptgb.material_zoo(80, 60), 80, 60, dict(rr_depth=10)),
         "heightfield_c3": (ptgb.heightfield_scene(96, 54, cells=48, env_w=256, env_h=128), 96, 54,
                            dict(rr_depth=10)),
+        "moving": (ptgb.moving_spheres(96, 54), 96, 54, dict(rr_depth=10)),
     }
 
 
@@ -31,7 +32,7 @@ def cases(ptgb_mod, oracle_mod):
         g.close()
 
 
-NAMES = ["cornell_ref", "cornell_c1", "spheres_c2", "zoo", "heightfield_c3"]
+NAMES = ["cornell_ref", "cornell_c1", "spheres_c2", "zoo", "heightfield_c3", "moving"]
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -124,12 +125,15 @@ def test_errors(ptgb_mod):
 
 
 @pytest.mark.parametrize("builder", [1, 2])
-@pytest.mark.parametrize("name", ["zoo", "heightfield", "spheres"])
+@pytest.mark.parametrize("name", ["zoo", "heightfield", "spheres", "moving"])
 def test_builders_match_oracle(ptgb_mod, oracle_mod, builder, name):
     """The host (binned SAH) and GPU (LBVH + treelets) BVH8 builders give the
-    same first hits and paths as the oracle."""
+    same first hits and paths as the oracle (moving spheres: boxes over the
+    camera's shutter)."""
     if name == "zoo":
         s, w, h = ptgb_mod.material_zoo(64, 48), 64, 48
+    elif name == "moving":
+        s, w, h = ptgb_mod.moving_spheres(64, 36, grid=8), 64, 36
     elif name == "spheres":
         s, w, h = ptgb_mod.random_spheres(64, 36), 64, 36
     else:
@@ -178,7 +182,7 @@ def test_gpu_builder_large_mesh(ptgb_mod):
     g.close()
 
 
-CONSISTENT = ["cornell_c1", "zoo", "heightfield_c3", "spheres_c2"]
+CONSISTENT = ["cornell_c1", "zoo", "heightfield_c3", "spheres_c2", "moving"]
 
 
 @pytest.mark.parametrize("name", CONSISTENT)

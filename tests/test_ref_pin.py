@@ -243,6 +243,37 @@ def test_intersection_and_hitrecord(rng, ptgb_mod, oracle_mod, name):
     assert hits > 400
 
 
+def test_moving_sphere_program(rng, oracle_mod):
+    """programs/hitables/moving_sphere.cu (compiled over the stand-in, its
+    time taken from the ray's payload) against the oracle's moving sphere on
+    random rays at random times, also outside [time0, time1] (the centre is
+    extrapolated): the same hit, t, P, shading normal, u, v and Wo; and its
+    get_bounds box lies inside the oracle's box (which also covers the
+    camera's times)."""
+    hits = 0
+    for _ in range(4000):
+        c0 = rng.uniform(-1, 1, 3).astype(np.float32)
+        c1 = (c0 + rng.uniform(-0.8, 0.8, 3)).astype(np.float32)
+        r = np.float32(rng.uniform(0.2, 0.9))
+        t0 = np.float32(rng.uniform(-0.5, 0.5))
+        t1 = np.float32(t0 + rng.uniform(0.1, 2.0))
+        f9 = np.array(list(c0) + [r, t0, t1] + list(c1), np.float32)
+        time = np.float32(rng.uniform(t0 - 0.5, t1 + 0.5))
+        o = rng.uniform(-3, 3, 3).astype(np.float32)
+        d = (rng.uniform(-0.8, 0.8, 3) - o).astype(np.float32)
+        if rng.uniform() < 0.5:
+            d = (d * rng.uniform(0.1, 10.0)).astype(np.float32)
+        tmin = np.float32(1e-3 if rng.uniform() < 0.5 else 1e-6)
+        hr, outr, boxr = refpin.msphere(f9, o, d, tmin, np.float32(1e20), time)
+        ho, outo, boxo = oracle_mod.msphere(f9, o, d, tmin, np.float32(1e20), time, t0, t1)
+        assert hr == ho, (f9, o, d, time)
+        if hr:
+            hits += 1
+            assert np.array_equal(outr, outo), (f9, o, d, time, outr, outo)
+        assert np.all(boxo[:3] <= boxr[:3]) and np.all(boxo[3:] >= boxr[3:])
+    assert hits > 500
+
+
 def test_software_triangle_program_against_watertight(rng, ptgb_mod):
     """The reference's non-RTX triangle program (triangle.cu:26-58,
     Moller-Trumbore without a watertight guarantee) against the watertight

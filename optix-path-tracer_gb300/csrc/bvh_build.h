@@ -29,6 +29,13 @@ struct WideChild {
   uint32_t prim_off;  /* leaf: offset from the node's prim_base */
 };
 
+/* Device scratch of the GPU builder, kept by its owner across builds (grown
+ * on demand, freed with cudaFree by the owner). */
+struct BuildArena {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
 struct Bvh8Out {
   std::vector<uint32_t> nodes;       /* 20 words per node */
   std::vector<uint32_t> leaf_order;  /* primitive index at each leaf position */

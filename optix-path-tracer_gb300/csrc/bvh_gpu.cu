@@ -578,10 +578,19 @@ __global__ void k_gather_boxes(const float4* lo, const float4* hi, const uint32_
   shi[i] = hi[p];
 }
 
-template <typename T>
-static cudaError_t dalloc(T** p, size_t n) {
-  return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
-}
+// Carves the builder's scratch arrays out of one device arena that persists
+// across builds (grown only when a scene needs more), so a commit makes no
+// allocation once the arena fits.
+struct Carve {
+  unsigned char* base;
+  size_t off;
+  template <typename T>
+  void take(T** p, size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    *p = base ? (T*)(base + off) : nullptr;
+    off += (n ? n : 1) * sizeof(T);
+  }
+};
 
 }  // namespace
 
@@ -595,7 +604,7 @@ namespace pt {
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
                            uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
-                           float cam_t0, float cam_t1, cudaStream_t st) {
+                           float cam_t0, float cam_t1, BuildArena* arena, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
   if (width < 2 || width > 8) width = 8;
   float4 *lo = nullptr, *hi = nullptr, *ilo = nullptr, *ihi = nullptr, *slo = nullptr,
@@ -615,33 +624,50 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
     e = (x);                          \
     if (e != cudaSuccess) goto done;  \
   } while (0)
-  BV(dalloc(&lo, n));
-  BV(dalloc(&hi, n));
-  BV(dalloc(&slo, n));
-  BV(dalloc(&shi, n));
-  BV(dalloc(&ilo, ni));
-  BV(dalloc(&ihi, ni));
-  BV(dalloc(&keys, n));
-  BV(dalloc(&vals, n));
-  BV(dalloc(&keys2, n));
-  BV(dalloc(&vals2, n));
-  BV(dalloc(&left, ni));
-  BV(dalloc(&right, ni));
-  BV(dalloc(&pint, ni));
-  BV(dalloc(&pleaf, n));
-  BV(dalloc(&flags, ni));
-  BV(dalloc(&counters, 4));
-  BV(dalloc(&cbox, 6));
-  BV(dalloc(&qa, n));
-  BV(dalloc(&qb, n));
+  // the radix sort's temporary size (a query: no sorting, no allocation)
+  BV(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0, 30,
+                                     st));
+  {
+    Carve cv{nullptr, 0};
+    for (int pass = 0; pass < 2; pass++) {
+      cv.off = 0;
+      cv.take(&lo, n);
+      cv.take(&hi, n);
+      cv.take(&slo, n);
+      cv.take(&shi, n);
+      cv.take(&ilo, ni);
+      cv.take(&ihi, ni);
+      cv.take(&keys, n);
+      cv.take(&vals, n);
+      cv.take(&keys2, n);
+      cv.take(&vals2, n);
+      cv.take(&left, ni);
+      cv.take(&right, ni);
+      cv.take(&pint, ni);
+      cv.take(&pleaf, n);
+      cv.take(&flags, ni);
+      cv.take(&counters, 4);
+      cv.take(&cbox, 6);
+      cv.take(&qa, n);
+      cv.take(&qb, n);
+      unsigned char* t8 = nullptr;
+      cv.take(&t8, tmp_bytes);
+      tmp = t8;
+      if (pass == 0 && cv.off > arena->bytes) {  // grow the arena
+        if (arena->p) cudaFree(arena->p);
+        arena->p = nullptr;
+        arena->bytes = 0;
+        BV(cudaMalloc(&arena->p, cv.off));
+        arena->bytes = cv.off;
+      }
+      cv.base = (unsigned char*)arena->p;
+    }
+  }
   BV(cudaMemcpyAsync(cbox, h_cbox, sizeof(h_cbox), cudaMemcpyHostToDevice, st));
   {
     uint32_t g = (n + 255) / 256;
     k_bounds<<<g, 256, 0, st>>>(d_rec, d_xforms, n, cam_t0, cam_t1, lo, hi, cbox);
     k_morton<<<g, 256, 0, st>>>(lo, hi, n, cbox, keys, vals);
-    BV(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0, 30,
-                                       st));
-    BV(cudaMalloc(&tmp, tmp_bytes ? tmp_bytes : 1));
     BV(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0, 30, st));
     // leaf bounds in sorted order
     BV(cudaMemsetAsync(pint, 0xff, ni * 4, st));
@@ -687,26 +713,6 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
   }
 done:
 #undef BV
-  cudaFree(lo);
-  cudaFree(hi);
-  cudaFree(slo);
-  cudaFree(shi);
-  cudaFree(ilo);
-  cudaFree(ihi);
-  cudaFree(keys);
-  cudaFree(vals);
-  cudaFree(keys2);
-  cudaFree(vals2);
-  cudaFree(left);
-  cudaFree(right);
-  cudaFree(pint);
-  cudaFree(pleaf);
-  cudaFree(flags);
-  cudaFree(counters);
-  cudaFree(cbox);
-  cudaFree(qa);
-  cudaFree(qb);
-  cudaFree(tmp);
   return e;
 }
 

@@ -32,7 +32,7 @@ namespace pt {
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
                            uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
-                           float cam_t0, float cam_t1, cudaStream_t st);
+                           float cam_t0, float cam_t1, BuildArena* arena, cudaStream_t st);
 }
 
 namespace {
@@ -130,6 +130,13 @@ int pth::device_ptr_kind(const void* p, int device) {
 
 // World-space AABB of a primitive, padded so that rounding in the primitive
 // tests can never place a reported hit outside its box.
+// Forgets the captured wavefront graphs (a new scene, buffers or options).
+static void drop_graphs(pt_context* ctx) {
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  if (ctx->graph2) cudaGraphExecDestroy(ctx->graph2);
+  ctx->graph = ctx->graph2 = nullptr;
+}
+
 static pt::Box prim_box(const pt_context* ctx, const HostPrim& p) {
   float lo[3], hi[3];
   const float* f = p.f;
@@ -212,7 +219,9 @@ PT_API int pt_context_create(const pt_options* opt, pt_context** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
-  if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_ctr, sizeof(WaveCounters));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_ctr, 2 * sizeof(WaveCounters));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->evc[0], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->evc[1], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_ctl, sizeof(WaveCtl));
   if (e != cudaSuccess) {
     int rc = (e == cudaErrorMemoryAllocation) ? PT_ENOMEM : PT_ECUDA;
@@ -228,6 +237,9 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   if (!ctx) return PT_EINVAL;
   cudaSetDevice(ctx->device);
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  if (ctx->graph2) cudaGraphExecDestroy(ctx->graph2);
+  for (cudaEvent_t e : ctx->evc)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
   ctx->d_nodes.release();
   ctx->d_prims.release();
@@ -240,6 +252,10 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_uvs.release();
   ctx->d_leaf_of_id.release();
   ctx->d_rec_in.release();
+  ctx->h_rec.release();
+  ctx->h_check.release();
+  if (ctx->build_arena.p) cudaFree(ctx->build_arena.p);
+  ctx->build_arena = pt::BuildArena{};
   ctx->d_env_marg.release();
   ctx->d_env_cond.release();
   ctx->d_env_rows.release();
@@ -821,12 +837,11 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
   size_t nn = 0;
   if (builder == 2 && n > 0) {
     // records in call order (filled by several host threads for large
-    // scenes), built into leaf order on the device
-    std::unique_ptr<float4[]> rec(new (std::nothrow) float4[3 * n]);
-    if (!rec) return fail(ctx, PT_ENOMEM, "host memory for the primitive records");
+    // scenes, into page-locked staging), built into leaf order on the device
+    CK(ctx->h_rec.ensure(3 * n));
     {
       const HostPrim* src = ctx->prims.data();
-      float4* dst = rec.get();
+      float4* dst = ctx->h_rec.p;
       auto fill = [src, dst](size_t a, size_t b) {
         for (size_t i = a; i < b; i++) prim_record(src[i], (uint32_t)i, dst + 3 * i);
       };
@@ -836,7 +851,7 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
       fill(0, n / parts);
       for (std::thread& th : pool) th.join();
     }
-    CK(ctx->d_rec_in.upload(rec.get(), 3 * n, st));
+    CK(ctx->d_rec_in.upload(ctx->h_rec.p, 3 * n, st));
     CK(d_nodes.ensure(5 * std::max<size_t>(1, n)));
     CK(d_prims.ensure(3 * n));
     CK(d_leaf_of_id.ensure(n));
@@ -844,19 +859,21 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
     int depth = 0;
     CK(pt::build_bvh8_gpu(ctx->d_rec_in.p, ctx->d_xforms.p, (uint32_t)n, d_nodes.p,
                           d_prims.p, d_leaf_of_id.p, &nodes, &depth, PT_TREELET_ROUNDS, width,
-                          ctx->cam.time0, ctx->cam.time1, st));
+                          ctx->cam.time0, ctx->cam.time1, &ctx->build_arena, st));
     if (depth < 0)
       return fail(ctx, PT_EINVAL,
                   "GPU BVH8 failed validation (collapse check " + std::to_string(-depth) + ")");
     nn = nodes;
     bvh.depth = depth;
-    // host-side structural check before any traversal runs on it
-    bvh.nodes.resize((size_t)nodes * 20);
-    std::vector<uint32_t> loid(n);
-    CK(cudaMemcpyAsync(bvh.nodes.data(), d_nodes.p, bvh.nodes.size() * 4,
-                       cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(loid.data(), d_leaf_of_id.p, n * 4, cudaMemcpyDeviceToHost, st));
+    // host-side structural check before any traversal runs on it (nodes and
+    // leaf positions read back through page-locked staging)
+    const size_t nw = (size_t)nodes * 20;
+    CK(ctx->h_check.ensure(nw + n));
+    CK(cudaMemcpyAsync(ctx->h_check.p, d_nodes.p, nw * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctx->h_check.p + nw, d_leaf_of_id.p, n * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    bvh.nodes.assign(ctx->h_check.p, ctx->h_check.p + nw);
+    const uint32_t* loid = ctx->h_check.p + nw;
     bvh.leaf_order.assign(n, 0xffffffffu);
     for (size_t i = 0; i < n; i++) {
       if (loid[i] >= n) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
@@ -894,10 +911,7 @@ PT_API int pt_commit(pt_context* ctx) {
   CK(cudaSetDevice(ctx->device));
   auto t0 = std::chrono::steady_clock::now();
   cudaStream_t st = ctx->stream;
-  if (ctx->graph) {
-    cudaGraphExecDestroy(ctx->graph);
-    ctx->graph = nullptr;
-  }
+  drop_graphs(ctx);
   size_t n = ctx->prims.size();
   std::vector<float4> xf(ctx->xforms.size() / 4 + 1);
   if (!ctx->xforms.empty()) memcpy(xf.data(), ctx->xforms.data(), ctx->xforms.size() * 4);
@@ -1025,10 +1039,7 @@ extern "C" {
 static int ensure_wave(pt_context* ctx, size_t results_needed) {
   int slots = ctx->opt.path_slots > 0 ? ctx->opt.path_slots : (1 << 21);
   if (ctx->slots != slots || !ctx->d_slot_f4.p) {
-    if (ctx->graph) {
-      cudaGraphExecDestroy(ctx->graph);
-      ctx->graph = nullptr;
-    }
+    drop_graphs(ctx);
     CK(ctx->d_slot_f4.ensure((size_t)slots * PT_SLOT_F4));
     CK(ctx->d_slot_u4.ensure((size_t)slots * PT_SLOT_U4));
     CK(ctx->d_ctr.ensure(1));
@@ -1038,10 +1049,7 @@ static int ensure_wave(pt_context* ctx, size_t results_needed) {
     ctx->W.ctr = ctx->d_ctr.p;
   }
   if (ctx->d_results.n < results_needed || !ctx->d_results.p) {
-    if (ctx->graph) {
-      cudaGraphExecDestroy(ctx->graph);
-      ctx->graph = nullptr;
-    }
+    drop_graphs(ctx);
     CK(ctx->d_results.ensure(results_needed));
   }
   ctx->W.results = ctx->d_results.p;
@@ -1072,7 +1080,7 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   bool counters = ctx->opt.enable_counters != 0;
   bool timing = ctx->opt.enable_timing != 0;
   if (timing && ctx->tev.empty()) {
-    ctx->tev.resize(6 * kItersPerGraph);
+    ctx->tev.resize(2 * 6 * kItersPerGraph);  // a set for each graph instance
     for (auto& e : ctx->tev) CK(cudaEventCreate(&e));
   }
   const bool guide = p->guide != 0;
@@ -1081,21 +1089,22 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   if (!ctx->graph || ctx->graph_counters != counters || ctx->graph_timing != timing ||
       ctx->graph_mode != p->mode || ctx->graph_guide != guide ||
       memcmp(&ctx->graph_W, &ctx->W, sizeof(WaveState)) != 0) {
-    if (ctx->graph) {
-      cudaGraphExecDestroy(ctx->graph);
-      ctx->graph = nullptr;
+    drop_graphs(ctx);
+    // with timing, a second instance records on its own events, so one
+    // launch can run while the host reads the other's times
+    for (int inst = 0; inst < (timing ? 2 : 1); inst++) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < kItersPerGraph; i++)
+        pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters, ctx->lc,
+                             st, timing ? &ctx->tev[6 * (kItersPerGraph * inst + i)] : nullptr,
+                             p->mode, nullptr, false, 0, guide ? &gi : nullptr);
+      cudaError_t ce = cudaStreamEndCapture(st, &g);
+      if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+      cudaError_t e = cudaGraphInstantiate(inst ? &ctx->graph2 : &ctx->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
     }
-    cudaGraph_t g;
-    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < kItersPerGraph; i++)
-      pt::launch_iteration(ctx->scene, ctx->W, ctx->d_ctl.p, ctx->max_stack, counters, ctx->lc,
-                           st, timing ? &ctx->tev[6 * i] : nullptr, p->mode, nullptr, false, 0,
-                           guide ? &gi : nullptr);
-    cudaError_t ce = cudaStreamEndCapture(st, &g);
-    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
-    cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
     ctx->graph_counters = counters;
     ctx->graph_timing = timing;
     ctx->graph_mode = p->mode;
@@ -1104,31 +1113,60 @@ static int run_chunk(pt_context* ctx, const pt_render_params* p, int frame0, int
   }
   // bounded host loop: a path needs at most max_depth iterations after its
   // generation, and every iteration generates at least one path while any
-  // remain, so this many iterations always suffice
+  // remain, so this many iterations always suffice.  The loop keeps one graph
+  // launch queued ahead of the one whose counters it reads (slot 0 / 1:
+  // counters, completion event and, with timing, graph instance and events),
+  // so the GPU does not wait for the host between launches; the launch queued
+  // after the chunk drained runs empty iterations.
   unsigned long long max_iters = ctl.chunk_paths + (unsigned long long)p->max_depth + 16;
   unsigned long long iters = 0;
-  while (true) {
-    CK(cudaGraphLaunch(ctx->graph, st));
+  auto launch = [&](int slot) -> cudaError_t {
+    cudaError_t e = cudaGraphLaunch(timing && slot ? ctx->graph2 : ctx->graph, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&ctx->h_ctr[slot], ctx->d_ctr.p, sizeof(WaveCounters),
+                          cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->evc[slot], st);
     ctx->stats.graph_launches++;
     iters += kItersPerGraph;
-    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr.p, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    return e;
+  };
+  auto harvest = [&](int slot) -> cudaError_t {
+    cudaError_t e = cudaEventSynchronize(ctx->evc[slot]);
     ctx->stats.iterations += kItersPerGraph;
     ctx->stats.kernel_launches += 7 * kItersPerGraph;
-    if (timing) {
+    if (timing && e == cudaSuccess) {
+      const cudaEvent_t* ev = &ctx->tev[6 * kItersPerGraph * slot];
       for (int i = 0; i < kItersPerGraph; i++)
         for (int k = 0; k < 5; k++) {
           float ms = 0.f;
-          if (cudaEventElapsedTime(&ms, ctx->tev[6 * i + k], ctx->tev[6 * i + k + 1]) ==
-              cudaSuccess)
+          if (cudaEventElapsedTime(&ms, ev[6 * i + k], ev[6 * i + k + 1]) == cudaSuccess)
             ctx->stats.stage_ms[k] += ms;
           else
             cudaGetLastError();  // a missing sample is not an error of the render
         }
     }
-    if (c.error) return fail(ctx, PT_EQUEUE, "traversal stack overflow");
-    if (c.next_path >= ctl.chunk_paths && c.n_cur == 0) break;
-    if (iters > max_iters) return fail(ctx, PT_ETIMEOUT, "wavefront did not drain");
+    return e;
+  };
+  CK(launch(0));
+  int cur = 0;  // the oldest launch in flight
+  while (true) {
+    CK(launch(cur ^ 1));
+    CK(harvest(cur));
+    const WaveCounters& cc = ctx->h_ctr[cur];
+    if (cc.error) {
+      CK(cudaStreamSynchronize(st));
+      return fail(ctx, PT_EQUEUE, "traversal stack overflow");
+    }
+    if (cc.next_path >= ctl.chunk_paths && cc.n_cur == 0) {
+      CK(harvest(cur ^ 1));
+      c = ctx->h_ctr[cur ^ 1];
+      break;
+    }
+    if (iters > max_iters) {
+      CK(cudaStreamSynchronize(st));
+      return fail(ctx, PT_ETIMEOUT, "wavefront did not drain");
+    }
+    cur ^= 1;
   }
   ctx->stats.paths += ctl.chunk_paths;
   ctx->stats.ext_rays += c.ext_rays;

@@ -48,9 +48,32 @@ struct DevBuf {
   }
 };
 
+// Page-locked host memory that grows on demand (staging of large uploads and
+// read-backs at commit, which then run at full copy-engine speed).
+template <typename T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost((void**)&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
 }  // namespace pth
 
 using pth::DevBuf;
+using pth::PinnedBuf;
 using pth::HostPrim;
 
 /* State of the learned sampling guide of a context. */
@@ -114,6 +137,9 @@ struct pt_context {
   DevBuf<float> d_normals, d_uvs;
   DevBuf<uint32_t> d_leaf_of_id;
   DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
+  PinnedBuf<float4> h_rec;  // their host staging
+  pt::BuildArena build_arena;  // GPU builder scratch, reused by every commit
+  PinnedBuf<uint32_t> h_check;  // read-back of a GPU-built BVH8 for the host's structural check
   DevBuf<float> d_env_marg, d_env_cond;  // environment sampling CDFs
   DevBuf<double> d_env_rows;
   DevBuf<double> d_env_pre;   // per texel: weights, then row prefix sums
@@ -136,9 +162,11 @@ struct pt_context {
   DevBuf<double> d_acc64;     // staging for host double accumulators
   DevBuf<float> d_tmp;
   DevBuf<uint32_t> d_tmpu;
-  WaveCounters* h_ctr = nullptr;  // pinned
+  WaveCounters* h_ctr = nullptr;  // pinned, 2 (the counters after each of two graph launches)
   WaveCtl* h_ctl = nullptr;       // pinned
   cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph2 = nullptr;  // a second instance on its own timing events (timing)
+  cudaEvent_t evc[2] = {nullptr, nullptr};  // the counters of a graph launch have arrived
   bool graph_counters = false;
   bool graph_timing = false;
   int graph_mode = 0;

@@ -138,6 +138,36 @@ PT_BVH_HD inline void moving_sphere_box(const float* f, float cam_t0, float cam_
   }
 }
 
+// Structural rules of node k of an nn-node BVH8 over n primitives: internal
+// children fill slots 0..r-1 with child index base + slot, each above k and
+// below nn, the internal-slot mask (bits 24-31 of word 3) is (1 << r) - 1,
+// and every leaf slot holds 1..3 primitive positions below n, each passed to
+// on_prim (which counts how often a position is covered).  Returns false on
+// the first broken rule.  The host validator and the GPU builder's check
+// both apply it.
+template <typename F>
+PT_BVH_HD inline bool check_node8(const uint32_t* w, uint64_t k, uint64_t nn, uint64_t n,
+                                  F&& on_prim) {
+  uint32_t rank = 0;
+  for (int i = 0; i < 8; i++) {
+    const uint32_t meta = ((i < 4 ? w[6] : w[7]) >> (8 * (i & 3))) & 0xffu;
+    if (!meta) continue;
+    if (meta & 0x80u) {
+      const uint64_t c = (uint64_t)w[4] + (meta & 7u);
+      if ((meta & 7u) != rank || (uint32_t)i != rank || c <= k || c >= nn) return false;
+      rank++;
+    } else {
+      const uint32_t cnt = meta >> 5, off = meta & 31u;
+      if (cnt < 1 || cnt > 3) return false;
+      for (uint32_t q = 0; q < cnt; q++) {
+        const uint64_t pi = (uint64_t)w[5] + off + q;
+        if (pi >= n || !on_prim(pi)) return false;
+      }
+    }
+  }
+  return (w[3] >> 24) == (1u << rank) - 1u;
+}
+
 inline void encode_node(const Box& parent, const WideChild* ch, int nch, uint32_t child_base,
                         uint32_t prim_base, uint32_t out[20]) {
   encode_node_dev(parent, ch, nch, child_base, prim_base, out);

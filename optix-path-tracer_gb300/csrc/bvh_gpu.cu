@@ -20,6 +20,9 @@
  *                   (or the requested width);
  *                   subtrees of <= 3 primitives become leaf slots; child
  *                   boxes are quantised to 8 bits (node format: pt_types.h)
+ *  7. k_check_*     structural check of the finished tree before any
+ *                   traversal runs on it (check_node8 on every node, every
+ *                   leaf position covered once, leaf_of_id a permutation)
  * The result is order independent for rendering (closest hit is the minimum
  * of (t, primitive id)), so the atomics that place nodes do not change images.
  */
@@ -592,6 +595,45 @@ struct Carve {
   }
 };
 
+// Structural check, per node: the rules of check_node8, counting in cover
+// how often each leaf position is referenced.
+__global__ void __launch_bounds__(256) k_check_nodes(const uint4* __restrict__ nodes,
+                                                     uint32_t nn, uint32_t n,
+                                                     uint32_t* __restrict__ cover,
+                                                     uint32_t* err) {
+  const uint32_t k = blockIdx.x * 256u + threadIdx.x;
+  if (k >= nn) return;
+  const uint4 a = nodes[5 * (size_t)k], b = nodes[5 * (size_t)k + 1];
+  const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};  // words 3..7 are read
+  const bool ok = pt::check_node8(w, k, nn, n, [cover](uint64_t pi) {
+    atomicAdd(&cover[pi], 1u);
+    return true;
+  });
+  if (!ok) atomicOr(err, 8u);
+}
+
+// Counts in ids how often each leaf position is some primitive's position.
+__global__ void __launch_bounds__(256) k_check_ids(const uint32_t* __restrict__ leaf_of_id,
+                                                   uint32_t n, uint32_t* __restrict__ ids,
+                                                   uint32_t* err) {
+  const uint32_t i = blockIdx.x * 256u + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t p = leaf_of_id[i];
+  if (p >= n)
+    atomicOr(err, 8u);
+  else
+    atomicAdd(&ids[p], 1u);
+}
+
+// Every leaf position must be covered by exactly one leaf slot and be the
+// position of exactly one primitive.
+__global__ void __launch_bounds__(256) k_check_cover(const uint32_t* __restrict__ cover,
+                                                     const uint32_t* __restrict__ ids, uint32_t n,
+                                                     uint32_t* err) {
+  const uint32_t i = blockIdx.x * 256u + threadIdx.x;
+  if (i < n && (cover[i] != 1u || ids[i] != 1u)) atomicOr(err, 8u);
+}
+
 }  // namespace
 
 namespace pt {
@@ -600,7 +642,8 @@ namespace pt {
 // d_nodes / d_rec_out / d_leaf_of_id (allocated by the caller: n nodes,
 // n records, n ids).  Returns the number of nodes and the depth (depth < 0:
 // the collapse met an inconsistent tree and stopped before overrunning a
-// buffer; -depth: 1 bad count, 2 capacity, 4 leaf gather mismatch).
+// buffer; -depth: 1 bad count, 2 capacity, 4 leaf gather mismatch; 8: the
+// finished tree broke a structural rule).
 cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t n,
                            uint4* d_nodes, float4* d_rec_out, uint32_t* d_leaf_of_id,
                            uint32_t* out_nodes, int* out_depth, int treelet_rounds, int width,
@@ -706,6 +749,21 @@ cudaError_t build_bvh8_gpu(const float4* d_rec, const float4* d_xforms, uint32_t
       uint2* tq = qa;
       qa = qb;
       qb = tq;
+    }
+    // structural check of the result (keys and vals are free by now)
+    if (!h_cnt[3] && n > 0) {
+      const uint32_t nn = h_cnt[0];
+      if (nn == 0 || nn > n) {
+        h_cnt[3] = 8;
+      } else {
+        BV(cudaMemsetAsync(keys, 0, (size_t)n * 4, st));
+        BV(cudaMemsetAsync(vals, 0, (size_t)n * 4, st));
+        k_check_nodes<<<(nn + 255) / 256, 256, 0, st>>>(d_nodes, nn, n, keys, counters + 3);
+        k_check_ids<<<g, 256, 0, st>>>(d_leaf_of_id, n, vals, counters + 3);
+        k_check_cover<<<g, 256, 0, st>>>(keys, vals, n, counters + 3);
+        BV(cudaMemcpyAsync(&h_cnt[3], counters + 3, 4, cudaMemcpyDeviceToHost, st));
+        BV(cudaStreamSynchronize(st));
+      }
     }
     BV(cudaGetLastError());
     *out_nodes = h_cnt[3] ? 0u : h_cnt[0];

@@ -255,28 +255,12 @@ bool validate_bvh8(const Bvh8Out& b, size_t num_prims) {
   if (num_prims == 0) return nn == 0 && b.leaf_order.empty();
   if (nn == 0 || b.leaf_order.size() != num_prims) return false;
   std::vector<uint8_t> seen(num_prims, 0);
-  for (size_t k = 0; k < nn; k++) {
-    const uint32_t* w = &b.nodes[k * 20];
-    uint32_t rank = 0;
-    for (int i = 0; i < 8; i++) {
-      uint32_t meta = ((i < 4 ? w[6] : w[7]) >> (8 * (i & 3))) & 0xffu;
-      if (!meta) continue;
-      if (meta & 0x80u) {
-        uint64_t c = (uint64_t)w[4] + (meta & 7u);
-        if ((meta & 7u) != rank || (uint32_t)i != rank || c <= k || c >= nn) return false;
-        rank++;
-      } else {
-        uint32_t cnt = meta >> 5, off = meta & 31u;
-        if (cnt < 1 || cnt > 3) return false;
-        for (uint32_t q = 0; q < cnt; q++) {
-          uint64_t pi = (uint64_t)w[5] + off + q;
-          if (pi >= num_prims || b.leaf_order[pi] >= num_prims) return false;
-          if (seen[b.leaf_order[pi]]++) return false;
-        }
-      }
-    }
-    if ((w[3] >> 24) != (1u << rank) - 1u) return false;  // internal children in slots 0..rank-1
-  }
+  auto cover = [&](uint64_t pi) {
+    const uint32_t id = b.leaf_order[pi];
+    return id < num_prims && seen[id]++ == 0;
+  };
+  for (size_t k = 0; k < nn; k++)
+    if (!check_node8(&b.nodes[k * 20], k, nn, num_prims, cover)) return false;
   for (uint8_t v : seen)
     if (v != 1) return false;
   return true;

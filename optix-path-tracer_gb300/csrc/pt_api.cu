@@ -128,8 +128,6 @@ int pth::device_ptr_kind(const void* p, int device) {
   return 0;
 }
 
-// World-space AABB of a primitive, padded so that rounding in the primitive
-// tests can never place a reported hit outside its box.
 // Forgets the captured wavefront graphs (a new scene, buffers or options).
 static void drop_graphs(pt_context* ctx) {
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
@@ -137,6 +135,20 @@ static void drop_graphs(pt_context* ctx) {
   ctx->graph = ctx->graph2 = nullptr;
 }
 
+// Uploads a host table, or `zeros` zeroed elements when it is empty (the
+// scene's device pointers are never null).
+template <typename T>
+static cudaError_t upload_or_zero(DevBuf<T>& d, const std::vector<T>& v, size_t zeros,
+                                  cudaStream_t st) {
+  if (!v.empty()) return d.upload(v.data(), v.size(), st);
+  const std::vector<T> z(zeros);
+  cudaError_t e = d.upload(z.data(), z.size(), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // z is a local
+  return e;
+}
+
+// World-space AABB of a primitive, padded so that rounding in the primitive
+// tests can never place a reported hit outside its box.
 static pt::Box prim_box(const pt_context* ctx, const HostPrim& p) {
   float lo[3], hi[3];
   const float* f = p.f;
@@ -217,6 +229,7 @@ PT_API int pt_context_create(const pt_options* opt, pt_context** out) {
   ctx->device = opt ? opt->device : 0;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_ctr, 2 * sizeof(WaveCounters));
@@ -253,7 +266,6 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   ctx->d_leaf_of_id.release();
   ctx->d_rec_in.release();
   ctx->h_rec.release();
-  ctx->h_check.release();
   if (ctx->build_arena.p) cudaFree(ctx->build_arena.p);
   ctx->build_arena = pt::BuildArena{};
   ctx->d_env_marg.release();
@@ -294,6 +306,7 @@ PT_API int pt_context_destroy(pt_context* ctx) {
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
   delete ctx;
   return PT_OK;
 }
@@ -541,6 +554,8 @@ static int push_prim(pt_context* ctx, HostPrim& p, const float* xform, uint32_t*
   p.xform = add_xform(ctx, xform);
   ctx->prims.push_back(p);
   ctx->tri_attr.push_back(make_uint4(0, 0, 0, 0));
+  if (p.type != PT_PRIM_TRIANGLE) ctx->num_non_triangles++;
+  if (p.moving) ctx->num_moving++;
   ctx->committed = false;
   if (prim_id) *prim_id = (uint32_t)ctx->prims.size() - 1;
   return PT_OK;
@@ -862,24 +877,9 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
                           ctx->cam.time0, ctx->cam.time1, &ctx->build_arena, st));
     if (depth < 0)
       return fail(ctx, PT_EINVAL,
-                  "GPU BVH8 failed validation (collapse check " + std::to_string(-depth) + ")");
+                  "GPU BVH8 failed validation (check " + std::to_string(-depth) + ")");
     nn = nodes;
-    bvh.depth = depth;
-    // host-side structural check before any traversal runs on it (nodes and
-    // leaf positions read back through page-locked staging)
-    const size_t nw = (size_t)nodes * 20;
-    CK(ctx->h_check.ensure(nw + n));
-    CK(cudaMemcpyAsync(ctx->h_check.p, d_nodes.p, nw * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(ctx->h_check.p + nw, d_leaf_of_id.p, n * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    bvh.nodes.assign(ctx->h_check.p, ctx->h_check.p + nw);
-    const uint32_t* loid = ctx->h_check.p + nw;
-    bvh.leaf_order.assign(n, 0xffffffffu);
-    for (size_t i = 0; i < n; i++) {
-      if (loid[i] >= n) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
-      bvh.leaf_order[loid[i]] = (uint32_t)i;
-    }
-    if (!pt::validate_bvh8(bvh, n)) return fail(ctx, PT_EINVAL, "GPU BVH8 failed validation");
+    bvh.depth = depth;  // the builder checked the tree's structure on the device
   } else {
     std::vector<pt::Box> boxes(n);
     for (size_t i = 0; i < n; i++) boxes[i] = prim_box(ctx, ctx->prims[i]);
@@ -906,6 +906,44 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
 
 extern "C" {
 
+// Uploads the scene's tables (materials, lights, textures, triangle
+// attributes, the environment) on the context's second stream and builds the
+// importance-sampling tables of a spherical HDR environment; returns when
+// they are on the device.  Runs on its own host thread during the BVH build.
+static cudaError_t upload_tables(pt_context* ctx) {
+  cudaStream_t st = ctx->aux_stream;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_mats, ctx->mats, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_lights, ctx->lights, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_textures, ctx->textures, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tex_data, ctx->tex_data, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tex_list, ctx->tex_list, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tri_attr, ctx->tri_attr, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_normals, ctx->normals, 3, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_uvs, ctx->uvs, 2, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_env, ctx->env, 1, st);
+  ctx->env_valid = 0;
+  if (e == cudaSuccess && ctx->miss.type == PT_MISS_HDR && ctx->miss.spherical &&
+      !ctx->env.empty()) {
+    const int w = ctx->miss.w, h = ctx->miss.h;
+    e = ctx->d_env_marg.ensure((size_t)h + 1);
+    if (e == cudaSuccess) e = ctx->d_env_cond.ensure((size_t)h * (w + 1));
+    if (e == cudaSuccess) e = ctx->d_env_rows.ensure((size_t)h);
+    if (e == cudaSuccess) e = ctx->d_env_pre.ensure((size_t)w * h);
+    if (e == cudaSuccess) e = ctx->d_env_valid.ensure(1);
+    if (e == cudaSuccess) {
+      pt::launch_env_cdf(ctx->d_env.p, w, h, ctx->d_env_marg.p, ctx->d_env_cond.p,
+                         ctx->d_env_rows.p, ctx->d_env_pre.p, ctx->d_env_valid.p, st);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&ctx->env_valid, ctx->d_env_valid.p, sizeof(int),
+                          cudaMemcpyDeviceToHost, st);
+  }
+  cudaError_t s = cudaStreamSynchronize(st);
+  return e != cudaSuccess ? e : s;
+}
+
 PT_API int pt_commit(pt_context* ctx) {
   if (!ctx) return PT_EINVAL;
   CK(cudaSetDevice(ctx->device));
@@ -919,49 +957,19 @@ PT_API int pt_commit(pt_context* ctx) {
   size_t nn = 0;
   int depth = 0;
   int width = ctx->opt.bvh_width ? ctx->opt.bvh_width : 8;
-  int rc = build_bvh(ctx, width, ctx->d_nodes, ctx->d_prims, ctx->d_leaf_of_id, &nn, &depth);
-  if (rc) return rc;
-  std::vector<GpuMaterial> mats = ctx->mats;
-  if (mats.empty()) mats.resize(1);
-  CK(ctx->d_mats.upload(mats.data(), mats.size(), st));
-  std::vector<GpuLight> lights = ctx->lights;
-  if (lights.empty()) lights.resize(1);
-  CK(ctx->d_lights.upload(lights.data(), lights.size(), st));
-  std::vector<GpuTexture> texs = ctx->textures;
-  if (texs.empty()) texs.resize(1);
-  std::vector<float4> tdata = ctx->tex_data;
-  if (tdata.empty()) tdata.resize(1);
-  std::vector<int> tlist = ctx->tex_list;
-  if (tlist.empty()) tlist.resize(1);
-  CK(ctx->d_textures.upload(texs.data(), texs.size(), st));
-  CK(ctx->d_tex_data.upload(tdata.data(), tdata.size(), st));
-  CK(ctx->d_tex_list.upload(tlist.data(), tlist.size(), st));
-  std::vector<uint4> ta = ctx->tri_attr;
-  if (ta.empty()) ta.resize(1);
-  CK(ctx->d_tri_attr.upload(ta.data(), ta.size(), st));
-  std::vector<float> nrm = ctx->normals, uv = ctx->uvs;
-  if (nrm.empty()) nrm.resize(3);
-  if (uv.empty()) uv.resize(2);
-  CK(ctx->d_normals.upload(nrm.data(), nrm.size(), st));
-  CK(ctx->d_uvs.upload(uv.data(), uv.size(), st));
-  std::vector<float4> env = ctx->env;
-  if (env.empty()) env.resize(1);
-  CK(ctx->d_env.upload(env.data(), env.size(), st));
-  // importance-sampling tables of a spherical HDR environment
-  ctx->env_valid = 0;
-  if (ctx->miss.type == PT_MISS_HDR && ctx->miss.spherical && !ctx->env.empty()) {
-    int w = ctx->miss.w, h = ctx->miss.h;
-    CK(ctx->d_env_marg.ensure((size_t)h + 1));
-    CK(ctx->d_env_cond.ensure((size_t)h * (w + 1)));
-    CK(ctx->d_env_rows.ensure((size_t)h));
-    CK(ctx->d_env_pre.ensure((size_t)w * h));
-    CK(ctx->d_env_valid.ensure(1));
-    pt::launch_env_cdf(ctx->d_env.p, w, h, ctx->d_env_marg.p, ctx->d_env_cond.p,
-                       ctx->d_env_rows.p, ctx->d_env_pre.p, ctx->d_env_valid.p, st);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(&ctx->env_valid, ctx->d_env_valid.p, sizeof(int), cudaMemcpyDeviceToHost,
-                       st));
+  // the scene's tables go up from a helper thread on the second stream while
+  // this thread builds the BVH
+  cudaError_t te = cudaSuccess;
+  std::thread tables;
+  try {
+    tables = std::thread([ctx, &te] { te = upload_tables(ctx); });
+  } catch (...) {
+    te = upload_tables(ctx);
   }
+  int rc = build_bvh(ctx, width, ctx->d_nodes, ctx->d_prims, ctx->d_leaf_of_id, &nn, &depth);
+  if (tables.joinable()) tables.join();
+  if (rc) return rc;
+  if (te != cudaSuccess) return cuda_fail(ctx, te, "scene table upload");
   CK(cudaStreamSynchronize(st));
   DevScene& S = ctx->scene;
   memset(&S, 0, sizeof(S));
@@ -1191,17 +1199,9 @@ static void reset_render_stats(pt_context* ctx) {
 // the whole warp; rays through a small scene are short and alike.  (GB300,
 // 1080p: 2.1M-triangle heightfield 24 lanes +6% over 32; 488 spheres 32
 // lanes +1% over 24.)
-bool pth::has_motion(const pt_context* ctx) {
-  for (const HostPrim& p : ctx->prims)
-    if (p.moving) return true;
-  return false;
-}
+bool pth::has_motion(const pt_context* ctx) { return ctx->num_moving > 0; }
 
-bool pth::all_triangles(const pt_context* ctx) {
-  for (const HostPrim& p : ctx->prims)
-    if (p.type != PT_PRIM_TRIANGLE) return false;
-  return true;
-}
+bool pth::all_triangles(const pt_context* ctx) { return ctx->num_non_triangles == 0; }
 
 int pth::auto_refetch(size_t num_prims) { return num_prims > ((size_t)1 << 16) ? 24 : 32; }
 

@@ -110,10 +110,13 @@ struct pt_context {
   std::string err;
   pt_options opt{};
   cudaStream_t stream = nullptr;
+  cudaStream_t aux_stream = nullptr;  // scene table uploads during the BVH build
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // ---- host scene
   std::vector<GpuMaterial> mats;
   std::vector<HostPrim> prims;
+  size_t num_non_triangles = 0;  // primitives that are not triangles
+  size_t num_moving = 0;         // moving spheres
   std::vector<float> xforms;  // 24 floats each: m rows, inv rows (float4-padded 3x4)
   std::vector<uint4> tri_attr;
   std::vector<float> normals, uvs;
@@ -139,7 +142,6 @@ struct pt_context {
   DevBuf<float4> d_rec_in;  // primitive records in call order (GPU builder input)
   PinnedBuf<float4> h_rec;  // their host staging
   pt::BuildArena build_arena;  // GPU builder scratch, reused by every commit
-  PinnedBuf<uint32_t> h_check;  // read-back of a GPU-built BVH8 for the host's structural check
   DevBuf<float> d_env_marg, d_env_cond;  // environment sampling CDFs
   DevBuf<double> d_env_rows;
   DevBuf<double> d_env_pre;   // per texel: weights, then row prefix sums

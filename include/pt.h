@@ -105,6 +105,7 @@ typedef struct pt_stats {
   uint64_t graph_launches; /* CUDA-graph launches of the last render */
   uint64_t guide_samples;  /* training samples of each Adam step after the last guided
                               frame (0 without the guide) */
+  uint64_t upload_bytes;   /* bytes copied host to device by the last pt_commit */
 } pt_stats;
 
 /* ---- context (replaces optix::Context, host_includes/host_common.hpp:21-45) */

@@ -137,9 +137,11 @@ static void drop_graphs(pt_context* ctx) {
 
 // Uploads a host table, or `zeros` zeroed elements when it is empty (the
 // scene's device pointers are never null).
+// Adds the bytes copied to *bytes.
 template <typename T>
 static cudaError_t upload_or_zero(DevBuf<T>& d, const std::vector<T>& v, size_t zeros,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, size_t* bytes) {
+  *bytes += (v.empty() ? zeros : v.size()) * sizeof(T);
   if (!v.empty()) return d.upload(v.data(), v.size(), st);
   const std::vector<T> z(zeros);
   cudaError_t e = d.upload(z.data(), z.size(), st);
@@ -843,7 +845,9 @@ static void prim_record(const HostPrim& p, uint32_t id, float4* out) {
 // device) into nodes / leaf-ordered records / leaf_of_id, with at most
 // `width` children per node, and checks its structure on the host.
 int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<float4>& d_prims,
-                   DevBuf<uint32_t>& d_leaf_of_id, size_t* out_nodes, int* out_depth) {
+                   DevBuf<uint32_t>& d_leaf_of_id, size_t* out_nodes, int* out_depth,
+                   size_t* uploaded) {
+  size_t up = 0;
   cudaStream_t st = ctx->stream;
   size_t n = ctx->prims.size();
   int builder = ctx->opt.bvh_builder;
@@ -867,6 +871,7 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
       for (std::thread& th : pool) th.join();
     }
     CK(ctx->d_rec_in.upload(ctx->h_rec.p, 3 * n, st));
+    up += 3 * n * sizeof(float4);
     CK(d_nodes.ensure(5 * std::max<size_t>(1, n)));
     CK(d_prims.ensure(3 * n));
     CK(d_leaf_of_id.ensure(n));
@@ -897,8 +902,10 @@ int pth::build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<fl
     std::vector<uint32_t> leaf_of_id(n ? n : 1, 0);
     for (size_t k = 0; k < bvh.leaf_order.size(); k++) leaf_of_id[bvh.leaf_order[k]] = (uint32_t)k;
     CK(d_leaf_of_id.upload(leaf_of_id.data(), leaf_of_id.size(), st));
+    up += nodes.size() * sizeof(uint4) + rec.size() * sizeof(float4) + leaf_of_id.size() * 4;
   }
   CK(cudaStreamSynchronize(st));
+  if (uploaded) *uploaded = up;
   *out_nodes = nn;
   *out_depth = bvh.depth;
   return PT_OK;
@@ -909,19 +916,20 @@ extern "C" {
 // Uploads the scene's tables (materials, lights, textures, triangle
 // attributes, the environment) on the context's second stream and builds the
 // importance-sampling tables of a spherical HDR environment; returns when
-// they are on the device.  Runs on its own host thread during the BVH build.
-static cudaError_t upload_tables(pt_context* ctx) {
+// they are on the device (*bytes: the bytes copied host to device).  Runs on
+// its own host thread during the BVH build.
+static cudaError_t upload_tables(pt_context* ctx, size_t* bytes) {
   cudaStream_t st = ctx->aux_stream;
   cudaError_t e = cudaSetDevice(ctx->device);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_mats, ctx->mats, 1, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_lights, ctx->lights, 1, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_textures, ctx->textures, 1, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tex_data, ctx->tex_data, 1, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tex_list, ctx->tex_list, 1, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tri_attr, ctx->tri_attr, 1, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_normals, ctx->normals, 3, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_uvs, ctx->uvs, 2, st);
-  if (e == cudaSuccess) e = upload_or_zero(ctx->d_env, ctx->env, 1, st);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_mats, ctx->mats, 1, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_lights, ctx->lights, 1, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_textures, ctx->textures, 1, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tex_data, ctx->tex_data, 1, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tex_list, ctx->tex_list, 1, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_tri_attr, ctx->tri_attr, 1, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_normals, ctx->normals, 3, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_uvs, ctx->uvs, 2, st, bytes);
+  if (e == cudaSuccess) e = upload_or_zero(ctx->d_env, ctx->env, 1, st, bytes);
   ctx->env_valid = 0;
   if (e == cudaSuccess && ctx->miss.type == PT_MISS_HDR && ctx->miss.spherical &&
       !ctx->env.empty()) {
@@ -960,13 +968,16 @@ PT_API int pt_commit(pt_context* ctx) {
   // the scene's tables go up from a helper thread on the second stream while
   // this thread builds the BVH
   cudaError_t te = cudaSuccess;
+  size_t table_up = 0;
   std::thread tables;
   try {
-    tables = std::thread([ctx, &te] { te = upload_tables(ctx); });
+    tables = std::thread([ctx, &te, &table_up] { te = upload_tables(ctx, &table_up); });
   } catch (...) {
-    te = upload_tables(ctx);
+    te = upload_tables(ctx, &table_up);
   }
-  int rc = build_bvh(ctx, width, ctx->d_nodes, ctx->d_prims, ctx->d_leaf_of_id, &nn, &depth);
+  size_t bvh_up = 0;
+  int rc = build_bvh(ctx, width, ctx->d_nodes, ctx->d_prims, ctx->d_leaf_of_id, &nn, &depth,
+                     &bvh_up);
   if (tables.joinable()) tables.join();
   if (rc) return rc;
   if (te != cudaSuccess) return cuda_fail(ctx, te, "scene table upload");
@@ -1012,6 +1023,7 @@ PT_API int pt_commit(pt_context* ctx) {
   ctx->stats.bvh_nodes = nn;
   ctx->stats.bvh_bytes = nn * 80 + n * 48;
   ctx->stats.bvh_depth = depth;
+  ctx->stats.upload_bytes = xf.size() * sizeof(float4) + bvh_up + table_up;
   ctx->commit_gen++;
   ctx->committed = true;
   return PT_OK;

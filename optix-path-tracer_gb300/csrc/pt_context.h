@@ -184,9 +184,11 @@ struct pt_context {
 
 namespace pth {
 /* Builds the scene's BVH (at most `width` children per node) into the given
- * buffers; returns a PT_ status. */
+ * buffers; returns a PT_ status.  *uploaded (if given) receives the bytes
+ * copied host to device. */
 int build_bvh(pt_context* ctx, int width, DevBuf<uint4>& d_nodes, DevBuf<float4>& d_prims,
-              DevBuf<uint32_t>& d_leaf_of_id, size_t* out_nodes, int* out_depth);
+              DevBuf<uint32_t>& d_leaf_of_id, size_t* out_nodes, int* out_depth,
+              size_t* uploaded = nullptr);
 /* Carves the wavefront arrays of `slots` paths out of one float4 block
  * (PT_SLOT_F4 per slot) and one uint4 block (PT_SLOT_U4 per slot). */
 void carve_wave(WaveState& W, float4* f, uint4* u, size_t slots);

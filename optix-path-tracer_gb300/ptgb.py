@@ -58,7 +58,7 @@ class Stats(ctypes.Structure):
                 ("build_ms", ctypes.c_double), ("render_ms", ctypes.c_double),
                 ("iterations", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("stage_ms", ctypes.c_double * 5), ("graph_launches", ctypes.c_uint64),
-                ("guide_samples", ctypes.c_uint64)]
+                ("guide_samples", ctypes.c_uint64), ("upload_bytes", ctypes.c_uint64)]
 
 
 class BatchItem(ctypes.Structure):

@@ -177,6 +177,11 @@ def test_gpu_builder_large_mesh(ptgb_mod):
     st = g.stats()
     assert st["bvh_depth"] <= 24
     assert 2 * 1024 * 1024 // 24 < st["bvh_nodes"] < 2 * 1024 * 1024
+    # host-to-device bytes of the commit: 48-byte records and 16-byte
+    # attributes per triangle, per-vertex normals and uvs, the environment
+    n, nv = 2 * 1024 * 1024, 1025 * 1025
+    least = 64 * n + 20 * nv + 64 * 32 * 16
+    assert least <= st["upload_bytes"] < least + (1 << 20)
     acc = g.render(ptgb_mod.GpuRenderer.params(64, 36, 2))
     assert np.isfinite(acc).all() and np.all(acc[..., 3] == 2)
     g.close()

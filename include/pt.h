@@ -63,7 +63,8 @@ typedef struct pt_context pt_context;
 
 typedef struct pt_options {
   int device;          /* CUDA device ordinal */
-  int path_slots;      /* wavefront path-state slots; 0 = automatic */
+  int path_slots;      /* wavefront path-state slots; 0 = automatic (a render's
+                          paths per chunk rounded up to 64 Ki, at most 8 Mi) */
   int enable_counters; /* count BVH node fetches and primitive tests */
   int enable_timing;   /* per-stage device times (CUDA events in the graph) */
   int bvh_builder;     /* 0 automatic, 1 host (binned SAH), 2 GPU (LBVH + treelets) */

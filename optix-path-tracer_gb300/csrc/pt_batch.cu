@@ -805,7 +805,7 @@ PT_API int pt_batch_autotune(pt_batch* b, const pt_batch_item* items, int n, pt_
     }
     return PT_OK;
   };
-  const int slot_opts[] = {1 << 19, 1 << 20, 1 << 21, 1 << 22};
+  const int slot_opts[] = {1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23};
   const int tb_opts[] = {64, 128, 256};
   const int sb_opts[] = {128, 256};
   const int w_opts[] = {8, 4};

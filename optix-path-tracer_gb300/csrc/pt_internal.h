@@ -19,6 +19,15 @@
 #ifndef PT_SHADE_MINBLOCKS
 #define PT_SHADE_MINBLOCKS 4     /* of 256 threads: <= 64 registers, 1024 resident threads per SM */
 #endif
+/* consistent-mode shading: more resident blocks of fewer registers (the
+ * spills go to L1) hide more of its dependent loads: 7 blocks of 256 (<= 36
+ * registers) gave 1150 -> 1210 M paths/s on the 2.1 M-triangle heightfield
+ * (5: 1167, 6: 1182, 8: 1210); reference-mode shading (k_shade) is faster
+ * at 4 (5 blocks: 10 % slower on random spheres), and guided shading keeps
+ * PT_SHADE_MINBLOCKS (the setting its equal-time study was measured with) */
+#ifndef PT_SHADE_C_MINBLOCKS
+#define PT_SHADE_C_MINBLOCKS 7
+#endif
 
 /* Path state word st.z: depth (bits 0-15), previous bounce specular (bit 16),
  * scene of a batch (bits 17-31). */

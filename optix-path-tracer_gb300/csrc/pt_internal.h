@@ -23,10 +23,13 @@
  * spills go to L1) hide more of its dependent loads: 7 blocks of 256 (<= 36
  * registers) gave 1150 -> 1210 M paths/s on the 2.1 M-triangle heightfield
  * (5: 1167, 6: 1182, 8: 1210); reference-mode shading (k_shade) is faster
- * at 4 (5 blocks: 10 % slower on random spheres), and guided shading keeps
- * PT_SHADE_MINBLOCKS (the setting its equal-time study was measured with) */
+ * at 4 (5 blocks: 10 % slower on random spheres), and so is guided shading
+ * (7 blocks: 256 guided frames of the lit box 3 % slower) */
 #ifndef PT_SHADE_C_MINBLOCKS
 #define PT_SHADE_C_MINBLOCKS 7
+#endif
+#ifndef PT_SHADE_G_MINBLOCKS
+#define PT_SHADE_G_MINBLOCKS PT_SHADE_MINBLOCKS
 #endif
 
 /* Path state word st.z: depth (bits 0-15), previous bounce specular (bit 16),

@@ -881,7 +881,7 @@ __device__ __forceinline__ void shade_c_path(const DevScene& S0, const WaveState
 }
 
 template <bool BATCH, bool SORT, bool GUIDE, bool TEX>
-__global__ void __launch_bounds__(PT_SHADE_BLOCK, GUIDE ? PT_SHADE_MINBLOCKS : PT_SHADE_C_MINBLOCKS) k_shade_c(DevScene S0, WaveState W,
+__global__ void __launch_bounds__(PT_SHADE_BLOCK, GUIDE ? PT_SHADE_G_MINBLOCKS : PT_SHADE_C_MINBLOCKS) k_shade_c(DevScene S0, WaveState W,
                                                             const WaveCtl* __restrict__ ctlp,
                                                             BatchRefs br) {
   __shared__ SortTile tile;

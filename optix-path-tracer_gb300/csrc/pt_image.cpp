@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <new>
 #include <string>
 #include <vector>
 
@@ -266,6 +267,11 @@ int load_png(const std::vector<uint8_t>& f, int* W, int* H, std::vector<float>* 
   if (!(depth == 8 || (depth == 16 && ctype != 3)))
     return img_fail(PT_EINVAL, "PNG bit depth " + std::to_string(depth) + " is not supported");
   if (ctype == 3 && plte.size() < 3) return img_fail(PT_EINVAL, "PNG palette missing");
+  const size_t bpp = (size_t)chans * (depth / 8), row = (size_t)w * bpp;
+  // deflate expands its input at most 1032-fold: a header whose image cannot
+  // come out of the data it carries is refused before anything is sized by it
+  if ((row + 1) * h > idat.size() * 1032 + 1024)
+    return img_fail(PT_EINVAL, "PNG data too short for its size");
   *W = (int)w;
   *H = (int)h;
   if (!rgba) return PT_OK;
@@ -273,7 +279,6 @@ int load_png(const std::vector<uint8_t>& f, int* W, int* H, std::vector<float>* 
   if (idat.size() < 6 || (idat[0] & 15) != 8 || ((idat[0] << 8) | idat[1]) % 31 != 0 ||
       (idat[1] & 0x20))
     return img_fail(PT_EINVAL, "bad zlib stream in PNG");
-  const size_t bpp = (size_t)chans * (depth / 8), row = (size_t)w * bpp;
   std::vector<uint8_t> raw;
   raw.reserve((row + 1) * h);
   Inflater inf(idat.data() + 2, idat.size() - 2, raw);
@@ -347,23 +352,29 @@ int load_ppm(const std::vector<uint8_t>& f, int* W, int* H, std::vector<float>* 
     }
     if (p >= f.size() || !isdigit(f[p])) return false;
     v = 0;
-    while (p < f.size() && isdigit(f[p])) v = v * 10 + (f[p++] - '0');
+    while (p < f.size() && isdigit(f[p])) {
+      if (v > 100000000) return false;  // larger than any valid size or sample
+      v = v * 10 + (f[p++] - '0');
+    }
     return true;
   };
   long w, h, mx;
   if (!token(w) || !token(h) || !token(mx) || w <= 0 || h <= 0 || w > 32768 || h > 32768 ||
       mx <= 0 || mx > 65535)
     return img_fail(PT_EINVAL, "bad PPM header");
+  const bool binary = f[1] == '6';
+  const size_t n = (size_t)w * h;
+  const size_t bs = mx > 255 ? 2 : 1;
+  // the samples must fit in the file (binary ones exactly, text ones one
+  // digit and one separator each at the least) before the size is reported
+  if (binary ? p + 1 + n * 3 * bs > f.size() : 2 * 3 * n > f.size() - p + 1)
+    return img_fail(PT_EINVAL, "truncated PPM data");
   *W = (int)w;
   *H = (int)h;
   if (!rgba) return PT_OK;
-  const bool binary = f[1] == '6';
-  const size_t n = (size_t)w * h;
   rgba->assign(n * 4, 1.f);
   if (binary) {
     p++;  // the single whitespace after maxval
-    const size_t bs = mx > 255 ? 2 : 1;
-    if (p + n * 3 * bs > f.size()) return img_fail(PT_EINVAL, "truncated PPM data");
     for (size_t i = 0; i < 3 * n; i++) {
       long v = bs == 2 ? ((f[p + 2 * i] << 8) | f[p + 2 * i + 1]) : f[p + i];
       (*rgba)[4 * (i / 3) + i % 3] = (float)v / (float)mx;
@@ -384,7 +395,7 @@ extern "C" {
 
 // Any supported image: w x h, RGBA floats, first file row first.  rgba NULL
 // returns the size only.
-PT_API int pt_image_load(const char* path, int* w, int* h, float* rgba) {
+static int image_load_body(const char* path, int* w, int* h, float* rgba) {
   if (!path || !w || !h) return img_fail(PT_EINVAL, "null argument");
   std::vector<uint8_t> f;
   if (!read_all(path, f)) return img_fail(PT_EINVAL, std::string("cannot read ") + path);
@@ -409,6 +420,16 @@ PT_API int pt_image_load(const char* path, int* w, int* h, float* rgba) {
     return img_fail(PT_EINVAL, std::string(path) + ": JPEG images are not decoded (PNG, PPM, "
                                                   "Radiance HDR are)");
   return img_fail(PT_EINVAL, std::string(path) + ": unknown image format");
+}
+
+// Host memory running out while reading an untrusted file (a header can
+// claim sizes its data cannot hold) is an error of the call, not an abort.
+PT_API int pt_image_load(const char* path, int* w, int* h, float* rgba) {
+  try {
+    return image_load_body(path, w, h, rgba);
+  } catch (const std::bad_alloc&) {
+    return img_fail(PT_ENOMEM, "out of host memory reading the image");
+  }
 }
 
 PT_API const char* pt_image_last_error(void) { return g_img_err.c_str(); }

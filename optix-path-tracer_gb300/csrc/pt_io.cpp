@@ -14,6 +14,8 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -255,7 +257,7 @@ extern "C" {
 
 PT_API const char* pt_io_last_error(void) { return g_io_err.c_str(); }
 
-PT_API int pt_obj_load(const char* path, pt_obj** out) {
+static int obj_load_body(const char* path, pt_obj** out) {
   if (!path || !out) return io_fail(PT_EINVAL, "null argument");
   *out = nullptr;
   std::string text;
@@ -309,7 +311,7 @@ PT_API int pt_obj_load(const char* path, pt_obj** out) {
           return io_fail(PT_EINVAL, "cannot read material library " + t[i]);
     }
   }
-  pt_obj* m = new (std::nothrow) pt_obj();
+  std::unique_ptr<pt_obj> m(new (std::nothrow) pt_obj());
   if (!m) return io_fail(PT_ENOMEM, "out of host memory");
   const size_t nc = tris.size();
   bool all_n = nc > 0, all_t = nc > 0;
@@ -335,8 +337,18 @@ PT_API int pt_obj_load(const char* path, pt_obj** out) {
     m->mat[i] = tri_mat[i] < 0 ? PT_OBJ_NO_MATERIAL : (uint32_t)tri_mat[i];
   m->mats = std::move(mats);
   m->dir = dir_of(path);
-  *out = m;
+  *out = m.release();
   return PT_OK;
+}
+
+// Host memory running out while reading an untrusted file (a header can
+// claim sizes its data cannot hold) is an error of the call, not an abort.
+PT_API int pt_obj_load(const char* path, pt_obj** out) {
+  try {
+    return obj_load_body(path, out);
+  } catch (const std::bad_alloc&) {
+    return io_fail(PT_ENOMEM, "out of host memory reading the OBJ file");
+  }
 }
 
 PT_API int pt_obj_free(pt_obj* m) {
@@ -357,16 +369,18 @@ PT_API int pt_obj_info(const pt_obj* m, size_t* n_tris, size_t* n_materials, int
 PT_API int pt_obj_get(const pt_obj* m, float* verts, float* normals, float* uvs,
                       uint32_t* mat_per_tri) {
   if (!m) return io_fail(PT_EINVAL, "null mesh");
-  if (verts) memcpy(verts, m->pos.data(), m->pos.size() * sizeof(float));
+  // (a mesh without faces has empty arrays: nothing is copied)
+  if (verts && !m->pos.empty()) memcpy(verts, m->pos.data(), m->pos.size() * sizeof(float));
   if (normals) {
     if (!m->has_nrm) return io_fail(PT_EINVAL, "the mesh has no normals on every corner");
-    memcpy(normals, m->nrm.data(), m->nrm.size() * sizeof(float));
+    if (!m->nrm.empty()) memcpy(normals, m->nrm.data(), m->nrm.size() * sizeof(float));
   }
   if (uvs) {
     if (!m->has_uv) return io_fail(PT_EINVAL, "the mesh has no texture coordinates on every corner");
-    memcpy(uvs, m->uv.data(), m->uv.size() * sizeof(float));
+    if (!m->uv.empty()) memcpy(uvs, m->uv.data(), m->uv.size() * sizeof(float));
   }
-  if (mat_per_tri) memcpy(mat_per_tri, m->mat.data(), m->mat.size() * sizeof(uint32_t));
+  if (mat_per_tri && !m->mat.empty())
+    memcpy(mat_per_tri, m->mat.data(), m->mat.size() * sizeof(uint32_t));
   return PT_OK;
 }
 
@@ -446,7 +460,7 @@ PT_API int pt_add_obj(pt_context* ctx, const pt_obj* m, uint32_t material, const
 // length encoded (the 2 2 hi lo scanline form, and the older repeat-pixel
 // form).  A pixel (r, g, b, e) is (r, g, b) / 256 * 2^(e - 128), first
 // scanline first, as the reference's loader stores it.
-PT_API int pt_hdr_load(const char* path, int* w, int* h, float* rgba) {
+static int hdr_load_body(const char* path, int* w, int* h, float* rgba) {
   if (!path || !w || !h) return io_fail(PT_EINVAL, "null argument");
   std::string s;
   if (!read_file(path, s)) return io_fail(PT_EINVAL, std::string("cannot read ") + path);
@@ -461,6 +475,10 @@ PT_API int pt_hdr_load(const char* path, int* w, int* h, float* rgba) {
   if (sscanf(s.substr(p, e - p).c_str(), "-Y %ld +X %ld", &H, &W) != 2 || H <= 0 || W <= 0 ||
       H > 65536 || W > 65536)
     return io_fail(PT_EINVAL, "unsupported resolution line (expected -Y h +X w)");
+  // at most 2^28 pixels (4 GiB of float texels), and at least one 4-byte
+  // pixel of data per scanline, before the size is reported
+  if ((uint64_t)W * (uint64_t)H > ((uint64_t)1 << 28)) return io_fail(PT_EINVAL, "HDR image too large");
+  if ((size_t)H * 4 > s.size() - (e + 1)) return io_fail(PT_EINVAL, "truncated HDR data");
   *w = (int)W;
   *h = (int)H;
   if (!rgba) return PT_OK;
@@ -521,6 +539,16 @@ PT_API int pt_hdr_load(const char* path, int* w, int* h, float* rgba) {
     }
   }
   return PT_OK;
+}
+
+// Host memory running out while reading an untrusted file (a header can
+// claim sizes its data cannot hold) is an error of the call, not an abort.
+PT_API int pt_hdr_load(const char* path, int* w, int* h, float* rgba) {
+  try {
+    return hdr_load_body(path, w, h, rgba);
+  } catch (const std::bad_alloc&) {
+    return io_fail(PT_ENOMEM, "out of host memory reading the HDR file");
+  }
 }
 
 // Save_HDR (image_save.hpp:40-73): the average over spp, Reinhard's c/(1+c)

@@ -1,5 +1,5 @@
 // Malformed-file driver for the host file readers (pt_image_load: PNG, PPM,
-// Radiance HDR; pt_hdr_load; pt_obj_load with its MTL): every seed file is
+// Radiance HDR; pt_hdr_load; pt_obj_load and its MTL): every seed file is
 // mutated many times (bytes flipped, cut short, spans duplicated or
 // dropped) and read back; a reader must return an error or a consistent
 // image / mesh.  Built by tests/test_io_fuzz.py with the address and
@@ -155,12 +155,19 @@ int main(int argc, char** argv) {
       return 2;
     }
     const bool obj = seed.size() > 4 && seed.compare(seed.size() - 4, 4, ".obj") == 0;
+    // a material library is mutated in place as <work dir>/fz.mtl and read
+    // through <work dir>/mtlref.obj, which names it
+    const bool mtl = seed.size() > 4 && seed.compare(seed.size() - 4, 4, ".mtl") == 0;
     const bool hdr = seed.size() > 4 && seed.compare(seed.size() - 4, 4, ".hdr") == 0;
     const std::string ext = seed.substr(seed.rfind('.'));
     for (int k = 0; k < muts; k++) {
-      const std::string path = dir + "/m" + std::to_string(a) + "_" + std::to_string(k % 4) + ext;
+      const std::string path =
+          mtl ? dir + "/fz.mtl" : dir + "/m" + std::to_string(a) + "_" + std::to_string(k % 4) + ext;
       write_file(path, k == 0 ? src : mutate(src));
-      bad += obj ? check_obj(path) : check_image(path, false);
+      if (mtl)
+        bad += check_obj(dir + "/mtlref.obj");
+      else
+        bad += obj ? check_obj(path) : check_image(path, false);
       if (hdr) bad += check_image(path, true);
       files++;
     }

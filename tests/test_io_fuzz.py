@@ -63,7 +63,8 @@ def seeds(d):
     p.write_text("P3 4 3 255\n" + " ".join(str(x) for x in px.reshape(-1)) + "\n")
     out.append(p)
     (d / "fz.mtl").write_text("newmtl red\nKa 0.8 0.1 0.1\nKd 0.5 0 0\nmap_Kd red.png\n"
-                              "newmtl blue\nKa 0.1 0.1 0.9\n")
+                              "newmtl blue\nKa 0.1 0.1 0.9\n# note\nnewmtl green\nKa 0 1 0\n")
+    out.append(d / "fz.mtl")
     p = d / "s.obj"
     p.write_text("mtllib fz.mtl\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nv 0.5 0.2 0\n"
                  "vt 0 0\nvt 1 0\nvt 1 1\nvt 0 1\nvn 0 0 1\n"
@@ -89,7 +90,8 @@ def test_readers_survive_malformed_files(tmp_path):
     work = tmp_path / "work"
     work.mkdir()
     files = seeds(tmp_path)
-    shutil.copy(tmp_path / "fz.mtl", work / "fz.mtl")
+    (work / "mtlref.obj").write_text("mtllib fz.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\nusemtl red\n"
+                                     "f 1 2 3\nusemtl green\nf 3 2 1\n")
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0",
                UBSAN_OPTIONS="print_stacktrace=1")
     run = subprocess.run([exe, str(work), str(MUTATIONS)] + [str(f) for f in files],

@@ -591,19 +591,20 @@ PT_API int pt_hdr_save(const char* path, int w, int h, const float* accum_rgba, 
 // ------------------------------------------------------------- PNG ----------
 namespace {
 
-uint32_t crc_table[256];
-bool crc_ready = false;
-
-uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
-  if (!crc_ready) {
+struct CrcTable {
+  uint32_t t[256];
+  CrcTable() {
     for (uint32_t i = 0; i < 256; i++) {
       uint32_t c = i;
       for (int k = 0; k < 8; k++) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-      crc_table[i] = c;
+      t[i] = c;
     }
-    crc_ready = true;
   }
-  for (size_t i = 0; i < n; i++) crc = crc_table[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
+};
+
+uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
+  static const CrcTable table;  // built once, safely under concurrent first calls
+  for (size_t i = 0; i < n; i++) crc = table.t[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
   return crc;
 }
 
